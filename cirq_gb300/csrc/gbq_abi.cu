@@ -1,0 +1,650 @@
+// C ABI of cirq_gb300 (declared in include/cirq_gb300.h).
+//
+// Host-side validation happens here, before any launch: every pass's tile
+// geometry and every op's bit positions are checked against the state width
+// so that no kernel can index outside its tile or its state.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "gbq_internal.cuh"
+
+namespace gbq {
+
+// implemented in gbq_kernels.cu
+int do_set_basis(Ctx* c, float2* s, int nbits, uint64_t index);
+int do_norm2(Ctx* c, const float2* s, int nbits, float scale, int use_scale, double* d_out);
+int do_scale(Ctx* c, float2* s, int nbits, float scale);
+int do_project(Ctx* c, float2* s, int nbits, uint64_t mask, uint64_t value, float scale);
+int do_probs(Ctx* c, const float2* s, int nq, int dm, float* out);
+int do_sample(Ctx* c, const float2* s, int nq, int dm, const double* d_u, int64_t R,
+              uint64_t* d_out, double* d_cdf);
+int do_expect(Ctx* c, const float2* s, int nbits, const gbq_pauli* d_terms, int nterms,
+              double* d_partial, double* d_out);
+int expect_chunk_bits(int nbits);
+int dm_expect_chunks(Ctx* c, int nq);
+int do_dm_expect(Ctx* c, const float2* rho, int nq, const gbq_pauli* d_terms, int nterms,
+                 double* d_partial, double* d_out);
+int do_apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* d_terms, int nterms,
+                      float2* out);
+int do_inner(Ctx* c, const float2* a, const float2* b, int nbits, double* d_out);
+int do_reduce_slots(Ctx* c, const double* partial, int nslots, int64_t ntiles, double* out);
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return e == cudaErrorMemoryAllocation ? GBQ_ERR_OOM : GBQ_ERR_CUDA;
+}
+
+static int arg_fail(const std::string& msg) {
+  g_err = msg;
+  return GBQ_ERR_ARG;
+}
+
+int ensure_scratch(Ctx* c, size_t bytes) {
+  if (c->scratch_bytes >= bytes) return GBQ_OK;
+  if (c->scratch) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+  }
+  const size_t want = bytes < 4096 ? 4096 : bytes;
+  cudaError_t e = cudaMalloc(&c->scratch, want);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+  c->scratch_bytes = want;
+  return GBQ_OK;
+}
+
+int ensure_host_scratch(Ctx* c, size_t bytes) {
+  if (c->host_scratch_bytes >= bytes) return GBQ_OK;
+  if (c->host_scratch) {
+    cudaStreamSynchronize(c->stream);
+    cudaFreeHost(c->host_scratch);
+    c->host_scratch = nullptr;
+    c->host_scratch_bytes = 0;
+  }
+  const size_t want = bytes < 4096 ? 4096 : bytes;
+  cudaError_t e = cudaMallocHost(&c->host_scratch, want);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost(scratch)");
+  c->host_scratch_bytes = want;
+  return GBQ_OK;
+}
+
+static int set_device(Ctx* c) {
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return GBQ_OK;
+}
+
+static int sync(Ctx* c, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return GBQ_OK;
+}
+
+// Validates one pass and its ops against a state of nbits bits; fills `ti`.
+static int build_tile_info(const gbq_pass& p, const gbq_op* ops, int nops, int nbits,
+                           bool dual, TileInfo& ti) {
+  if (p.L < 1 || p.L > GBQ_MAX_TILE_BITS || p.L > nbits)
+    return arg_fail("pass: tile bits L=" + std::to_string(p.L) + " invalid for " +
+                    std::to_string(nbits) + "-bit state");
+  if (p.m < 1 || p.m > p.L) return arg_fail("pass: contiguous bits m out of range");
+  if (p.op_count < 0 || p.op_count > GBQ_MAX_OPS_PER_PASS)
+    return arg_fail("pass: op_count out of range (max 64)");
+  if (p.op_begin < 0 || p.op_begin + p.op_count > nops) return arg_fail("pass: ops out of range");
+  uint64_t inmask = (p.m >= 64) ? ~0ull : ((1ull << p.m) - 1ull);
+  for (int j = 0; j < p.L - p.m; ++j) {
+    const int b = p.hi[j];
+    if (b < p.m || b >= nbits) return arg_fail("pass: tile high bit out of range");
+    if ((inmask >> b) & 1ull) return arg_fail("pass: duplicate tile bit");
+    inmask |= 1ull << b;
+  }
+  memset(&ti, 0, sizeof(ti));
+  ti.nbits = nbits;
+  ti.L = p.L;
+  ti.m = p.m;
+  ti.nops = p.op_count;
+  ti.ntiles = (int64_t)1 << (nbits - p.L);
+  for (int j = 0; j < 16; ++j) ti.hi[j] = p.hi[j];
+  int c = 0;
+  for (int b = 0; b < nbits; ++b)
+    if (!((inmask >> b) & 1ull)) ti.nt[c++] = (int8_t)b;
+  for (int o = 0; o < p.op_count; ++o) {
+    const gbq_op& op = ops[p.op_begin + o];
+    const bool dense = op.kind == GBQ_OP_DENSE || op.kind == GBQ_OP_PROBE;
+    const bool diag = op.kind == GBQ_OP_DIAG || op.kind == GBQ_OP_PROBE_DIAG;
+    if (!dense && !diag) return arg_fail("op: unknown kind");
+    if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && !dual)
+      return arg_fail("op: probe ops need a two-state pass");
+    if (op.mat < 0 || (op.mat & 1)) return arg_fail("op: matrix offset must be even and >= 0");
+    if (dense) {
+      const int kmax = op.kind == GBQ_OP_PROBE ? 3 : GBQ_MAX_DENSE_K;
+      if (op.k < 1 || op.k > kmax || op.k > p.L) return arg_fail("op: dense k out of range");
+      if (op.nsel < 0 || op.nsel > 3) return arg_fail("op: nsel out of range");
+      uint32_t used = 0;
+      for (int j = 0; j < op.k; ++j) {
+        if (op.bits[j] < 0 || op.bits[j] >= p.L || ((used >> op.bits[j]) & 1u))
+          return arg_fail("op: dense target bit invalid");
+        used |= 1u << op.bits[j];
+      }
+      for (int j = 0; j < p.L - op.k; ++j) {
+        if (op.gorder[j] < 0 || op.gorder[j] >= p.L || ((used >> op.gorder[j]) & 1u))
+          return arg_fail("op: group order invalid");
+        used |= 1u << op.gorder[j];
+      }
+      for (int j = 0; j < op.nsel; ++j) {
+        const int s = op.sel[j];
+        if (s >= 0) {
+          if (s >= p.L) return arg_fail("op: selector tile bit out of range");
+          for (int t = 0; t < op.k; ++t)
+            if (op.bits[t] == s) return arg_fail("op: selector bit is a target");
+        } else {
+          const int gb = -s - 1;
+          if (gb >= nbits || ((inmask >> gb) & 1ull))
+            return arg_fail("op: selector global bit invalid (must be outside the tile)");
+        }
+      }
+    } else {
+      if (op.k < 1 || op.k > GBQ_MAX_DIAG_K) return arg_fail("op: diag k out of range");
+      for (int j = 0; j < op.k; ++j) {
+        const int s = op.bits[j];
+        if (s >= 0) {
+          if (s >= p.L) return arg_fail("op: diag tile bit out of range");
+        } else {
+          const int gb = -s - 1;
+          if (gb >= nbits || ((inmask >> gb) & 1ull)) return arg_fail("op: diag global bit invalid");
+        }
+      }
+    }
+    if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && op.slot < 0)
+      return arg_fail("op: probe slot < 0");
+  }
+  return GBQ_OK;
+}
+
+static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pass* passes,
+                      int npasses, const gbq_op* ops, int nops, const float2* mats,
+                      double* partial) {
+  const bool dual = lam != nullptr;
+  PassArgs a;
+  for (int q = 0; q < npasses; ++q) {
+    memset(&a, 0, sizeof(a));
+    int rc = build_tile_info(passes[q], ops, nops, nbits, dual, a.ti);
+    if (rc) return rc;
+    a.psi = psi;
+    a.lam = lam;
+    a.ti.mats = mats;
+    a.ti.partial = partial;
+    memcpy(a.ops, ops + passes[q].op_begin, sizeof(gbq_op) * passes[q].op_count);
+    rc = launch_pass(c, a, dual);
+    if (rc) return rc;
+  }
+  return GBQ_OK;
+}
+
+}  // namespace gbq
+
+using namespace gbq;
+
+#define CHECK_CTX(c)                                   \
+  do {                                                 \
+    if (!(c)) return arg_fail("null context");         \
+    int _rc = set_device(c);                           \
+    if (_rc) return _rc;                               \
+  } while (0)
+
+extern "C" {
+
+const char* gbq_last_error(void) { return g_err.c_str(); }
+
+int gbq_version(void) { return 1; }
+
+int gbq_struct_sizes(int* op, int* pass, int* pauli, int* point) {
+  if (op) *op = (int)sizeof(gbq_op);
+  if (pass) *pass = (int)sizeof(gbq_pass);
+  if (pauli) *pauli = (int)sizeof(gbq_pauli);
+  if (point) *point = (int)sizeof(gbq_point);
+  return GBQ_OK;
+}
+
+int gbq_ctx_create(int device, gbq_ctx** out) {
+  if (!out) return arg_fail("null output pointer");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= ndev) return arg_fail("device index out of range");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  gbq_ctx* c = new gbq_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(e, "cudaDeviceGetAttribute");
+  }
+  *out = c;
+  return GBQ_OK;
+}
+
+int gbq_ctx_destroy(gbq_ctx* c) {
+  if (!c) return GBQ_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->host_scratch) cudaFreeHost(c->host_scratch);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return GBQ_OK;
+}
+
+int gbq_ctx_sync(gbq_ctx* c) {
+  CHECK_CTX(c);
+  return sync(c, "gbq_ctx_sync");
+}
+
+int gbq_device_info(gbq_ctx* c, int* sm_count, size_t* free_bytes, size_t* total_bytes) {
+  CHECK_CTX(c);
+  if (sm_count) *sm_count = c->sm_count;
+  size_t f = 0, t = 0;
+  cudaError_t e = cudaMemGetInfo(&f, &t);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return GBQ_OK;
+}
+
+int gbq_set_graphs(gbq_ctx* c, int enable) {
+  if (!c) return arg_fail("null context");
+  c->use_graphs = enable != 0;
+  return GBQ_OK;
+}
+
+int gbq_launch_count(gbq_ctx* c, int64_t* out) {
+  if (!c || !out) return arg_fail("null argument");
+  *out = c->launches;
+  return GBQ_OK;
+}
+
+int gbq_alloc(gbq_ctx* c, size_t bytes, void** dptr) {
+  CHECK_CTX(c);
+  if (!dptr) return arg_fail("null output pointer");
+  cudaError_t e = cudaMalloc(dptr, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    *dptr = nullptr;
+    return cuda_fail(e, "cudaMalloc");
+  }
+  return GBQ_OK;
+}
+
+int gbq_free(gbq_ctx* c, void* dptr) {
+  CHECK_CTX(c);
+  if (!dptr) return GBQ_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaError_t e = cudaFree(dptr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
+  return GBQ_OK;
+}
+
+int gbq_host_alloc(size_t bytes, void** hptr) {
+  if (!hptr) return arg_fail("null output pointer");
+  cudaError_t e = cudaMallocHost(hptr, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    *hptr = nullptr;
+    return cuda_fail(e, "cudaMallocHost");
+  }
+  return GBQ_OK;
+}
+
+int gbq_host_free(void* hptr) {
+  if (!hptr) return GBQ_OK;
+  cudaError_t e = cudaFreeHost(hptr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFreeHost");
+  return GBQ_OK;
+}
+
+int gbq_h2d(gbq_ctx* c, void* dst, const void* src, size_t bytes) {
+  CHECK_CTX(c);
+  if (!bytes) return GBQ_OK;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+  // the caller may free or reuse `src` as soon as we return
+  return sync(c, "gbq_h2d");
+}
+
+int gbq_d2h(gbq_ctx* c, void* dst, const void* src, size_t bytes) {
+  CHECK_CTX(c);
+  if (!bytes) return GBQ_OK;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+  return sync(c, "gbq_d2h");
+}
+
+int gbq_sv_set_basis(gbq_ctx* c, gbq_c64* state, int nbits, uint64_t index) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_set_basis: bad state");
+  if (nbits < 64 && index >= (1ull << nbits)) return arg_fail("gbq_sv_set_basis: index out of range");
+  return do_set_basis(c, reinterpret_cast<float2*>(state), nbits, index);
+}
+
+int gbq_run(gbq_ctx* c, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
+            const gbq_op* ops, int nops, const gbq_c64* mats) {
+  CHECK_CTX(c);
+  if (!state || nbits < 1 || nbits > 40) return arg_fail("gbq_run: bad state");
+  if (npasses < 0 || (npasses && (!passes || !ops || !mats))) return arg_fail("gbq_run: null program");
+  return run_passes(c, reinterpret_cast<float2*>(state), nullptr, nbits, passes, npasses, ops, nops,
+                    reinterpret_cast<const float2*>(mats), nullptr);
+}
+
+int gbq_run_dual(gbq_ctx* c, gbq_c64* psi, gbq_c64* lam, int nbits, const gbq_pass* passes,
+                 int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, double* partial) {
+  CHECK_CTX(c);
+  if (!psi || !lam || nbits < 1 || nbits > 40) return arg_fail("gbq_run_dual: bad states");
+  if (npasses < 0 || (npasses && (!passes || !ops || !mats))) return arg_fail("gbq_run_dual: null program");
+  for (int q = 0; q < npasses; ++q)
+    for (int o = 0; o < passes[q].op_count; ++o) {
+      const int idx = passes[q].op_begin + o;
+      if (idx < 0 || idx >= nops) return arg_fail("gbq_run_dual: op index out of range");
+      const int k = ops[idx].kind;
+      if ((k == GBQ_OP_PROBE || k == GBQ_OP_PROBE_DIAG) && !partial)
+        return arg_fail("gbq_run_dual: probe ops need a partial buffer");
+    }
+  return run_passes(c, reinterpret_cast<float2*>(psi), reinterpret_cast<float2*>(lam), nbits,
+                    passes, npasses, ops, nops, reinterpret_cast<const float2*>(mats), partial);
+}
+
+int gbq_reduce_slots(gbq_ctx* c, const double* partial, int nslots, int64_t ntiles, double* out) {
+  CHECK_CTX(c);
+  if (nslots <= 0) return GBQ_OK;
+  if (!partial || !out || ntiles < 1) return arg_fail("gbq_reduce_slots: bad arguments");
+  return do_reduce_slots(c, partial, nslots, ntiles, out);
+}
+
+int gbq_sv_norm2(gbq_ctx* c, const gbq_c64* state, int nbits, double* out) {
+  CHECK_CTX(c);
+  if (!state || !out || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_norm2: bad arguments");
+  int rc = ensure_scratch(c, 64);
+  if (rc) return rc;
+  double* d = reinterpret_cast<double*>(c->scratch);
+  rc = do_norm2(c, reinterpret_cast<const float2*>(state), nbits, 1.f, 0, d);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync");
+  return sync(c, "gbq_sv_norm2");
+}
+
+int gbq_sv_scale(gbq_ctx* c, gbq_c64* state, int nbits, float scale) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_scale: bad arguments");
+  return do_scale(c, reinterpret_cast<float2*>(state), nbits, scale);
+}
+
+int gbq_sv_project(gbq_ctx* c, gbq_c64* state, int nbits, uint64_t mask, uint64_t value,
+                   float scale) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_project: bad arguments");
+  return do_project(c, reinterpret_cast<float2*>(state), nbits, mask, value, scale);
+}
+
+int gbq_sv_final_renormalize(gbq_ctx* c, gbq_c64* state, int nbits, int* applied) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_final_renormalize: bad arguments");
+  if (applied) *applied = 0;
+  double n2 = 0.0;
+  int rc = gbq_sv_norm2(c, state, nbits, &n2);
+  if (rc) return rc;
+  const double norm = sqrt(n2);
+  const double tol = 3.4526698e-4;  // sqrt(float32 eps), the reference's threshold
+  if (fabs(norm - 1.0) > tol || norm == 0.0) return GBQ_OK;
+  const float inv = (float)(1.0 / norm);
+  double* d = reinterpret_cast<double*>(c->scratch);
+  rc = do_norm2(c, reinterpret_cast<const float2*>(state), nbits, inv, 1, d);
+  if (rc) return rc;
+  double n2s = 0.0;
+  cudaError_t e = cudaMemcpyAsync(&n2s, d, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync");
+  rc = sync(c, "gbq_sv_final_renormalize");
+  if (rc) return rc;
+  if (fabs(n2s - 1.0) - fabs(n2 - 1.0) < 0) {
+    rc = do_scale(c, reinterpret_cast<float2*>(state), nbits, inv);
+    if (rc) return rc;
+    if (applied) *applied = 1;
+  }
+  return GBQ_OK;
+}
+
+int gbq_probabilities(gbq_ctx* c, const gbq_c64* state, int nbits, int dm, float* out) {
+  CHECK_CTX(c);
+  if (!state || !out || nbits < 0 || nbits > 40) return arg_fail("gbq_probabilities: bad arguments");
+  return do_probs(c, reinterpret_cast<const float2*>(state), nbits, dm, out);
+}
+
+int gbq_sample(gbq_ctx* c, const gbq_c64* state, int nbits, int dm, const double* u, int64_t R,
+               uint64_t* out) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40 || R < 0 || (R && (!u || !out)))
+    return arg_fail("gbq_sample: bad arguments");
+  if (R == 0) return GBQ_OK;
+  const int bbits = nbits < 12 ? nbits : 12;
+  const int64_t nblocks = (int64_t)1 << (nbits - bbits);
+  const size_t need = (size_t)nblocks * 8 + (size_t)R * 8 + (size_t)R * 8 + 256;
+  int rc = ensure_scratch(c, need);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  double* d_cdf = reinterpret_cast<double*>(base);
+  double* d_u = reinterpret_cast<double*>(base + (size_t)nblocks * 8);
+  uint64_t* d_out = reinterpret_cast<uint64_t*>(base + (size_t)nblocks * 8 + (size_t)R * 8);
+  cudaError_t e = cudaMemcpyAsync(d_u, u, (size_t)R * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(uniforms)");
+  rc = do_sample(c, reinterpret_cast<const float2*>(state), nbits, dm, d_u, R, d_out, d_cdf);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, (size_t)R * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(samples)");
+  return sync(c, "gbq_sample");
+}
+
+static int validate_terms(const gbq_pauli* terms, int nterms, int nbits) {
+  if (nterms < 0 || (nterms && !terms)) return arg_fail("pauli terms: bad arguments");
+  const uint64_t mask = nbits >= 64 ? ~0ull : ((1ull << nbits) - 1ull);
+  for (int t = 0; t < nterms; ++t)
+    if ((terms[t].x & ~mask) || (terms[t].zy & ~mask))
+      return arg_fail("pauli term acts on a qubit outside the state");
+  return GBQ_OK;
+}
+
+int gbq_sv_expect_paulis(gbq_ctx* c, const gbq_c64* state, int nbits, const gbq_pauli* terms,
+                         int nterms, double* out) {
+  CHECK_CTX(c);
+  if (!state || nbits < 0 || nbits > 40 || (nterms && !out)) return arg_fail("gbq_sv_expect_paulis: bad arguments");
+  int rc = validate_terms(terms, nterms, nbits);
+  if (rc || nterms == 0) return rc;
+  const int cbits = expect_chunk_bits(nbits);
+  const int64_t nchunks = (int64_t)1 << (nbits - cbits);
+  const size_t tbytes = (size_t)nterms * sizeof(gbq_pauli);
+  const size_t pbytes = (size_t)nterms * nchunks * 2 * sizeof(double);
+  const size_t obytes = (size_t)nterms * 2 * sizeof(double);
+  rc = ensure_scratch(c, tbytes + pbytes + obytes + 512);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(base);
+  double* d_partial = reinterpret_cast<double*>(base + ((tbytes + 255) & ~(size_t)255));
+  double* d_out = reinterpret_cast<double*>(base + ((tbytes + 255) & ~(size_t)255) + pbytes);
+  cudaError_t e = cudaMemcpyAsync(d_terms, terms, tbytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
+  rc = do_expect(c, reinterpret_cast<const float2*>(state), nbits, d_terms, nterms, d_partial, d_out);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(expectations)");
+  rc = sync(c, "gbq_sv_expect_paulis");
+  if (rc) return rc;
+  for (int t = 0; t < nterms; ++t) {
+    // multiply by coef * i^ny
+    double re = out[2 * t], im = out[2 * t + 1];
+    const int ny = terms[t].ny & 3;
+    double r2 = re, i2 = im;
+    if (ny == 1) { r2 = -im; i2 = re; }
+    else if (ny == 2) { r2 = -re; i2 = -im; }
+    else if (ny == 3) { r2 = im; i2 = -re; }
+    out[2 * t] = terms[t].coef * r2;
+    out[2 * t + 1] = terms[t].coef * i2;
+  }
+  return GBQ_OK;
+}
+
+int gbq_dm_expect_paulis(gbq_ctx* c, const gbq_c64* rho, int nbits, const gbq_pauli* terms,
+                         int nterms, double* out) {
+  CHECK_CTX(c);
+  if (!rho || nbits < 0 || nbits > 20 || (nterms && !out)) return arg_fail("gbq_dm_expect_paulis: bad arguments");
+  int rc = validate_terms(terms, nterms, nbits);
+  if (rc || nterms == 0) return rc;
+  const int chunks = dm_expect_chunks(c, nbits);
+  const size_t tbytes = (size_t)nterms * sizeof(gbq_pauli);
+  const size_t pbytes = (size_t)nterms * chunks * 2 * sizeof(double);
+  const size_t obytes = (size_t)nterms * 2 * sizeof(double);
+  rc = ensure_scratch(c, tbytes + pbytes + obytes + 512);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(base);
+  double* d_partial = reinterpret_cast<double*>(base + ((tbytes + 255) & ~(size_t)255));
+  double* d_out = reinterpret_cast<double*>(base + ((tbytes + 255) & ~(size_t)255) + pbytes);
+  cudaError_t e = cudaMemcpyAsync(d_terms, terms, tbytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
+  rc = do_dm_expect(c, reinterpret_cast<const float2*>(rho), nbits, d_terms, nterms, d_partial, d_out);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, obytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(expectations)");
+  rc = sync(c, "gbq_dm_expect_paulis");
+  if (rc) return rc;
+  for (int t = 0; t < nterms; ++t) {
+    double re = out[2 * t], im = out[2 * t + 1];
+    const int ny = terms[t].ny & 3;
+    double r2 = re, i2 = im;
+    if (ny == 1) { r2 = -im; i2 = re; }
+    else if (ny == 2) { r2 = -re; i2 = -im; }
+    else if (ny == 3) { r2 = im; i2 = -re; }
+    out[2 * t] = terms[t].coef * r2;
+    out[2 * t + 1] = terms[t].coef * i2;
+  }
+  return GBQ_OK;
+}
+
+int gbq_sv_apply_paulisum(gbq_ctx* c, const gbq_c64* psi, int nbits, const gbq_pauli* terms,
+                          int nterms, gbq_c64* out) {
+  CHECK_CTX(c);
+  if (!psi || !out || psi == out || nbits < 0 || nbits > 40)
+    return arg_fail("gbq_sv_apply_paulisum: bad arguments (out must differ from psi)");
+  int rc = validate_terms(terms, nterms, nbits);
+  if (rc) return rc;
+  const size_t tbytes = (size_t)(nterms ? nterms : 1) * sizeof(gbq_pauli);
+  rc = ensure_scratch(c, tbytes);
+  if (rc) return rc;
+  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(c->scratch);
+  if (nterms) {
+    cudaError_t e = cudaMemcpyAsync(d_terms, terms, tbytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
+  }
+  rc = do_apply_paulisum(c, reinterpret_cast<const float2*>(psi), nbits, d_terms, nterms,
+                         reinterpret_cast<float2*>(out));
+  if (rc) return rc;
+  // terms live in the shared scratch buffer: finish before it can be reused
+  return sync(c, "gbq_sv_apply_paulisum");
+}
+
+int gbq_sv_inner(gbq_ctx* c, const gbq_c64* a, const gbq_c64* b, int nbits, double* out) {
+  CHECK_CTX(c);
+  if (!a || !b || !out || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_inner: bad arguments");
+  int rc = ensure_scratch(c, 64);
+  if (rc) return rc;
+  double* d = reinterpret_cast<double*>(c->scratch);
+  rc = do_inner(c, reinterpret_cast<const float2*>(a), reinterpret_cast<const float2*>(b), nbits, d);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(out, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync");
+  return sync(c, "gbq_sv_inner");
+}
+
+int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq_pass* passes,
+                     int npasses, const gbq_op* ops, int nops, const gbq_c64* mats,
+                     const gbq_pauli* terms, int nterms, int max_nbits, double* out) {
+  CHECK_CTX(c);
+  if (npoints < 0 || (npoints && (!points || !out))) return arg_fail("gbq_batch_expect: bad arguments");
+  if (npoints == 0) return GBQ_OK;
+  if (max_nbits < 1 || max_nbits > 30) return arg_fail("gbq_batch_expect: max_nbits out of range (1..30)");
+  if (!mats) return arg_fail("gbq_batch_expect: null matrix pool");
+  // validate every point's program on the host
+  TileInfo ti;
+  for (int p = 0; p < npoints; ++p) {
+    const gbq_point& pt = points[p];
+    if (pt.nbits < 1 || pt.nbits > max_nbits) return arg_fail("gbq_batch_expect: point width out of range");
+    if (pt.pass_begin < 0 || pt.pass_count < 0 || pt.pass_begin + pt.pass_count > npasses)
+      return arg_fail("gbq_batch_expect: point passes out of range");
+    if (pt.term_begin < 0 || pt.term_count < 0 || pt.term_begin + pt.term_count > nterms)
+      return arg_fail("gbq_batch_expect: point terms out of range");
+    if (pt.mat_base < 0 || (pt.mat_base & 1)) return arg_fail("gbq_batch_expect: mat_base must be even");
+    for (int q = 0; q < pt.pass_count; ++q) {
+      int rc = build_tile_info(passes[pt.pass_begin + q], ops, nops, pt.nbits, false, ti);
+      if (rc) return rc;
+    }
+    int rc = validate_terms(terms + pt.term_begin, pt.term_count, pt.nbits);
+    if (rc) return rc;
+  }
+  int nslots = c->sm_count * 2;
+  if (nslots > npoints) nslots = npoints;
+  const size_t slot_bytes = ((size_t)1 << max_nbits) * sizeof(float2);
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_points = al((size_t)npoints * sizeof(gbq_point));
+  const size_t b_passes = al((size_t)(npasses ? npasses : 1) * sizeof(gbq_pass));
+  const size_t b_ops = al((size_t)(nops ? nops : 1) * sizeof(gbq_op));
+  const size_t b_terms = al((size_t)(nterms ? nterms : 1) * sizeof(gbq_pauli));
+  const size_t b_out = al((size_t)npoints * 2 * sizeof(double));
+  const size_t b_counter = 256;
+  const size_t head = b_points + b_passes + b_ops + b_terms + b_out + b_counter;
+  int rc = ensure_scratch(c, head + slot_bytes * nslots);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  gbq_point* d_points = reinterpret_cast<gbq_point*>(base);
+  gbq_pass* d_passes = reinterpret_cast<gbq_pass*>(base + b_points);
+  gbq_op* d_ops = reinterpret_cast<gbq_op*>(base + b_points + b_passes);
+  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(base + b_points + b_passes + b_ops);
+  double* d_out = reinterpret_cast<double*>(base + b_points + b_passes + b_ops + b_terms);
+  int* d_counter = reinterpret_cast<int*>(base + b_points + b_passes + b_ops + b_terms + b_out);
+  float2* slots = reinterpret_cast<float2*>(base + head);
+  cudaError_t e;
+  e = cudaMemcpyAsync(d_points, points, (size_t)npoints * sizeof(gbq_point), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(points)");
+  if (npasses) {
+    e = cudaMemcpyAsync(d_passes, passes, (size_t)npasses * sizeof(gbq_pass), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(passes)");
+  }
+  if (nops) {
+    e = cudaMemcpyAsync(d_ops, ops, (size_t)nops * sizeof(gbq_op), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(ops)");
+  }
+  if (nterms) {
+    e = cudaMemcpyAsync(d_terms, terms, (size_t)nterms * sizeof(gbq_pauli), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
+  }
+  e = cudaMemsetAsync(d_counter, 0, sizeof(int), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(counter)");
+  rc = launch_batch(c, d_points, npoints, d_passes, d_ops, reinterpret_cast<const float2*>(mats),
+                    d_terms, max_nbits, slots, nslots, d_counter, d_out);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, (size_t)npoints * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(out)");
+  return sync(c, "gbq_batch_expect");
+}
+
+}  // extern "C"

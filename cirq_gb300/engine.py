@@ -1,0 +1,314 @@
+"""Python handle on the CUDA engine: contexts, device buffers and program runs.
+
+Everything here calls the C ABI of ``libcirq_gb300.so`` (include/cirq_gb300.h)
+through ctypes.  Device memory belongs to an :class:`Engine`; host arrays are
+numpy arrays owned by the caller.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+import weakref
+
+import numpy as np
+
+from cirq_gb300 import _lib
+from cirq_gb300._lib import check
+
+
+class DeviceBuffer:
+    """A device allocation owned by an Engine (freed when garbage-collected)."""
+
+    def __init__(self, engine: "Engine", nbytes: int):
+        self.engine = engine
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        check(engine.lib.gbq_alloc(engine.ctx, self.nbytes, ctypes.byref(p)), "gbq_alloc")
+        self.ptr = p.value
+        self._fin = weakref.finalize(self, Engine._free, engine.lib, engine.ctx, self.ptr)
+
+    def free(self) -> None:
+        self._fin()
+
+    def upload(self, host: np.ndarray) -> None:
+        host = np.ascontiguousarray(host)
+        if host.nbytes > self.nbytes:
+            raise ValueError("upload larger than the device buffer")
+        check(self.engine.lib.gbq_h2d(self.engine.ctx, self.ptr, host.ctypes.data, host.nbytes), "gbq_h2d")
+
+    def download(self, host: np.ndarray) -> np.ndarray:
+        if not host.flags.c_contiguous or host.nbytes > self.nbytes:
+            raise ValueError("bad host buffer")
+        check(self.engine.lib.gbq_d2h(self.engine.ctx, host.ctypes.data, self.ptr, host.nbytes), "gbq_d2h")
+        return host
+
+
+class PinnedArrayPool:
+    """Reusable pinned host buffers handed out as numpy arrays.
+
+    Device->host copies of large states run at full link speed only into
+    page-locked memory; pinning is slow, so buffers are recycled when the
+    numpy array that owns one is garbage-collected."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.free: dict[int, list[int]] = {}
+        self.lock = threading.Lock()
+
+    def array(self, shape, dtype) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        with self.lock:
+            lst = self.free.get(nbytes)
+            p = lst.pop() if lst else None
+        if p is None:
+            hp = ctypes.c_void_p()
+            check(self.lib.gbq_host_alloc(nbytes, ctypes.byref(hp)), "gbq_host_alloc")
+            p = hp.value
+        raw = (ctypes.c_char * nbytes).from_address(p)
+        arr = np.frombuffer(raw, dtype=dtype).reshape(shape)
+        pool = self
+
+        class _Owner:
+            pass
+
+        owner = _Owner()
+        weakref.finalize(owner, pool._release, nbytes, p)
+        # keep the owner alive as long as the array (and its views) live
+        arr = _OwnedArray(arr, owner)
+        return arr
+
+    def _release(self, nbytes, p):
+        with self.lock:
+            self.free.setdefault(nbytes, []).append(p)
+
+
+class _OwnedArray(np.ndarray):
+    def __new__(cls, arr, owner):
+        obj = arr.view(cls)
+        obj._owner = owner
+        return obj
+
+    def __array_finalize__(self, obj):
+        if obj is not None:
+            self._owner = getattr(obj, "_owner", None)
+
+
+class Engine:
+    """One CUDA context (device + stream) of the engine."""
+
+    _instances: dict[int, "Engine"] = {}
+    _lock = threading.Lock()
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        ctx = ctypes.c_void_p()
+        check(self.lib.gbq_ctx_create(int(device), ctypes.byref(ctx)), "gbq_ctx_create")
+        self.ctx = ctx.value
+        self.device = device
+        sm = ctypes.c_int()
+        free = ctypes.c_size_t()
+        total = ctypes.c_size_t()
+        check(self.lib.gbq_device_info(self.ctx, ctypes.byref(sm), ctypes.byref(free), ctypes.byref(total)))
+        self.sm_count = sm.value
+        self.total_bytes = total.value
+        self.pinned = PinnedArrayPool(self.lib)
+        self._pool_cache: dict = {}
+
+    @classmethod
+    def get(cls, device: int = 0) -> "Engine":
+        with cls._lock:
+            eng = cls._instances.get(device)
+            if eng is None:
+                eng = cls(device)
+                cls._instances[device] = eng
+            return eng
+
+    @staticmethod
+    def _free(lib, ctx, ptr):
+        try:
+            lib.gbq_free(ctx, ptr)
+        except Exception:
+            pass
+
+    # ---- buffers -------------------------------------------------------
+    def alloc(self, nbytes: int) -> DeviceBuffer:
+        return DeviceBuffer(self, nbytes)
+
+    def upload(self, host: np.ndarray) -> DeviceBuffer:
+        host = np.ascontiguousarray(host)
+        buf = self.alloc(max(host.nbytes, 16))
+        buf.upload(host)
+        return buf
+
+    def sync(self) -> None:
+        check(self.lib.gbq_ctx_sync(self.ctx), "gbq_ctx_sync")
+
+    def launches(self) -> int:
+        v = ctypes.c_int64()
+        check(self.lib.gbq_launch_count(self.ctx, ctypes.byref(v)))
+        return v.value
+
+    # ---- state vectors -------------------------------------------------
+    def new_state(self, nbits: int, basis: int = 0, initial: np.ndarray | None = None) -> DeviceBuffer:
+        buf = self.alloc(8 * (1 << nbits))
+        if initial is not None:
+            arr = np.ascontiguousarray(np.asarray(initial, dtype=np.complex64).reshape(-1))
+            if arr.size != 1 << nbits:
+                raise ValueError(f"initial state has {arr.size} amplitudes, expected {1 << nbits}")
+            buf.upload(arr)
+        else:
+            check(self.lib.gbq_sv_set_basis(self.ctx, buf.ptr, nbits, int(basis)), "gbq_sv_set_basis")
+        return buf
+
+    def run(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer | None = None) -> None:
+        if plan.npasses == 0:
+            return
+        if pool_dev is None:
+            pool_dev = self.upload(plan.pool)
+        check(
+            self.lib.gbq_run(
+                self.ctx,
+                state.ptr,
+                nbits,
+                plan.passes.ctypes.data,
+                len(plan.passes),
+                plan.ops.ctypes.data,
+                len(plan.ops),
+                pool_dev.ptr,
+            ),
+            "gbq_run",
+        )
+        # keep the pool alive until the stream has consumed it
+        self.sync()
+
+    def run_dual(self, psi, lam, nbits, plan, pool_dev, partial) -> None:
+        if plan.npasses == 0:
+            return
+        check(
+            self.lib.gbq_run_dual(
+                self.ctx,
+                psi.ptr,
+                lam.ptr,
+                nbits,
+                plan.passes.ctypes.data,
+                len(plan.passes),
+                plan.ops.ctypes.data,
+                len(plan.ops),
+                pool_dev.ptr,
+                partial.ptr if partial is not None else None,
+            ),
+            "gbq_run_dual",
+        )
+
+    def norm2(self, state: DeviceBuffer, nbits: int) -> float:
+        v = ctypes.c_double()
+        check(self.lib.gbq_sv_norm2(self.ctx, state.ptr, nbits, ctypes.byref(v)), "gbq_sv_norm2")
+        return v.value
+
+    def final_renormalize(self, state: DeviceBuffer, nbits: int) -> bool:
+        v = ctypes.c_int()
+        check(self.lib.gbq_sv_final_renormalize(self.ctx, state.ptr, nbits, ctypes.byref(v)))
+        return bool(v.value)
+
+    def scale(self, state: DeviceBuffer, nbits: int, factor: float) -> None:
+        check(self.lib.gbq_sv_scale(self.ctx, state.ptr, nbits, ctypes.c_float(factor)))
+
+    def project(self, state, nbits, mask, value, scale) -> None:
+        check(self.lib.gbq_sv_project(self.ctx, state.ptr, nbits, int(mask), int(value), ctypes.c_float(scale)))
+
+    def download_state(self, state: DeviceBuffer, nbits: int, pinned: bool = True) -> np.ndarray:
+        n = 1 << nbits
+        if pinned and n >= (1 << 16):
+            out = self.pinned.array((n,), np.complex64)
+        else:
+            out = np.empty(n, dtype=np.complex64)
+        check(self.lib.gbq_d2h(self.ctx, out.ctypes.data, state.ptr, out.nbytes), "gbq_d2h")
+        return out
+
+    def sample(self, state: DeviceBuffer, nbits: int, uniforms: np.ndarray, dm: bool = False) -> np.ndarray:
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        out = np.empty(u.size, dtype=np.uint64)
+        check(
+            self.lib.gbq_sample(self.ctx, state.ptr, nbits, int(dm), u.ctypes.data, u.size, out.ctypes.data),
+            "gbq_sample",
+        )
+        return out
+
+    def probabilities(self, state: DeviceBuffer, nbits: int, dm: bool = False) -> np.ndarray:
+        buf = self.alloc(4 * (1 << nbits))
+        check(self.lib.gbq_probabilities(self.ctx, state.ptr, nbits, int(dm), buf.ptr), "gbq_probabilities")
+        out = np.empty(1 << nbits, dtype=np.float32)
+        return buf.download(out)
+
+    @staticmethod
+    def pauli_records(terms) -> np.ndarray:
+        rec = np.zeros(len(terms), dtype=_lib.PAULI_DTYPE)
+        for i, (x, zy, ny, coef) in enumerate(terms):
+            rec[i]["x"] = x
+            rec[i]["zy"] = zy
+            rec[i]["ny"] = ny
+            rec[i]["coef"] = float(np.real(coef))
+        return rec
+
+    def expect_paulis(self, state, nbits, terms, dm: bool = False) -> np.ndarray:
+        """Per-term complex values coef * <P> (terms from ir.pauli_terms).
+
+        Complex coefficients are handled by evaluating the unit string and
+        multiplying on the host."""
+        if not terms:
+            return np.zeros(0, dtype=np.complex128)
+        unit = [(x, zy, ny, 1.0) for x, zy, ny, _ in terms]
+        rec = self.pauli_records(unit)
+        out = np.zeros(2 * len(terms), dtype=np.float64)
+        fn = self.lib.gbq_dm_expect_paulis if dm else self.lib.gbq_sv_expect_paulis
+        check(fn(self.ctx, state.ptr, nbits, rec.ctypes.data, len(rec), out.ctypes.data), "expect_paulis")
+        vals = out[0::2] + 1j * out[1::2]
+        return vals * np.array([c for *_, c in terms], dtype=np.complex128)
+
+    def apply_paulisum(self, psi, nbits, terms, out) -> None:
+        rec = self.pauli_records(terms)
+        for t in terms:
+            if abs(np.imag(t[3])) > 0:
+                raise NotImplementedError("apply_paulisum needs real coefficients")
+        check(
+            self.lib.gbq_sv_apply_paulisum(self.ctx, psi.ptr, nbits, rec.ctypes.data, len(rec), out.ptr),
+            "gbq_sv_apply_paulisum",
+        )
+
+    def inner(self, a, b, nbits) -> complex:
+        out = np.zeros(2, dtype=np.float64)
+        check(self.lib.gbq_sv_inner(self.ctx, a.ptr, b.ptr, nbits, out.ctypes.data), "gbq_sv_inner")
+        return complex(out[0], out[1])
+
+    def reduce_slots(self, partial, nslots, ntiles, out) -> None:
+        check(self.lib.gbq_reduce_slots(self.ctx, partial.ptr, nslots, int(ntiles), out.ptr), "gbq_reduce_slots")
+
+    def batch_expect(self, points, passes, ops, pool_dev, terms, max_nbits) -> np.ndarray:
+        out = np.zeros(2 * len(points), dtype=np.float64)
+        check(
+            self.lib.gbq_batch_expect(
+                self.ctx,
+                points.ctypes.data,
+                len(points),
+                passes.ctypes.data,
+                len(passes),
+                ops.ctypes.data,
+                len(ops),
+                pool_dev.ptr,
+                terms.ctypes.data,
+                len(terms),
+                int(max_nbits),
+                out.ctypes.data,
+            ),
+            "gbq_batch_expect",
+        )
+        return out[0::2] + 1j * out[1::2]
+
+
+def default_engine(device: int | None = None) -> Engine:
+    if device is None:
+        device = int(os.environ.get("CIRQ_GB300_DEVICE", "0"))
+    return Engine.get(device)

@@ -1,0 +1,587 @@
+"""Host planner: groups gates into tile passes and fuses them into k-qubit blocks.
+
+Input: a list of :class:`cirq_gb300.ir.BitGate` over an ``nbits``-bit vector.
+Output: a :class:`Plan` -- the ``gbq_pass`` / ``gbq_op`` arrays of the C ABI
+plus a pool of complex64 matrices.
+
+One pass = one read + one write of the state.  A pass owns a set S of L
+"tile" index bits (always including the low ``m`` bits, so loads stay
+contiguous).  Walking the gates in circuit order, a gate joins the pass when
+every earlier gate it does not commute with has joined too, and, if it is not
+diagonal, its bits fit in S.  Diagonal gates never need their bits in S: a
+bit outside S is constant over a tile, so its value just selects which of
+2^nsel precomputed matrices a dense op uses (``gbq_op.sel``).
+
+Inside a pass gates are fused greedily (qsim-style) into dense ops on at most
+``kmax`` bits or diagonal tables on at most 8 bits.  A pass stops growing when
+its estimated arithmetic (sum of 2^k complex multiply-adds per amplitude plus
+a per-op overhead) reaches ``budget``: beyond that the pass would be
+compute-bound rather than HBM-bound.
+
+Every fused op records a *recipe* (the sequence of embed/multiply steps), so
+the matrices of a plan can be recomputed for a batch of parameter points with
+vectorised numpy, without re-planning (``Plan.pool_for``).
+
+The reference's own fusion (``merge_k_qubit_unitaries``,
+``cirq-core/cirq/transformers/merge_k_qubit_gates.py:71-140``) only merges
+nested qubit sets; this planner grows genuine k-bit blocks instead.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Sequence
+
+import numpy as np
+
+from cirq_gb300 import _lib
+from cirq_gb300.ir import BitGate
+
+# Swizzle column vectors of tile bits 4..13 (must match gbq_tile.cu kSwzV).
+SWZ_V = (3, 5, 6, 9, 10, 12, 7, 11, 13, 14)
+
+MAX_OPS = 64
+MAX_DIAG_BITS = 8
+MAX_SEL = 3
+
+
+def swz_vec(tile_bit: int) -> int:
+    return 1 << tile_bit if tile_bit < 4 else SWZ_V[tile_bit - 4]
+
+
+def group_order(L: int, targets: Sequence[int]) -> list[int]:
+    """Tile bits of the group index: 4 bank-independent lane bits first."""
+    free = [b for b in range(L) if b not in targets]
+    lanes: list[int] = []
+    basis: list[int] = []  # GF(2) basis, reduced
+    for b in free:
+        v = swz_vec(b)
+        for e in basis:
+            v = min(v, v ^ e)
+        if v:
+            basis.append(v)
+            basis.sort(reverse=True)
+            lanes.append(b)
+            if len(lanes) == 4:
+                break
+    rest = [b for b in free if b not in lanes]
+    return lanes + rest
+
+
+# ---------------------------------------------------------------- fused ops
+@dataclasses.dataclass
+class _Dense:
+    tg: list  # global bits, matrix bit j <-> tg[j]
+    sl: list  # global bits, selector bit j <-> sl[j]
+    M: np.ndarray  # (P, 2^nsel, 2^k, 2^k)
+    recipe: list
+
+    kind = "dense"
+
+    def touches(self):
+        return set(self.tg) | set(self.sl)
+
+    def cost(self, ovh):
+        return 2 ** len(self.tg) + ovh
+
+
+@dataclasses.dataclass
+class _Diag:
+    bits: list  # global bits, table bit j <-> bits[j]
+    d: np.ndarray  # (P, 2^b)
+    recipe: list
+
+    kind = "diag"
+
+    def touches(self):
+        return set(self.bits)
+
+    def cost(self, ovh):
+        return 1 + ovh
+
+
+def _sub_index(size_bits: int, pos: Sequence[int]) -> tuple[np.ndarray, np.ndarray]:
+    idx = np.arange(2**size_bits)
+    sub = np.zeros_like(idx)
+    mask = 0
+    for i, p in enumerate(pos):
+        sub |= ((idx >> p) & 1) << i
+        mask |= 1 << p
+    return sub, idx & ~mask
+
+
+def _expand(G: np.ndarray, pos: Sequence[int], k: int) -> np.ndarray:
+    """(P, 2^kg, 2^kg) gate on target positions `pos` -> (P, 2^k, 2^k)."""
+    sub, rest = _sub_index(k, pos)
+    same = rest[:, None] == rest[None, :]
+    return G[:, sub[:, None], sub[None, :]] * same
+
+
+def _diag_index(nsel: int, k: int, tpos, spos) -> np.ndarray:
+    """Gate sub-index for every (selector value, target index): shape (2^nsel, 2^k)."""
+    s = np.arange(2**nsel)[:, None]
+    t = np.arange(2**k)[None, :]
+    sub = np.zeros((2**nsel, 2**k), dtype=np.int64)
+    for j, (tp, sp) in enumerate(zip(tpos, spos)):
+        if tp is not None:
+            sub = sub | (((t >> tp) & 1) << j)
+        else:
+            sub = sub | (((s >> sp) & 1) << j)
+    return sub
+
+
+class _Replayer:
+    """Applies recipe steps to batched matrices (shared by planning and replay)."""
+
+    @staticmethod
+    def dense_step(M: np.ndarray, step, gates: dict) -> np.ndarray:
+        kind = step[0]
+        P, ns, d, _ = M.shape
+        if kind == "tx":  # add `n` identity target bits (new highest bits)
+            n = step[1]
+            eye = np.eye(2**n, dtype=M.dtype)
+            return np.einsum("ab,psij->psaibj", eye, M).reshape(P, ns, d * 2**n, d * 2**n)
+        if kind == "sx":  # add `n` selector bits (new highest selector bits)
+            n = step[1]
+            return np.concatenate([M] * (2**n), axis=1)
+        if kind == "s2t":  # selector i becomes the new highest target bit
+            i = step[1]
+            sidx = np.arange(ns)
+            keep = sidx[((sidx >> i) & 1) == 0]
+            lo = ((keep & ((1 << i) - 1)) | ((keep >> (i + 1)) << i))
+            order = np.argsort(lo)
+            keep = keep[order]
+            out = np.zeros((P, ns // 2, 2 * d, 2 * d), dtype=M.dtype)
+            out[:, :, :d, :d] = M[:, keep]
+            out[:, :, d:, d:] = M[:, keep | (1 << i)]
+            return out
+        if kind == "mul":  # left-multiply a non-diagonal gate on target positions
+            _, gi, pos = step
+            k = int(np.log2(d))
+            F = _expand(gates[gi], pos, k)  # (P, d, d)
+            return np.einsum("pij,psjk->psik", F, M)
+        if kind == "dmul":  # row-scale by a diagonal gate over (targets, selectors)
+            _, gi, tpos, spos = step
+            k = int(np.log2(d))
+            nsel = int(np.log2(ns))
+            dg = np.diagonal(gates[gi], axis1=1, axis2=2)  # (P, 2^kg)
+            sub = _diag_index(nsel, k, tpos, spos)  # (ns, d)
+            return dg[:, sub][..., None] * M
+        raise ValueError(step)
+
+    @staticmethod
+    def diag_step(D: np.ndarray, step, gates: dict) -> np.ndarray:
+        kind = step[0]
+        if kind == "dx":
+            n = step[1]
+            return np.concatenate([D] * (2**n), axis=1)
+        if kind == "dd":
+            _, gi, pos = step
+            b = int(np.log2(D.shape[1]))
+            dg = np.diagonal(gates[gi], axis1=1, axis2=2)
+            sub, _ = _sub_index(b, pos)
+            return D * dg[:, sub]
+        raise ValueError(step)
+
+
+@dataclasses.dataclass
+class PassPlan:
+    L: int
+    m: int
+    hi: list
+    ops: list  # _Dense / _Diag
+
+
+@dataclasses.dataclass
+class Plan:
+    """A planned program: passes, ops and the matrix pool (complex64)."""
+
+    nbits: int
+    passes: np.ndarray
+    ops: np.ndarray
+    pool: np.ndarray  # complex64 (pool_len,) for the planning point
+    pass_plans: list
+    ngates: int
+    # op index -> (kind, recipe, pool offset, shape) for replay
+    layout: list
+    pool_len: int
+
+    @property
+    def npasses(self) -> int:
+        return len(self.passes)
+
+    def cost(self) -> float:
+        """Estimated complex MACs per amplitude summed over all passes."""
+        tot = 0.0
+        for pp in self.pass_plans:
+            for op in pp.ops:
+                tot += op.cost(0.0)
+        return tot
+
+    def pool_for(self, gates: dict, npoints: int) -> np.ndarray:
+        """Recomputes the matrix pool for a batch: gates[gi] is (P, d, d).
+
+        Returns complex64 (P, pool_len).
+        """
+        out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
+        for kind, recipe, off, shape in self.layout:
+            if kind == "dense":
+                ns, d = shape
+                M = np.broadcast_to(np.eye(1, dtype=np.complex128), (npoints, 1, 1, 1)).copy()
+                for step in recipe:
+                    M = _Replayer.dense_step(M, step, gates)
+                out[:, off : off + ns * d * d] = M.reshape(npoints, -1)
+            else:
+                (b,) = shape
+                D = np.ones((npoints, 1), dtype=np.complex128)
+                for step in recipe:
+                    D = _Replayer.diag_step(D, step, gates)
+                out[:, off : off + 2**b] = D
+        return out
+
+
+class Planner:
+    """Greedy pass/fusion planner (see module docstring)."""
+
+    def __init__(
+        self,
+        tile_bits: int = 12,
+        low_bits: int = 5,
+        kmax: int = 4,
+        budget: float = 40.0,
+        op_overhead: float = 1.0,
+    ):
+        if not 1 <= kmax <= 5:
+            raise ValueError("fusion width kmax must be in 1..5")
+        if not 1 <= tile_bits <= 13:
+            raise ValueError("tile_bits must be in 1..13")
+        self.tile_bits = tile_bits
+        self.low_bits = low_bits
+        self.kmax = kmax
+        self.budget = budget
+        self.ovh = op_overhead
+
+    # ------------------------------------------------------------------
+    def plan(self, gates: Sequence[BitGate], nbits: int, batch: dict | None = None) -> Plan:
+        """Plans `gates`; `batch` optionally gives (P, d, d) matrices per gate index
+        (default: each gate's own matrix, P = 1)."""
+        if batch is None:
+            batch = {i: g.matrix[None] for i, g in enumerate(gates)}
+        L = min(self.tile_bits, nbits)
+        m = min(self.low_bits, L)
+        remaining = list(range(len(gates)))
+        pass_plans: list[PassPlan] = []
+        while remaining:
+            pp, remaining = self._one_pass(gates, remaining, nbits, L, m, batch)
+            pass_plans.append(pp)
+        return self._emit(pass_plans, nbits, len(gates))
+
+    def _one_pass(self, gates, remaining, nbits, L, m, batch):
+        S = set(range(m))
+        ops: list = []
+        last: dict = {}  # global bit -> index of latest op touching it
+        blocked_nd: set = set()
+        blocked_d: set = set()
+        cost = 0.0
+        taken: list = []
+        left: list = []
+        budget = self.budget if nbits > L else float("inf")
+        for gi in remaining:
+            g = gates[gi]
+            bits = g.bits
+            ok = all(b not in blocked_nd for b in bits) and (
+                g.diagonal or all(b not in blocked_d for b in bits)
+            )
+            if ok and len(ops) >= MAX_OPS:
+                ok = False
+            if ok and not g.diagonal:
+                need = [b for b in bits if b not in S]
+                if len(S) + len(need) > L:
+                    ok = False
+            if ok:
+                plan = self._fusion_choice(g, gi, ops, last, S if g.diagonal else S | set(bits))
+                delta = plan[0]
+                if taken and cost + delta > budget:
+                    ok = False
+            if not ok:
+                (blocked_d if g.diagonal else blocked_nd).update(bits)
+                left.append(gi)
+                continue
+            if not g.diagonal:
+                S.update(bits)
+            self._apply_fusion(plan, g, gi, ops, last, batch)
+            cost += delta
+            taken.append(gi)
+        # fill the tile to exactly L bits
+        b = 0
+        while len(S) < L:
+            if b not in S:
+                S.add(b)
+            b += 1
+        hi = sorted(x for x in S if x >= m)
+        # selectors/diag bits that ended up inside S are fine: codes are resolved at emit
+        return PassPlan(L=L, m=m, hi=hi, ops=ops), left
+
+    # ---- fusion decisions ------------------------------------------------
+    def _fusion_choice(self, g: BitGate, gi: int, ops, last, S):
+        """Returns (delta_cost, action...) for adding gate g to the pass."""
+        bits = list(g.bits)
+        c = max((last.get(b, -1) for b in bits), default=-1)
+        new_cost = (2 ** len(bits) if not g.diagonal else 1) + self.ovh
+        if not g.diagonal:
+            if c >= 0:
+                op = ops[c]
+                if op.kind == "dense":
+                    tg = list(op.tg)
+                    for b in bits:
+                        if b not in tg:
+                            tg.append(b)
+                    if len(tg) <= self.kmax:
+                        delta = 2 ** len(tg) - 2 ** len(op.tg)
+                        if delta < new_cost:
+                            return (delta, "merge_dense", c)
+                elif op.kind == "diag":
+                    loc = [b for b in op.bits if b in S]
+                    glob = [b for b in op.bits if b not in S]
+                    tg = list(loc)
+                    for b in bits:
+                        if b not in tg:
+                            tg.append(b)
+                    if len(tg) <= self.kmax and len(glob) <= MAX_SEL:
+                        delta = 2 ** len(tg) - op.cost(0)
+                        if delta < new_cost:
+                            return (delta, "diag_to_dense", c, loc, glob)
+            return (new_cost, "new_dense")
+        # diagonal gate: absorb into a dense op (targets/selectors) or a diag table
+        lo = max(c, 0)
+        best = None
+        for d in range(len(ops) - 1, lo - 1, -1):
+            op = ops[d]
+            if op.kind == "dense":
+                tg = list(op.tg)
+                sl = list(op.sl)
+                grow_t = []
+                grow_s = []
+                for b in bits:
+                    if b in tg or b in sl:
+                        continue
+                    if len(sl) + len(grow_s) < MAX_SEL:
+                        grow_s.append(b)
+                    elif b in S and len(tg) + len(grow_t) < self.kmax:
+                        grow_t.append(b)
+                    else:
+                        grow_s = None
+                        break
+                if grow_s is None:
+                    continue
+                delta = 2 ** (len(tg) + len(grow_t)) - 2 ** len(tg)
+                cand = (delta, "absorb_dense", d, grow_t, grow_s)
+            else:
+                ub = list(op.bits) + [b for b in bits if b not in op.bits]
+                if len(ub) > MAX_DIAG_BITS:
+                    continue
+                cand = (0.0, "absorb_diag", d)
+            if best is None or cand[0] < best[0]:
+                best = cand
+            if best[0] == 0:
+                break
+        if best is not None and best[0] < new_cost:
+            return best
+        return (new_cost, "new_diag")
+
+    def _apply_fusion(self, plan, g: BitGate, gi: int, ops, last, batch):
+        action = plan[1]
+        G = batch[gi]
+        bits = list(g.bits)
+        if action == "new_dense":
+            op = _Dense(tg=bits, sl=[], M=G[:, None].copy(), recipe=[("init_dense", gi, len(bits))])
+            ops.append(op)
+            idx = len(ops) - 1
+        elif action == "new_diag":
+            op = _Diag(bits=bits, d=np.diagonal(G, axis1=1, axis2=2).copy(), recipe=[("init_diag", gi, len(bits))])
+            ops.append(op)
+            idx = len(ops) - 1
+        elif action in ("merge_dense", "diag_to_dense"):
+            idx = plan[2]
+            op = ops[idx]
+            if action == "diag_to_dense":
+                op = self._diag_to_dense(op, ops, idx, plan[3], plan[4])
+            newb = [b for b in bits if b not in op.tg and b not in op.sl]
+            # selectors hit by a non-diagonal gate become targets
+            for b in bits:
+                if b in op.sl:
+                    i = op.sl.index(b)
+                    step = ("s2t", i)
+                    op.M = _Replayer.dense_step(op.M, step, batch)
+                    op.recipe.append(step)
+                    op.sl.pop(i)
+                    op.tg.append(b)
+            if newb:
+                step = ("tx", len(newb))
+                op.M = _Replayer.dense_step(op.M, step, batch)
+                op.recipe.append(step)
+                op.tg.extend(newb)
+            pos = tuple(op.tg.index(b) for b in bits)
+            step = ("mul", gi, pos)
+            op.M = _Replayer.dense_step(op.M, step, batch)
+            op.recipe.append(step)
+        elif action == "absorb_dense":
+            _, _, idx, grow_t, grow_s = plan
+            op = ops[idx]
+            if grow_t:
+                step = ("tx", len(grow_t))
+                op.M = _Replayer.dense_step(op.M, step, batch)
+                op.recipe.append(step)
+                op.tg.extend(grow_t)
+            if grow_s:
+                step = ("sx", len(grow_s))
+                op.M = _Replayer.dense_step(op.M, step, batch)
+                op.recipe.append(step)
+                op.sl.extend(grow_s)
+            tpos = tuple(op.tg.index(b) if b in op.tg else None for b in bits)
+            spos = tuple(op.sl.index(b) if b in op.sl else None for b in bits)
+            step = ("dmul", gi, tpos, spos)
+            op.M = _Replayer.dense_step(op.M, step, batch)
+            op.recipe.append(step)
+        elif action == "absorb_diag":
+            idx = plan[2]
+            op = ops[idx]
+            newb = [b for b in bits if b not in op.bits]
+            if newb:
+                step = ("dx", len(newb))
+                op.d = _Replayer.diag_step(op.d, step, batch)
+                op.recipe.append(step)
+                op.bits.extend(newb)
+            pos = tuple(op.bits.index(b) for b in bits)
+            step = ("dd", gi, pos)
+            op.d = _Replayer.diag_step(op.d, step, batch)
+            op.recipe.append(step)
+        else:
+            raise AssertionError(action)
+        for b in ops[idx].touches():
+            last[b] = max(last.get(b, -1), idx)
+
+    def _diag_to_dense(self, dop: _Diag, ops, idx, loc, glob):
+        """Turns a diagonal table into a dense op: its tile bits become targets and
+        its out-of-tile bits selectors (the caller checked both limits)."""
+        tg = list(loc)
+        sl = list(glob)
+        recipe = [("diag_as_dense", list(dop.recipe), list(dop.bits), list(tg), list(sl))]
+        M = _diag_to_dense_matrix(dop.d, dop.bits, tg, sl)
+        op = _Dense(tg=tg, sl=sl, M=M, recipe=recipe)
+        ops[idx] = op
+        return op
+
+    # ---- emission -----------------------------------------------------------
+    def _emit(self, pass_plans, nbits, ngates) -> Plan:
+        passes = np.zeros(len(pass_plans), dtype=_lib.PASS_DTYPE)
+        nops = sum(len(pp.ops) for pp in pass_plans)
+        ops = np.zeros(nops, dtype=_lib.OP_DTYPE)
+        layout = []
+        chunks = []
+        off = 0
+        oi = 0
+        for q, pp in enumerate(pass_plans):
+            tile_of = {b: b for b in range(pp.m)}
+            for j, b in enumerate(pp.hi):
+                tile_of[b] = pp.m + j
+            rec = passes[q]
+            rec["L"] = pp.L
+            rec["m"] = pp.m
+            rec["op_begin"] = oi
+            rec["op_count"] = len(pp.ops)
+            rec["hi"][: len(pp.hi)] = pp.hi
+
+            def code(b):
+                return tile_of[b] if b in tile_of else -(b + 1)
+
+            for op in pp.ops:
+                r = ops[oi]
+                if op.kind == "dense":
+                    k = len(op.tg)
+                    tbits = [tile_of[b] for b in op.tg]
+                    r["kind"] = _lib.OP_DENSE
+                    r["k"] = k
+                    r["nsel"] = len(op.sl)
+                    r["bits"][:k] = tbits
+                    r["sel"][: len(op.sl)] = [code(b) for b in op.sl]
+                    go = group_order(pp.L, tbits)
+                    r["gorder"][: len(go)] = go
+                    data = op.M[0].reshape(-1)
+                    layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2])))
+                else:
+                    r["kind"] = _lib.OP_DIAG
+                    r["k"] = len(op.bits)
+                    r["bits"][: len(op.bits)] = [code(b) for b in op.bits]
+                    data = op.d[0]
+                    layout.append(("diag", op.recipe, off, (len(op.bits),)))
+                r["mat"] = off
+                chunks.append(data.astype(np.complex64))
+                off += len(data)
+                if off & 1:
+                    chunks.append(np.zeros(1, np.complex64))
+                    off += 1
+                oi += 1
+        pool = np.concatenate(chunks) if chunks else np.zeros(2, np.complex64)
+        return Plan(
+            nbits=nbits,
+            passes=passes,
+            ops=ops,
+            pool=pool,
+            pass_plans=pass_plans,
+            ngates=ngates,
+            layout=layout,
+            pool_len=max(off, 2),
+        )
+
+
+def _diag_to_dense_matrix(d: np.ndarray, bits, tg, sl) -> np.ndarray:
+    """(P, 2^b) diagonal table over `bits` -> (P, 2^|sl|, 2^|tg|, 2^|tg|) diagonal matrices."""
+    P = d.shape[0]
+    ns, dt = 2 ** len(sl), 2 ** len(tg)
+    s = np.arange(ns)[:, None]
+    t = np.arange(dt)[None, :]
+    sub = np.zeros((ns, dt), dtype=np.int64)
+    for j, b in enumerate(bits):
+        if b in tg:
+            sub = sub | (((t >> tg.index(b)) & 1) << j)
+        else:
+            sub = sub | (((s >> sl.index(b)) & 1) << j)
+    vals = d[:, sub]  # (P, ns, dt)
+    M = np.zeros((P, ns, dt, dt), dtype=d.dtype)
+    ar = np.arange(dt)
+    M[:, :, ar, ar] = vals
+    return M
+
+
+# recipe steps that need access to nested recipes are handled here
+_orig_dense_step = _Replayer.dense_step
+
+
+def _dense_step(M, step, gates):
+    kind = step[0]
+    if kind == "init_dense":
+        _, gi, k = step
+        return np.asarray(gates[gi])[:, None].astype(np.complex128, copy=True)
+    if kind == "diag_as_dense":
+        _, sub_recipe, bits, tg, sl = step
+        P = np.asarray(next(iter(gates.values()))).shape[0]
+        D = np.ones((P, 1), dtype=np.complex128)
+        for st in sub_recipe:
+            D = _Replayer.diag_step(D, st, gates)
+        return _diag_to_dense_matrix(D, bits, tg, sl)
+    return _orig_dense_step(M, step, gates)
+
+
+_orig_diag_step = _Replayer.diag_step
+
+
+def _diag_step(D, step, gates):
+    if step[0] == "init_diag":
+        _, gi, k = step
+        return np.diagonal(np.asarray(gates[gi]), axis1=1, axis2=2).astype(np.complex128, copy=True)
+    return _orig_diag_step(D, step, gates)
+
+
+_Replayer.dense_step = staticmethod(_dense_step)
+_Replayer.diag_step = staticmethod(_diag_step)

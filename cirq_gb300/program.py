@@ -1,0 +1,279 @@
+"""Circuits compiled once, evaluated for many parameter points.
+
+A :class:`CompiledCircuit` holds the structure of a (possibly parameterised)
+circuit over a fixed qubit order: its BitGates, the plan of passes/ops, and
+for every BitGate an evaluator that produces its matrices for a batch of
+``cirq.ParamResolver`` points.  Evaluating a sweep therefore costs one plan
+plus vectorised numpy per point, instead of the reference's per-point
+``resolve_parameters`` + per-operation dispatch
+(``cirq-core/cirq/sim/simulator.py:558-640``,
+``cirq-core/cirq/protocols/resolve_parameters.py:137-199``).
+
+EigenGates with a symbolic exponent (XPow/YPow/ZPow/CZPow/ZZPow/Rx/Ry/Rz,
+...) are evaluated from their eigen-decomposition, U(t) = sum_k
+exp(i pi t (h_k + s)) P_k, which is the formula of ``EigenGate._unitary_``
+(``cirq-core/cirq/ops/eigen_gate.py:295-305``); any other parameterised
+operation falls back to resolving it and calling ``cirq.unitary``/``cirq.kraus``
+per point.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Any, Callable, Sequence
+
+import numpy as np
+
+from cirq_gb300._cirq_env import ensure_cirq
+from cirq_gb300.ir import BitGate, UnsupportedOperation, is_diagonal
+from cirq_gb300.planner import Plan, Planner
+
+
+def _cirq():
+    return ensure_cirq()
+
+
+@dataclasses.dataclass
+class OpSource:
+    """How to produce one BitGate's matrix for a batch of resolvers."""
+
+    op: Any
+    transform: str  # 'u' (unitary), 'conj' (conjugate unitary), 'superop'
+    const: np.ndarray | None  # constant matrix (unparameterised ops)
+    eigen: tuple | None  # (components [(h, P)], shift, exponent expr) for EigenGates
+
+    def matrices(self, resolvers: Sequence[Any]) -> np.ndarray:
+        P = len(resolvers)
+        if self.const is not None:
+            return np.broadcast_to(self.const, (P,) + self.const.shape)
+        cirq = _cirq()
+        if self.eigen is not None:
+            comps, shift, expr = self.eigen
+            t = np.array([float(r.value_of(expr)) for r in resolvers])
+            out = 0
+            for h, proj in comps:
+                out = out + np.exp(1j * np.pi * t * (h + shift))[:, None, None] * proj[None]
+            return self._finish(np.asarray(out, dtype=np.complex128))
+        mats = []
+        for r in resolvers:
+            op = cirq.resolve_parameters(self.op, r)
+            if self.transform == "superop":
+                ks = cirq.kraus(op)
+                mats.append(sum(np.kron(np.conjugate(k), k) for k in ks))
+            else:
+                mats.append(np.asarray(cirq.unitary(op), dtype=np.complex128))
+        return self._finish(np.array(mats))
+
+    def _finish(self, m: np.ndarray) -> np.ndarray:
+        if self.transform == "conj":
+            return np.conjugate(m)
+        if self.transform == "phase":  # (P, 1, 1) scalar -> scalar * I_2
+            return m.reshape(-1, 1, 1) * np.eye(2)[None]
+        return m
+
+    def derivatives(self, resolvers: Sequence[Any], symbol) -> np.ndarray | None:
+        """dU/d(symbol) for every resolver (P, d, d), or None if U does not depend on it."""
+        cirq = _cirq()
+        if self.const is not None:
+            return None
+        if self.eigen is not None:
+            comps, shift, expr = self.eigen
+            import sympy
+
+            dexpr = sympy.diff(expr, symbol)
+            if dexpr == 0:
+                return None
+            t = np.array([float(r.value_of(expr)) for r in resolvers])
+            dt = np.array([float(r.value_of(dexpr)) for r in resolvers])
+            out = 0
+            for h, proj in comps:
+                f = 1j * np.pi * (h + shift) * np.exp(1j * np.pi * t * (h + shift)) * dt
+                out = out + f[:, None, None] * proj[None]
+            return self._finish(np.asarray(out, dtype=np.complex128))
+        if symbol not in cirq.parameter_symbols(self.op):
+            return None
+        h = 1e-6
+        mats = []
+        for r in resolvers:
+            base = dict(r.param_dict)
+            plus = dict(base)
+            minus = dict(base)
+            v = float(r.value_of(symbol))
+            plus[symbol] = v + h
+            minus[symbol] = v - h
+            up = np.asarray(cirq.unitary(cirq.resolve_parameters(self.op, plus)), dtype=np.complex128)
+            um = np.asarray(cirq.unitary(cirq.resolve_parameters(self.op, minus)), dtype=np.complex128)
+            mats.append((up - um) / (2 * h))
+        return self._finish(np.array(mats))
+
+
+def _eigen_info(op):
+    """(components, shift, exponent expression) for a GateOperation of an EigenGate
+    whose only parameter is its exponent; None otherwise."""
+    cirq = _cirq()
+    gate = getattr(op, "gate", None)
+    if not isinstance(gate, cirq.EigenGate):
+        return None
+    if type(op) is not cirq.GateOperation:
+        return None
+    expr = gate.exponent
+    if not cirq.is_parameterized(expr):
+        return None
+    if cirq.is_parameterized(gate.global_shift):
+        return None
+    try:
+        comps = [(float(h), np.asarray(p, dtype=np.complex128)) for h, p in gate._eigen_components()]
+    except Exception:
+        return None
+    return comps, float(gate.global_shift), expr
+
+
+def split_measurements(circuit):
+    """(unitary part ops, terminal measurement ops).
+
+    Raises NotImplementedError for measurements that are not terminal."""
+    cirq = _cirq()
+    from cirq_gb300.ir import flatten_ops
+
+    ops = flatten_ops(circuit)
+    if not any(cirq.is_measurement(op) for op in ops):
+        return ops, []
+    if not circuit.are_all_measurements_terminal():
+        raise NotImplementedError(
+            "cirq_gb300 simulates measurements only at the end of the circuit "
+            "(mid-circuit measurement needs per-repetition trajectories)"
+        )
+    body = [op for op in ops if not cirq.is_measurement(op)]
+    meas = [op for op in ops if cirq.is_measurement(op)]
+    for op in meas:
+        if not isinstance(op.gate, cirq.MeasurementGate):
+            raise NotImplementedError(f"unsupported measurement {op!r}")
+    return body, meas
+
+
+class CompiledCircuit:
+    """Structure + plan of a circuit over a fixed qubit order (see module doc)."""
+
+    def __init__(
+        self,
+        ops: Sequence[Any],
+        qubits: Sequence[Any],
+        *,
+        dm: bool,
+        planner: Planner,
+        resolvers: Sequence[Any],
+    ):
+        cirq = _cirq()
+        self.qubits = tuple(qubits)
+        self.n = len(qubits)
+        self.dm = dm
+        self.nbits = 2 * self.n if dm else self.n
+        index = {q: i for i, q in enumerate(self.qubits)}
+        n = self.n
+        self.sources: list[OpSource] = []
+        self.gates: list[BitGate] = []
+        self._phase_ops = [op for op in ops if not op.qubits]
+        for op in ops:
+            if not op.qubits:
+                if dm:
+                    continue  # a global phase cancels in rho
+                if not cirq.has_unitary(op) and not cirq.is_parameterized(op):
+                    raise UnsupportedOperation(f"operation without qubits: {op!r}")
+                if self.n == 0:
+                    continue
+                # a global phase is a diagonal gate on index bit 0 (absorbed for free)
+                const = None
+                if not cirq.is_parameterized(op):
+                    const = complex(np.asarray(cirq.unitary(op)).reshape(-1)[0]) * np.eye(2)
+                self._add(op, "phase", const, None, (0,))
+                continue
+            if any(q.dimension != 2 for q in op.qubits):
+                raise UnsupportedOperation(f"only qubits are supported, got {op!r}")
+            pos = [index[q] for q in op.qubits]
+            k = len(pos)
+            param = cirq.is_parameterized(op)
+            unitary = cirq.has_unitary(op) if not param else _param_has_unitary(op, resolvers[0])
+            if not unitary and not dm:
+                raise UnsupportedOperation(
+                    f"noisy operation {op!r}: the state-vector simulator only handles unitary "
+                    "operations (use DensityMatrixSimulator for channels)"
+                )
+            eig = _eigen_info(op) if param else None
+            if unitary:
+                if k > 5:
+                    raise UnsupportedOperation(f"gates on more than 5 qubits are not supported: {op!r}")
+                const = None if param else np.asarray(cirq.unitary(op), dtype=np.complex128)
+                if not dm:
+                    self._add(op, "u", const, eig, tuple(n - 1 - p for p in reversed(pos)))
+                else:
+                    self._add(op, "u", const, eig, tuple(2 * n - 1 - p for p in reversed(pos)))
+                    self._add(
+                        op, "conj", None if const is None else np.conjugate(const), eig,
+                        tuple(n - 1 - p for p in reversed(pos)),
+                    )
+            else:
+                if 2 * k > 5:
+                    raise UnsupportedOperation(
+                        f"channels on more than 2 qubits are not supported: {op!r}"
+                    )
+                const = None
+                if not param:
+                    ks = cirq.kraus(op)
+                    const = sum(np.kron(np.conjugate(np.asarray(kk)), np.asarray(kk)) for kk in ks)
+                    const = np.asarray(const, dtype=np.complex128)
+                rows = tuple(2 * n - 1 - p for p in reversed(pos))
+                cols = tuple(n - 1 - p for p in reversed(pos))
+                self._add(op, "superop", const, None, rows + cols)
+        self.planner = planner
+        self.plan: Plan | None = None
+        self._plan_resolvers(resolvers)
+
+    def _add(self, op, transform, const, eig, bits):
+        src = OpSource(op, transform, const, eig)
+        self.sources.append(src)
+        self.gates.append(BitGate(bits=bits, matrix=None, diagonal=False, tag=len(self.sources) - 1))
+
+    def gate_batch(self, resolvers) -> dict:
+        return {i: s.matrices(resolvers) for i, s in enumerate(self.sources)}
+
+    def _plan_resolvers(self, resolvers):
+        batch = self.gate_batch(resolvers)
+        keep = []
+        for i, g in enumerate(self.gates):
+            m = np.asarray(batch[i])
+            d = m.shape[-1]
+            g.matrix = m[0]
+            # diagonal only if diagonal at every point (a dense op handles any matrix)
+            g.diagonal = bool(all(is_diagonal(m[p]) for p in range(m.shape[0])))
+            ident = self.sources[i].const is not None and np.array_equal(m[0], np.eye(d))
+            if not ident:
+                keep.append(i)
+        self.kept = keep
+        gates = [self.gates[i] for i in keep]
+        sub = {j: batch[i][:1] for j, i in enumerate(keep)}
+        self.plan = self.planner.plan(gates, self.nbits, batch=sub)
+
+    def pool(self, resolvers) -> np.ndarray:
+        """complex64 (P, pool_len) matrix pools for the resolvers."""
+        batch = self.gate_batch(resolvers)
+        sub = {j: np.asarray(batch[i]) for j, i in enumerate(self.kept)}
+        return self.plan.pool_for(sub, len(resolvers))
+
+    def global_phase(self, resolver) -> complex:
+        """Product of the global-phase operations (used for 0-qubit circuits)."""
+        cirq = _cirq()
+        ph = 1.0 + 0j
+        for op in self._phase_ops:
+            ph *= complex(np.asarray(cirq.unitary(cirq.resolve_parameters(op, resolver))).reshape(-1)[0])
+        return ph
+
+
+def _param_has_unitary(op, resolver) -> bool:
+    cirq = _cirq()
+    return cirq.has_unitary(cirq.resolve_parameters(op, resolver))
+
+
+def structure_key(ops, qubits, dm, planner: Planner, noise_repr: str = "") -> Any:
+    """A cache key for the compiled structure of an op list (parameter values of
+    unparameterised gates are part of the structure)."""
+    return (tuple(ops), tuple(qubits), dm, planner.tile_bits, planner.kmax, planner.budget, noise_repr)

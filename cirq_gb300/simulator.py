@@ -1,0 +1,475 @@
+"""Drop-in GPU simulators with the ``cirq.Simulator`` / ``cirq.DensityMatrixSimulator`` API.
+
+``Simulator`` implements the reference's simulator interfaces
+(``cirq-core/cirq/sim/simulator.py``): ``SimulatesSamples._run`` (:97-117),
+``SimulatesFinalState.simulate_sweep_iter`` (:510-538),
+``SimulatesExpectationValues.simulate_expectation_values_sweep_iter``
+(:398-441) and ``SimulatesAmplitudes.compute_amplitudes_sweep_iter``
+(:188-216); ``run``, ``simulate``, ``simulate_sweep``,
+``simulate_expectation_values(_sweep)``, ``compute_amplitudes`` and
+``Sampler.run_batch`` come from the reference's base classes.  Results are the
+reference's own result types (``cirq.StateVectorTrialResult``,
+``cirq.DensityMatrixTrialResult``, ``cirq.ResultDict``).
+
+All amplitude arithmetic runs on the GPU through the C ABI; there is no CPU
+fallback.  Differences from the reference, by design:
+
+* arithmetic is complex64 only (``dtype=np.complex64``, the reference's
+  default); other dtypes raise ``ValueError``;
+* measurements must be terminal (mid-circuit measurement and state-vector
+  noise need per-repetition trajectories) -- other circuits raise
+  ``NotImplementedError``;
+* ``split_untangled_states`` is accepted and ignored: the reference's
+  product-state factoring (``cirq-core/cirq/sim/simulation_product_state.py``)
+  changes no result, only its CPU cost.
+"""
+
+from __future__ import annotations
+
+import collections
+import math
+from typing import Any, Iterator, Sequence
+
+import numpy as np
+
+from cirq_gb300._cirq_env import ensure_cirq
+from cirq_gb300.engine import Engine, default_engine
+from cirq_gb300.ir import pauli_terms
+from cirq_gb300.planner import Planner
+from cirq_gb300.program import CompiledCircuit, split_measurements, structure_key
+
+cirq = ensure_cirq()
+
+_MAX_CACHE = 8
+
+
+def _check_dtype(dtype):
+    if np.dtype(dtype).kind != "c":
+        raise ValueError(f"dtype must be a complex type but was {dtype}")
+    if np.dtype(dtype) != np.complex64:
+        raise ValueError(
+            f"cirq_gb300 simulates in complex64 only (got {np.dtype(dtype)}); "
+            "use dtype=np.complex64"
+        )
+
+
+def _check_all_resolved(program, resolver) -> None:
+    """Restates check_all_resolved (cirq-core/cirq/sim/simulator.py:942-949)."""
+    syms = cirq.parameter_symbols(program)
+    if not syms:
+        return
+    unresolved = [s for s in syms if cirq.is_parameterized(resolver.value_of(s))]
+    if unresolved:
+        ops = [
+            op
+            for op in cirq.resolve_parameters(program, resolver, recursive=False).all_operations()
+            if cirq.is_parameterized(op)
+        ]
+        raise ValueError(
+            "Circuit contains ops whose symbols were not specified in "
+            f"parameter sweep. Ops: {ops}"
+        )
+
+
+class _GpuSimulatorBase:
+    """Shared machinery of the state-vector and density-matrix drop-ins."""
+
+    _dm = False
+
+    def __init__(
+        self,
+        *,
+        dtype: type[np.complexfloating] = np.complex64,
+        noise: cirq.NOISE_MODEL_LIKE = None,
+        seed: cirq.RANDOM_STATE_OR_SEED_LIKE = None,
+        split_untangled_states: bool = True,
+        device: int | None = None,
+        fusion_max_qubits: int = 4,
+        tile_bits: int = 12,
+        pass_budget: float = 40.0,
+    ):
+        _check_dtype(dtype)
+        self._dtype = np.complex64
+        self.noise = cirq.NoiseModel.from_noise_model_like(noise)
+        self._prng = cirq.value.parse_random_state(seed)
+        self._split_untangled_states = split_untangled_states
+        self._device = device
+        self.planner = Planner(tile_bits=tile_bits, kmax=fusion_max_qubits, budget=pass_budget)
+        self._cache: collections.OrderedDict = collections.OrderedDict()
+        self._engine: Engine | None = None
+
+    # ---- plumbing --------------------------------------------------------
+    @property
+    def engine(self) -> Engine:
+        if self._engine is None:
+            self._engine = default_engine(self._device)
+        return self._engine
+
+    def _noisy_ops(self, program, qubits):
+        from cirq_gb300.ir import flatten_ops
+
+        if self.noise is cirq.NO_NOISE:
+            return None
+        if not self._dm:
+            raise NotImplementedError(
+                "cirq_gb300.Simulator has no noisy state-vector trajectories; "
+                "use cirq_gb300.DensityMatrixSimulator for noise"
+            )
+        moments = self.noise.noisy_moments(program, sorted(qubits))
+        return flatten_ops(cirq.Circuit(cirq.flatten_to_ops_or_moments(moments)))
+
+    def _compile(self, body_ops, qubits, resolvers) -> CompiledCircuit:
+        key = structure_key(body_ops, qubits, self._dm, self.planner)
+        c = self._cache.get(key)
+        if c is not None:
+            self._cache.move_to_end(key)
+            return c
+        c = CompiledCircuit(body_ops, qubits, dm=self._dm, planner=self.planner, resolvers=resolvers[:1])
+        self._cache[key] = c
+        if len(self._cache) > _MAX_CACHE:
+            self._cache.popitem(last=False)
+        return c
+
+    def _prepare(self, program, qubit_order, params):
+        qubit_order = cirq.QubitOrder.as_qubit_order(qubit_order)
+        qubits = tuple(qubit_order.order_for(program.all_qubits()))
+        resolvers = list(cirq.to_resolvers(params))
+        body, meas = split_measurements(program)
+        noisy = self._noisy_ops(cirq.Circuit(body), qubits) if body else None
+        if noisy is not None:
+            body = noisy
+        compiled = self._compile(body, qubits, resolvers or [cirq.ParamResolver({})])
+        return qubits, resolvers, compiled, meas
+
+    def _evolve(self, compiled: CompiledCircuit, pool_row: np.ndarray, initial_state):
+        """Allocates the initial state on the device and runs the program."""
+        eng = self.engine
+        nbits = compiled.nbits
+        state = self._initial_device_state(compiled, initial_state)
+        if compiled.plan.npasses:
+            pool_dev = eng.upload(np.ascontiguousarray(pool_row))
+            eng.run(state, nbits, compiled.plan, pool_dev)
+        return state
+
+    def _measure_terminal(self, state, compiled, meas_ops) -> dict[str, np.ndarray]:
+        """One shot of every terminal measurement, then collapse (the reference
+        measures inside simulate(): cirq-core/cirq/sim/state_vector.py:235-322)."""
+        if not meas_ops:
+            return {}
+        eng = self.engine
+        n = compiled.n
+        index = {q: i for i, q in enumerate(compiled.qubits)}
+        u = self._prng.random_sample(1)
+        idx = int(eng.sample(state, n, u, dm=self._dm)[0])
+        measured = []
+        for op in meas_ops:
+            for q in op.qubits:
+                if q not in measured:
+                    measured.append(q)
+        mask = 0
+        for q in measured:
+            mask |= 1 << (n - 1 - index[q])
+        value = idx & mask
+        records: dict[str, list] = {}
+        for op in meas_ops:
+            gate = op.gate
+            bits = [(idx >> (n - 1 - index[q])) & 1 for q in op.qubits]
+            inv = gate.full_invert_mask()
+            bits = [b ^ 1 if inv[i] else b for i, b in enumerate(bits)]
+            records.setdefault(gate.key, []).append(bits)
+        # collapse: keep the sampled outcome, renormalise
+        if self._dm:
+            full_mask = mask | (mask << n)
+            full_value = value | (value << n)
+            eng.project(state, compiled.nbits, full_mask, full_value, 1.0)
+            p = float(eng.probabilities(state, n, dm=True).astype(np.float64).sum())
+            if p > 0:
+                eng.scale(state, compiled.nbits, 1.0 / p)
+        else:
+            eng.project(state, n, mask, value, 1.0)
+            p = eng.norm2(state, n)
+            if p > 0:
+                eng.scale(state, n, 1.0 / math.sqrt(p))
+        out = {}
+        for key, v in records.items():
+            arr = np.array(v[-1], dtype=np.uint8)
+            out[key] = arr
+        return out
+
+    def _sample_records(self, state, compiled, meas_ops, repetitions) -> dict[str, np.ndarray]:
+        """Terminal-measurement sampling, mirroring StepResult.sample_measurement_ops
+        (cirq-core/cirq/sim/simulator.py:733-820) with _allow_repeated=True."""
+        eng = self.engine
+        n = compiled.n
+        index = {q: i for i, q in enumerate(compiled.qubits)}
+        u = self._prng.random_sample(repetitions)
+        samples = eng.sample(state, n, u, dm=self._dm).astype(np.int64)
+        results: dict[str, list] = {}
+        for op in meas_ops:
+            gate = op.gate
+            out = np.zeros((repetitions, len(op.qubits)), dtype=np.int8)
+            inv = gate.full_invert_mask()
+            for i, q in enumerate(op.qubits):
+                out[:, i] = (samples >> (n - 1 - index[q])) & 1
+                if inv[i]:
+                    out[:, i] ^= out[:, i] < 2
+            if gate.confusion_map:
+                _confuse(out, op.qubits, gate.confusion_map, self._prng)
+            results.setdefault(gate.key, []).append(out)
+        return {k: np.array(v).swapaxes(0, 1) for k, v in results.items()}
+
+    # ---- SimulatesSamples ---------------------------------------------------
+    def _run(self, circuit, param_resolver, repetitions) -> dict[str, np.ndarray]:
+        param_resolver = param_resolver or cirq.ParamResolver({})
+        _check_all_resolved(circuit, param_resolver)
+        qubits = tuple(sorted(circuit.all_qubits()))
+        _, resolvers, compiled, meas = self._prepare(circuit, qubits, param_resolver)
+        if compiled.n == 0:
+            return {op.gate.key: np.zeros((repetitions, 1, 0), dtype=np.int8) for op in meas}
+        pool = compiled.pool([param_resolver])[0]
+        state = self._evolve(compiled, pool, 0)
+        return self._sample_records(state, compiled, meas, repetitions)
+
+
+def _confuse(bits, qubits, confusion_map, prng) -> None:
+    """Applies measurement confusion matrices per repetition, as
+    StepResult._confuse_results does (cirq-core/cirq/sim/simulator.py:822-844)."""
+    for rep in bits:
+        for indices, confuser in confusion_map.items():
+            row = cirq.big_endian_digits_to_int((rep[k] for k in indices), base=[2] * len(indices))
+            new_val = prng.choice(len(confuser), p=confuser[row])
+            new_bits = cirq.big_endian_int_to_digits(new_val, base=[2] * len(indices))
+            for i, k in enumerate(indices):
+                rep[k] = new_bits[i]
+
+
+def _state_vector_result(params, measurements, qubits, vec: np.ndarray):
+    """Builds a genuine cirq.StateVectorTrialResult around `vec` without copying it."""
+    shape = (2,) * len(qubits)
+    try:
+        from cirq.sim.state_vector_simulation_state import _BufferedStateVector
+
+        st = cirq.StateVectorSimulationState.__new__(cirq.StateVectorSimulationState)
+        buffered = _BufferedStateVector(vec.reshape(shape), np.empty(0, dtype=np.complex64))
+        cirq.SimulationState.__init__(
+            st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None
+        )
+    except Exception:  # pragma: no cover - public-constructor route (copies vec)
+        st = cirq.StateVectorSimulationState(
+            qubits=tuple(qubits), initial_state=vec.reshape(shape), dtype=np.complex64
+        )
+    res = cirq.StateVectorTrialResult(
+        params=params, measurements=measurements, final_simulator_state=st
+    )
+    # the renormalisation rule was applied on the device
+    res.__dict__["final_state_vector"] = vec
+    return res
+
+
+class Simulator(
+    _GpuSimulatorBase,
+    cirq.SimulatesSamples,
+    cirq.SimulatesExpectationValues,
+    cirq.SimulatesFinalState,
+    cirq.SimulatesAmplitudes,
+):
+    """GPU state-vector simulator with the API of ``cirq.Simulator``
+    (``cirq-core/cirq/sim/sparse_simulator.py:31-218``)."""
+
+    def _initial_device_state(self, compiled, initial_state):
+        eng = self.engine
+        n = compiled.n
+        if initial_state is None:
+            initial_state = 0
+        if isinstance(initial_state, (int, np.integer)):
+            if not 0 <= int(initial_state) < 2**n:
+                raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
+            return eng.new_state(n, basis=int(initial_state))
+        if isinstance(initial_state, cirq.SimulationStateBase):
+            raise NotImplementedError("cirq_gb300.Simulator takes raw initial states, not SimulationState")
+        vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
+        return eng.new_state(n, initial=vec)
+
+    def simulate_sweep_iter(
+        self,
+        program: cirq.AbstractCircuit,
+        params: cirq.Sweepable,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+        initial_state: Any = None,
+    ) -> Iterator[cirq.StateVectorTrialResult]:
+        qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
+        for r in resolvers:
+            _check_all_resolved(program, r)
+        if compiled.n == 0:
+            for r in resolvers:
+                vec = np.array([compiled.global_phase(r)], dtype=np.complex64)
+                yield _state_vector_result(r, {}, qubits, vec)
+            return
+        pools = compiled.pool(resolvers)
+        eng = self.engine
+        for p, r in enumerate(resolvers):
+            state = self._evolve(compiled, pools[p], initial_state)
+            measurements = self._measure_terminal(state, compiled, meas)
+            eng.final_renormalize(state, compiled.n)
+            vec = eng.download_state(state, compiled.n)
+            state.free()
+            yield _state_vector_result(r, measurements, qubits, vec)
+
+    def simulate_expectation_values_sweep_iter(
+        self,
+        program: cirq.AbstractCircuit,
+        observables: cirq.PauliSumLike | list[cirq.PauliSumLike],
+        params: cirq.Sweepable,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+        initial_state: Any = None,
+        permit_terminal_measurements: bool = False,
+    ) -> Iterator[list[float]]:
+        """Mirrors Simulator.simulate_expectation_values_sweep_iter
+        (cirq-core/cirq/sim/sparse_simulator.py:193-218): expectation values are
+        evaluated on the device from the final state, which never leaves HBM."""
+        if not permit_terminal_measurements and program.are_any_measurements_terminal():
+            raise ValueError(
+                "Provided circuit has terminal measurements, which may "
+                "skew expectation values. If this is intentional, set "
+                "permit_terminal_measurements=True."
+            )
+        if not isinstance(observables, list):
+            observables = [observables]
+        pslist = [cirq.PauliSum.wrap(o) for o in observables]
+        for ps in pslist:
+            if any(abs(p.coefficient.imag) > 0.0001 for p in ps):
+                raise NotImplementedError(
+                    "Cannot compute expectation value of a non-Hermitian "
+                    f"PauliString <{ps}>. Coefficient must be real."
+                )
+        body_prog = cirq.Circuit(op for op in program.all_operations() if not cirq.is_measurement(op))
+        qubits, resolvers, compiled, _ = self._prepare(body_prog, qubit_order, params)
+        index = {q: i for i, q in enumerate(qubits)}
+        for ps in pslist:
+            for q in ps.qubits:
+                if q not in index:
+                    raise ValueError(f"Qubit {q} of the observable is not in the qubit order")
+        terms = [pauli_terms(ps, index, compiled.n) for ps in pslist]
+        for r in resolvers:
+            _check_all_resolved(body_prog, r)
+        pools = compiled.pool(resolvers)
+        eng = self.engine
+        for p, r in enumerate(resolvers):
+            state = self._evolve(compiled, pools[p], initial_state)
+            out = []
+            for t in terms:
+                vals = eng.expect_paulis(state, compiled.n, t)
+                out.append(complex(np.sum(vals)))
+            state.free()
+            yield out
+
+    def compute_amplitudes_sweep_iter(
+        self,
+        program: cirq.AbstractCircuit,
+        bitstrings: Sequence[int],
+        params: cirq.Sweepable,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+    ) -> Iterator[Sequence[complex]]:
+        """Amplitudes of the final state (cirq-core/cirq/sim/state_vector_simulator.py:74-98)."""
+        for result in self.simulate_sweep_iter(program, params, qubit_order):
+            vec = result.final_state_vector
+            yield [vec[int(b)] for b in bitstrings]
+
+
+class DensityMatrixSimulator(
+    _GpuSimulatorBase,
+    cirq.SimulatesSamples,
+    cirq.SimulatesExpectationValues,
+    cirq.SimulatesFinalState,
+):
+    """GPU density-matrix simulator with the API of ``cirq.DensityMatrixSimulator``
+    (``cirq-core/cirq/sim/density_matrix_simulator.py:32-236``).
+
+    rho (2^n x 2^n complex64) lives in HBM as a 2n-bit vector; unitaries act
+    as U on the row bits and conj(U) on the column bits, channels as fused
+    superoperators sum_i conj(K_i) (x) K_i."""
+
+    _dm = True
+
+    def _initial_device_state(self, compiled, initial_state):
+        eng = self.engine
+        n = compiled.n
+        if initial_state is None:
+            initial_state = 0
+        if isinstance(initial_state, (int, np.integer)):
+            if not 0 <= int(initial_state) < 2**n:
+                raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
+            i = int(initial_state)
+            return eng.new_state(2 * n, basis=(i << n) | i)
+        if isinstance(initial_state, cirq.SimulationStateBase):
+            raise NotImplementedError("takes raw initial states, not SimulationState")
+        rho = cirq.to_valid_density_matrix(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
+        return eng.new_state(2 * n, initial=rho.reshape(-1))
+
+    def simulate_sweep_iter(
+        self,
+        program: cirq.AbstractCircuit,
+        params: cirq.Sweepable,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+        initial_state: Any = None,
+    ) -> Iterator[cirq.DensityMatrixTrialResult]:
+        qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
+        for r in resolvers:
+            _check_all_resolved(program, r)
+        n = compiled.n
+        if n == 0:
+            for r in resolvers:
+                st = cirq.DensityMatrixSimulationState(qubits=(), initial_state=np.ones((1, 1)), dtype=np.complex64)
+                yield cirq.DensityMatrixTrialResult(params=r, measurements={}, final_simulator_state=st)
+            return
+        pools = compiled.pool(resolvers)
+        eng = self.engine
+        for p, r in enumerate(resolvers):
+            state = self._evolve(compiled, pools[p], initial_state)
+            measurements = self._measure_terminal(state, compiled, meas)
+            rho = eng.download_state(state, 2 * n, pinned=False).reshape(2**n, 2**n)
+            state.free()
+            st = cirq.DensityMatrixSimulationState(
+                qubits=qubits, initial_state=rho, dtype=np.complex64
+            )
+            yield cirq.DensityMatrixTrialResult(
+                params=r, measurements=measurements, final_simulator_state=st
+            )
+
+    def simulate_expectation_values_sweep_iter(
+        self,
+        program: cirq.AbstractCircuit,
+        observables: cirq.PauliSumLike | list[cirq.PauliSumLike],
+        params: cirq.Sweepable,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+        initial_state: Any = None,
+        permit_terminal_measurements: bool = False,
+    ) -> Iterator[list[float]]:
+        """Mirrors DensityMatrixSimulator.simulate_expectation_values_sweep_iter
+        (cirq-core/cirq/sim/density_matrix_simulator.py:204-236): Tr(P rho)
+        is evaluated on the device."""
+        if not permit_terminal_measurements and program.are_any_measurements_terminal():
+            raise ValueError(
+                "Provided circuit has terminal measurements, which may "
+                "skew expectation values. If this is intentional, set "
+                "permit_terminal_measurements=True."
+            )
+        if not isinstance(observables, list):
+            observables = [observables]
+        pslist = [cirq.PauliSum.wrap(o) for o in observables]
+        body_prog = cirq.Circuit(op for op in program.all_operations() if not cirq.is_measurement(op))
+        qubits, resolvers, compiled, _ = self._prepare(body_prog, qubit_order, params)
+        index = {q: i for i, q in enumerate(qubits)}
+        terms = [pauli_terms(ps, index, compiled.n) for ps in pslist]
+        for r in resolvers:
+            _check_all_resolved(body_prog, r)
+        pools = compiled.pool(resolvers)
+        eng = self.engine
+        for p, r in enumerate(resolvers):
+            state = self._evolve(compiled, pools[p], initial_state)
+            out = []
+            for t in terms:
+                vals = eng.expect_paulis(state, compiled.n, t, dm=True)
+                out.append(complex(np.sum(vals)))
+            state.free()
+            yield out

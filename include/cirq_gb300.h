@@ -1,0 +1,216 @@
+/*
+ * cirq_gb300 -- C ABI of the GB300 (sm_103a) circuit-simulation engine.
+ *
+ * This is the device boundary under the Python drop-in simulators
+ * (cirq_gb300.Simulator / cirq_gb300.DensityMatrixSimulator).  The reference
+ * (quantumlib/Cirq) has no FFI: its simulators call numpy in-process.  Each
+ * entry point below replaces one numpy site of the reference's simulation
+ * path, cited as file:line relative to the Cirq repository.
+ *
+ * Conventions
+ *  - Amplitudes are complex64 (gbq_c64, interleaved float re/im), the layout
+ *    of numpy.complex64.  A state of n qubits is 2^n amplitudes; index bit b
+ *    belongs to the qubit at position n-1-b of the qubit order (Cirq's
+ *    big-endian order, cirq-core/cirq/sim/state_vector.py:81-112).
+ *  - A density matrix of n qubits is handled as a 2n-bit vector: index
+ *    row*2^n + col, exactly the reference's (2,)*2n tensor flattened
+ *    (cirq-core/cirq/sim/density_matrix_simulation_state.py:178).
+ *  - Every function returns 0 on success and a negative GBQ_ERR_* code on
+ *    failure; gbq_last_error() then returns a message (thread-local).
+ *  - All device work is ordered on the context's stream.  Functions that
+ *    return host data synchronise that stream before returning.
+ *  - Device pointers come from gbq_alloc; host pointers are caller-owned.
+ *  - A context is not thread-safe: use one context per thread.
+ */
+#ifndef CIRQ_GB300_H
+#define CIRQ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBQ_OK 0
+#define GBQ_ERR_ARG -1     /* invalid argument (maps to ValueError) */
+#define GBQ_ERR_CUDA -2    /* CUDA runtime error */
+#define GBQ_ERR_OOM -3     /* device allocation failed (maps to MemoryError) */
+#define GBQ_ERR_UNSUPPORTED -4
+
+typedef struct gbq_c64 {
+  float re, im;
+} gbq_c64;
+
+typedef struct gbq_ctx gbq_ctx;
+
+/* ---- operation program ------------------------------------------------
+ * A program is a list of passes.  One pass streams the state once through
+ * HBM in tiles of 2^L amplitudes: tile bits 0..m-1 are the global index bits
+ * 0..m-1 (contiguous runs of 2^m amplitudes) and tile bits m..L-1 are the
+ * global bits hi[0..L-m-1].  Inside a tile the pass applies its ops in
+ * order.  Bit codes: a value c >= 0 names tile bit c; c < 0 names global
+ * index bit (-c - 1), which is constant over one tile.
+ */
+#define GBQ_OP_DENSE 0      /* 2^k x 2^k matrix on k tile bits                */
+#define GBQ_OP_DIAG 1       /* 2^k-entry diagonal on k bit codes               */
+#define GBQ_OP_PROBE 2      /* two-state passes: Re<lam|D|psi> on k tile bits  */
+#define GBQ_OP_PROBE_DIAG 3 /* two-state passes: Re<lam|diag(d)|psi>, bit codes */
+
+#define GBQ_MAX_OPS_PER_PASS 64
+#define GBQ_MAX_TILE_BITS 13
+#define GBQ_MAX_DENSE_K 5
+#define GBQ_MAX_DIAG_K 8
+
+typedef struct gbq_op {
+  int8_t kind;       /* GBQ_OP_*                                              */
+  int8_t k;          /* dense/probe: number of target bits; diag: number of bits */
+  int8_t nsel;       /* dense/probe: selector bits (0..3), 2^nsel matrices     */
+  int8_t pad0;
+  int8_t bits[8];    /* dense/probe: tile bit of matrix-index bit j; diag: bit codes */
+  int8_t sel[4];     /* selector bit codes; matrix number = sum sel_j << j       */
+  int8_t gorder[16]; /* dense/probe: tile bit of group-index bit j (L-k entries) */
+  int32_t slot;      /* probe: output slot                                       */
+  int64_t mat;       /* offset (in gbq_c64) of the first matrix/table in the pool */
+} gbq_op;
+
+typedef struct gbq_pass {
+  int32_t L;         /* tile bits (<= GBQ_MAX_TILE_BITS, <= state bits)          */
+  int32_t m;         /* contiguous low bits (1..L)                               */
+  int32_t op_begin;  /* first op of this pass in the op array                    */
+  int32_t op_count;  /* <= GBQ_MAX_OPS_PER_PASS                                  */
+  int8_t hi[16];     /* global bits of tile bits m..L-1                          */
+} gbq_pass;
+
+/* Pauli string for expectation values: P = coef * i^{ny} X^{x} Z^{z} form
+ * with x = bits carrying X or Y, zy = bits carrying Z or Y, ny = #Y. */
+typedef struct gbq_pauli {
+  uint64_t x;
+  uint64_t zy;
+  int32_t ny;
+  int32_t pad;
+  double coef;
+} gbq_pauli;
+
+/* ---- context and memory ---------------------------------------------- */
+const char* gbq_last_error(void);
+int gbq_version(void);
+/* sizeof(gbq_op), sizeof(gbq_pass), sizeof(gbq_pauli), sizeof(gbq_point): lets
+ * a binding check its struct mirrors without touching a GPU. */
+int gbq_struct_sizes(int* op, int* pass, int* pauli, int* point);
+int gbq_ctx_create(int device, gbq_ctx** out);
+int gbq_ctx_destroy(gbq_ctx* ctx);
+int gbq_ctx_sync(gbq_ctx* ctx);
+int gbq_device_info(gbq_ctx* ctx, int* sm_count, size_t* free_bytes, size_t* total_bytes);
+int gbq_set_graphs(gbq_ctx* ctx, int enable);
+/* Number of kernels this context has launched (for launch accounting). */
+int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
+
+int gbq_alloc(gbq_ctx* ctx, size_t bytes, void** dptr);
+int gbq_free(gbq_ctx* ctx, void* dptr);
+int gbq_host_alloc(size_t bytes, void** hptr); /* pinned host memory */
+int gbq_host_free(void* hptr);
+int gbq_h2d(gbq_ctx* ctx, void* dst, const void* src, size_t bytes);
+int gbq_d2h(gbq_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* ---- state vectors ------------------------------------------------------
+ * Replaces StateVectorSimulationState construction
+ * (cirq-core/cirq/sim/state_vector_simulation_state.py:321-358): |index>. */
+int gbq_sv_set_basis(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t index);
+
+/* Runs a program over one state, in place.
+ * Replaces the per-operation loop SimulatorBase._core_iterator
+ * (cirq-core/cirq/sim/simulator_base.py:169-214) -> protocols.apply_unitary
+ * (cirq-core/cirq/protocols/apply_unitary_protocol.py:306-418) ->
+ * linalg.targeted_left_multiply / apply_matrix_to_slices
+ * (cirq-core/cirq/linalg/transformations.py:105-172, 310-380), and for
+ * density matrices protocols.apply_channel
+ * (cirq-core/cirq/protocols/apply_channel_protocol.py:168-356).
+ * mats is a device pool of matrices/tables referenced by gbq_op.mat. */
+int gbq_run(gbq_ctx* ctx, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
+            const gbq_op* ops, int nops, const gbq_c64* mats);
+
+/* Two-state reverse sweep for adjoint differentiation (no reference
+ * counterpart: the reference has no gradient code).  Dense/diag ops are
+ * applied to both psi and lam; probe ops add Re<lam|D|psi> of each tile to
+ * partial[slot * ntiles + tile] where ntiles = 2^(nbits - L) of that pass. */
+int gbq_run_dual(gbq_ctx* ctx, gbq_c64* psi, gbq_c64* lam, int nbits, const gbq_pass* passes,
+                 int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, double* partial);
+/* out[s] = sum_t partial[s * ntiles + t] for s < nslots (device arrays). */
+int gbq_reduce_slots(gbq_ctx* ctx, const double* partial, int nslots, int64_t ntiles, double* out);
+
+/* Sum of |psi_i|^2 in double (host result).
+ * Replaces np.linalg.norm in StateVectorTrialResult.final_state_vector
+ * (cirq-core/cirq/sim/state_vector_simulator.py:131-146). */
+int gbq_sv_norm2(gbq_ctx* ctx, const gbq_c64* state, int nbits, double* out);
+/* Keeps the amplitudes whose index satisfies (index & mask) == value, scaled
+ * by `scale`, and zeroes the rest: the collapse step of measure_state_vector
+ * (cirq-core/cirq/sim/state_vector.py:235-322) and, on a 2n-bit density
+ * vector, of measure_density_matrix (cirq-core/cirq/sim/density_matrix_utils.py:97-183). */
+int gbq_sv_project(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t mask, uint64_t value,
+                   float scale);
+/* state *= scale (device, in place). */
+int gbq_sv_scale(gbq_ctx* ctx, gbq_c64* state, int nbits, float scale);
+/* Final-state renormalisation rule of state_vector_simulator.py:131-146,
+ * evaluated on the device: renormalises in place only when that reduces the
+ * round-off of the total probability.  *applied = 1 when it did. */
+int gbq_sv_final_renormalize(gbq_ctx* ctx, gbq_c64* state, int nbits, int* applied);
+
+/* Inverse-CDF sampling of R basis indices from |psi|^2 (dm = 0) or from the
+ * diagonal of a density matrix of nbits qubits (dm = 1).  u[r] in [0, 1) are
+ * host uniforms; out[r] receives the sampled index.
+ * Replaces sample_state_vector (cirq-core/cirq/sim/state_vector.py:170-232),
+ * state_probabilities_by_indices (cirq-core/cirq/sim/simulation_utils.py:24-65)
+ * and sample_density_matrix (cirq-core/cirq/sim/density_matrix_utils.py:31-95). */
+int gbq_sample(gbq_ctx* ctx, const gbq_c64* state, int nbits, int dm, const double* u, int64_t R,
+               uint64_t* out);
+
+/* Probabilities |psi_i|^2 (dm = 0) or diag(rho) (dm = 1) as float32 into a
+ * device array of 2^nbits entries. */
+int gbq_probabilities(gbq_ctx* ctx, const gbq_c64* state, int nbits, int dm, float* out);
+
+/* Expectation values out[2t], out[2t+1] = (re, im) of coef_t <psi|P_t|psi>.
+ * Replaces PauliString._expectation_from_state_vector_no_validation
+ * (cirq-core/cirq/ops/pauli_string.py:625-655) summed by
+ * PauliSum.expectation_from_state_vector (cirq-core/cirq/ops/linear_combinations.py:659-718). */
+int gbq_sv_expect_paulis(gbq_ctx* ctx, const gbq_c64* state, int nbits, const gbq_pauli* terms,
+                         int nterms, double* out);
+/* Density-matrix counterpart: coef_t Tr(P_t rho) for rho of nbits qubits
+ * (cirq-core/cirq/ops/pauli_string.py:734-760). */
+int gbq_dm_expect_paulis(gbq_ctx* ctx, const gbq_c64* rho, int nbits, const gbq_pauli* terms,
+                         int nterms, double* out);
+/* out = sum_t coef_t P_t psi (a new state; used for lam = H psi). */
+int gbq_sv_apply_paulisum(gbq_ctx* ctx, const gbq_c64* psi, int nbits, const gbq_pauli* terms,
+                          int nterms, gbq_c64* out);
+/* out[j] = <a|b> as (re, im) in double. */
+int gbq_sv_inner(gbq_ctx* ctx, const gbq_c64* a, const gbq_c64* b, int nbits, double* out);
+
+/* ---- batched sweeps -----------------------------------------------------
+ * One persistent launch over many parameter points of possibly different
+ * widths.  Replaces the per-resolver loop of
+ * SimulatesIntermediateState.simulate_sweep_iter (cirq-core/cirq/sim/simulator.py:558-605)
+ * feeding Simulator.simulate_expectation_values_sweep_iter
+ * (cirq-core/cirq/sim/sparse_simulator.py:193-218).
+ * Point p runs passes [pass_begin, pass_begin+pass_count) of `passes`, with
+ * op.mat offsets relative to mat_base, on a 2^nbits state held in scratch
+ * slot (CTA) memory, then evaluates the diagonal observable sum_t coef_t
+ * Z^{zy_t} given by its Pauli terms; out[2p], out[2p+1] = (re, im) of <obs>.
+ * Host arrays: points, passes, ops, terms.  Device array: mats. */
+typedef struct gbq_point {
+  int32_t nbits;
+  int32_t pass_begin;
+  int32_t pass_count;
+  int32_t term_begin;
+  int32_t term_count;
+  int32_t pad;
+  int64_t mat_base;
+} gbq_point;
+
+int gbq_batch_expect(gbq_ctx* ctx, const gbq_point* points, int npoints, const gbq_pass* passes,
+                     int npasses, const gbq_op* ops, int nops, const gbq_c64* mats,
+                     const gbq_pauli* terms, int nterms, int max_nbits, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CIRQ_GB300_H */

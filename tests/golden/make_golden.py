@@ -1,0 +1,204 @@
+"""Generates the golden fixtures in this directory by running quantumlib/Cirq itself.
+
+Run from the repository root in a checkout that has the reference source:
+
+    python tests/golden/make_golden.py [/path/to/Cirq/cirq-core]
+
+The reference's own simulators (``cirq.Simulator``,
+``cirq.DensityMatrixSimulator``) and protocols produce every array stored
+here; nothing in this script re-implements them.  The fixtures are small
+(a few hundred KB in total) so the test suite can pin both the CPU oracle and
+the CUDA path against the reference on machines where the reference source is
+absent.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def _import_reference(path: str):
+    sys.path.insert(0, path)
+    sys.path.insert(0, ROOT)
+    from cirq_gb300._cirq_env import ensure_cirq
+
+    cirq = ensure_cirq()
+    assert os.path.abspath(cirq.__file__).startswith(os.path.abspath(path)), cirq.__file__
+    return cirq
+
+
+def main(ref_path: str) -> None:
+    cirq = _import_reference(ref_path)
+    import sympy
+
+    from cirq_gb300 import workloads
+
+    out = {}
+
+    # 1. random PhasedXZ + CZ layers, final states at complex128 and complex64.
+    for n, d, seed in [(10, 20, 1), (12, 8, 2), (5, 6, 3)]:
+        c = workloads.random_layer_circuit(n, d, seed)
+        s128 = cirq.Simulator(dtype=np.complex128).simulate(c).final_state_vector
+        s64 = cirq.Simulator(dtype=np.complex64).simulate(c).final_state_vector
+        out[f"layers_n{n}_d{d}_s{seed}_c128"] = s128
+        out[f"layers_n{n}_d{d}_s{seed}_c64"] = s64
+    # custom qubit order (reversed) and a basis-state initial state
+    c = workloads.random_layer_circuit(6, 5, 4)
+    q = sorted(c.all_qubits())
+    out["layers_n6_d5_s4_reversed_init5"] = (
+        cirq.Simulator(dtype=np.complex128)
+        .simulate(c, qubit_order=q[::-1], initial_state=5)
+        .final_state_vector
+    )
+
+    # 2. mixed gate zoo (every gate family the translator handles).
+    zoo = _gate_zoo(cirq)
+    out["zoo_c128"] = cirq.Simulator(dtype=np.complex128).simulate(zoo).final_state_vector
+
+    # 3. noisy density matrices.
+    c = workloads.noisy_layer_circuit(4, 4, seed=2, p=0.05, gamma=0.1)
+    out["dm_noisy_n4_d4"] = (
+        cirq.DensityMatrixSimulator(dtype=np.complex128).simulate(c).final_density_matrix
+    )
+    c = workloads.random_layer_circuit(3, 3, seed=5)
+    out["dm_noisemodel_n3"] = (
+        cirq.DensityMatrixSimulator(dtype=np.complex128, noise=cirq.depolarize(0.02))
+        .simulate(c)
+        .final_density_matrix
+    )
+    qd = cirq.LineQubit.range(3)
+    cg = cirq.Circuit(
+        cirq.H(qd[0]),
+        cirq.CNOT(qd[0], qd[1]),
+        cirq.generalized_amplitude_damp(0.3, 0.2).on(qd[1]),
+        cirq.phase_damp(0.25).on(qd[0]),
+        cirq.bit_flip(0.1).on(qd[2]),
+        cirq.asymmetric_depolarize(0.05, 0.1, 0.15).on(qd[2]),
+        cirq.CZ(qd[1], qd[2]) ** 0.3,
+        cirq.depolarize(0.1, n_qubits=2).on(qd[0], qd[2]),
+        cirq.reset(qd[1]),
+    )
+    out["dm_channels_n3"] = (
+        cirq.DensityMatrixSimulator(dtype=np.complex128).simulate(cg).final_density_matrix
+    )
+
+    # 4. QAOA expectation values over a sweep.
+    circuit, gammas, betas, obs, edges = workloads.qaoa_circuit(8, 4, seed=7)
+    pts = workloads.qaoa_points(4, 16, seed=8)
+    resolvers = [
+        cirq.ParamResolver({**dict(zip(gammas, p[:4])), **dict(zip(betas, p[4:]))}) for p in pts
+    ]
+    vals = cirq.Simulator(dtype=np.complex128).simulate_expectation_values_sweep(
+        circuit, obs, resolvers
+    )
+    out["qaoa_n8_p4_points"] = pts
+    out["qaoa_n8_p4_expect"] = np.array([v[0] for v in vals])
+
+    # 5. HEA energy, central finite differences and parameter-shift gradients
+    #    evaluated with the reference's simulate_expectation_values.
+    circuit, symbols, values = workloads.hea_circuit(5, 2, seed=9)
+    ham = workloads.random_pauli_hamiltonian(5, 12, seed=10)
+    sim = cirq.Simulator(dtype=np.complex128)
+
+    def energy(v):
+        return sim.simulate_expectation_values(
+            circuit, ham, param_resolver=dict(zip(symbols, v))
+        )[0].real
+
+    e0 = energy(values)
+    fd = np.zeros(len(symbols))
+    ps = np.zeros(len(symbols))
+    for i in range(len(symbols)):
+        vp = values.copy()
+        vm = values.copy()
+        vp[i] += 1e-4
+        vm[i] -= 1e-4
+        fd[i] = (energy(vp) - energy(vm)) / 2e-4
+        vp = values.copy()
+        vm = values.copy()
+        vp[i] += np.pi / 2
+        vm[i] -= np.pi / 2
+        ps[i] = (energy(vp) - energy(vm)) / 2
+    out["hea_n5_l2_values"] = values
+    out["hea_n5_l2_energy"] = np.array(e0)
+    out["hea_n5_l2_grad_fd"] = fd
+    out["hea_n5_l2_grad_ps"] = ps
+
+    # 6. Pauli-sum expectations on a random state.
+    rs = np.random.RandomState(11)
+    n = 6
+    psi = rs.normal(size=2**n) + 1j * rs.normal(size=2**n)
+    psi /= np.linalg.norm(psi)
+    qs = cirq.LineQubit.range(n)
+    ham = workloads.random_pauli_hamiltonian(n, 20, seed=12, min_w=1, max_w=4)
+    qmap = {x: i for i, x in enumerate(qs)}
+    out["pauli_n6_state"] = psi
+    out["pauli_n6_terms_expect"] = np.array(
+        [ps_.expectation_from_state_vector(psi, qmap) for ps_ in ham]
+    )
+    out["pauli_n6_sum_expect"] = np.array(ham.expectation_from_state_vector(psi, qmap))
+
+    # 7. marginal probabilities used for sampling.
+    probs = np.abs(psi) ** 2
+    for idx in ([0, 1, 2, 3, 4, 5], [2], [4, 1], [5, 0, 3]):
+        key = "probs_n6_" + "_".join(map(str, idx))
+        out[key] = cirq.sim.simulation_utils.state_probabilities_by_indices(probs, idx, (2,) * n)
+
+    # 8. known answers copied from the reference's own tests, kept as data.
+    out["known_expect_c1"] = np.array([-2.2, 0.0])  # sparse_simulator_test.py:638-640
+    out["known_expect_c2"] = np.array([0.0, 1.0])  # :643-645
+    out["known_expect_c3"] = np.array([2.0])  # :650
+    out["known_dm_ad"] = np.array([-0.8, 0.0])  # density_matrix_simulator_test.py:899-900
+    out["known_dm_dep"] = np.array([0.0, 0.6])  # :904-905
+
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
+    with open(os.path.join(HERE, "golden_meta.txt"), "w") as f:
+        f.write(f"generated by tests/golden/make_golden.py with cirq {cirq.__version__}\n")
+        for k in sorted(out):
+            f.write(f"{k}: shape={np.shape(out[k])} dtype={np.asarray(out[k]).dtype}\n")
+    print("wrote", len(out), "arrays")
+
+
+def _gate_zoo(cirq):
+    """A circuit that touches every gate family the GPU translator handles."""
+    q = cirq.LineQubit.range(5)
+    return cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.X(q[0]) ** 0.3,
+        cirq.Y(q[1]) ** 0.7,
+        cirq.Z(q[2]) ** 0.11,
+        cirq.rx(0.4).on(q[3]),
+        cirq.ry(-1.1).on(q[4]),
+        cirq.rz(2.3).on(q[0]),
+        cirq.S(q[1]),
+        cirq.T(q[2]),
+        cirq.CNOT(q[0], q[3]),
+        cirq.CZ(q[1], q[4]) ** 0.37,
+        cirq.SWAP(q[2], q[0]),
+        cirq.ISWAP(q[3], q[4]) ** 0.5,
+        cirq.ZZ(q[0], q[4]) ** 0.21,
+        cirq.XX(q[1], q[2]) ** 0.4,
+        cirq.YY(q[3], q[0]) ** -0.6,
+        cirq.CCZ(q[0], q[1], q[2]),
+        cirq.CCX(q[2], q[3], q[4]),
+        cirq.CSWAP(q[4], q[0], q[1]),
+        cirq.FSimGate(0.3, 0.9).on(q[1], q[3]),
+        cirq.PhasedXPowGate(phase_exponent=0.25, exponent=0.5).on(q[2]),
+        cirq.PhasedXZGate(x_exponent=0.3, z_exponent=-0.2, axis_phase_exponent=0.6).on(q[4]),
+        cirq.MatrixGate(cirq.testing.random_unitary(4, random_state=3)).on(q[4], q[1]),
+        cirq.DiagonalGate([0.1, 0.5, -0.7, 1.3]).on(q[3], q[2]),
+        cirq.ControlledGate(cirq.Y ** 0.25).on(q[0], q[4]),
+        cirq.global_phase_operation(np.exp(0.3j)),
+        cirq.I(q[2]),
+        cirq.MatrixGate(cirq.testing.random_unitary(8, random_state=4)).on(q[0], q[2], q[4]),
+    )
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/cirq-core")

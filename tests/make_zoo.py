@@ -1,0 +1,14 @@
+"""The gate-zoo circuit of tests/golden/make_golden.py (kept in sync by test_golden_zoo_matches)."""
+
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+
+def gate_zoo():
+    import cirq
+    import make_golden
+
+    return make_golden._gate_zoo(cirq)

@@ -1,0 +1,66 @@
+"""State-vector parity on the GPU: cirq_gb300.Simulator vs the reference's
+golden states and the complex128 CPU oracle."""
+
+import numpy as np
+import pytest
+
+import cirq
+import cirq_gb300
+from cirq_gb300 import workloads
+from oracle.circuits import simulate_state_vector
+
+pytestmark = pytest.mark.gpu
+
+GOLD = np.load(__file__.replace("test_gpu_statevector.py", "golden/golden.npz"))
+TOL = 1e-5  # max amplitude error for complex64
+
+
+@pytest.mark.parametrize("n,d,s", [(10, 20, 1), (12, 8, 2), (5, 6, 3)])
+@pytest.mark.parametrize(
+    "cfg",
+    [dict(), dict(tile_bits=8, fusion_max_qubits=3, pass_budget=20), dict(tile_bits=6, fusion_max_qubits=2, pass_budget=8),
+     dict(tile_bits=7, fusion_max_qubits=5, pass_budget=200), dict(tile_bits=10, fusion_max_qubits=1, pass_budget=10)],
+)
+def test_layers_vs_golden(n, d, s, cfg):
+    c = workloads.random_layer_circuit(n, d, s)
+    got = cirq_gb300.Simulator(**cfg).simulate(c).final_state_vector
+    assert got.dtype == np.complex64
+    np.testing.assert_allclose(got, GOLD[f"layers_n{n}_d{d}_s{s}_c128"], atol=TOL)
+    np.testing.assert_allclose(got, GOLD[f"layers_n{n}_d{d}_s{s}_c64"], atol=TOL)
+
+
+def test_reversed_order_and_initial_state():
+    c = workloads.random_layer_circuit(6, 5, 4)
+    q = sorted(c.all_qubits())
+    got = cirq_gb300.Simulator().simulate(c, qubit_order=q[::-1], initial_state=5).final_state_vector
+    np.testing.assert_allclose(got, GOLD["layers_n6_d5_s4_reversed_init5"], atol=TOL)
+
+
+def test_gate_zoo():
+    import make_zoo
+
+    zoo = make_zoo.gate_zoo()
+    got = cirq_gb300.Simulator().simulate(zoo).final_state_vector
+    np.testing.assert_allclose(got, GOLD["zoo_c128"], atol=TOL)
+
+
+@pytest.mark.parametrize("n", [16, 18, 20])
+def test_larger_vs_oracle(n):
+    c = workloads.random_layer_circuit(n, 10, seed=n)
+    got = cirq_gb300.Simulator().simulate(c).final_state_vector
+    want = simulate_state_vector(c)
+    assert np.max(np.abs(got - want)) < TOL
+
+
+def test_known_expectations():
+    """Known answers of the reference's own test (sparse_simulator_test.py:630-651)."""
+    q0, q1 = cirq.LineQubit.range(2)
+    psum1 = cirq.Z(q0) + 3.2 * cirq.Z(q1)
+    psum2 = -1 * cirq.X(q0) + 2 * cirq.X(q1)
+    sim = cirq_gb300.Simulator()
+    r = sim.simulate_expectation_values(cirq.Circuit(cirq.I(q0), cirq.X(q1)), [psum1, psum2])
+    np.testing.assert_allclose(np.real(r), GOLD["known_expect_c1"], atol=1e-6)
+    r = sim.simulate_expectation_values(cirq.Circuit(cirq.H(q0), cirq.H(q1)), [psum1, psum2])
+    np.testing.assert_allclose(np.real(r), GOLD["known_expect_c2"], atol=1e-6)
+    r = sim.simulate_expectation_values(cirq.Circuit(cirq.I(q0), cirq.H(q1)), cirq.Z(q0) + cirq.X(q1))
+    np.testing.assert_allclose(np.real(r), GOLD["known_expect_c3"], atol=1e-6)
