@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import asyncio
 import importlib
+import importlib.util
 import importlib.abc
 import importlib.machinery
 import os
