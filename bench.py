@@ -1,0 +1,442 @@
+"""Benchmark: 30-qubit random-layer circuit, gate-updates/s and HBM roofline.
+
+Workload (one "step"): simulate the 30-qubit, depth-40 random-layer circuit
+(PhasedXZ(x, z, a ~ U(-1,1)) on every qubit, then CZ on alternating pairs;
+1780 gates) from |0...0> on one GB300: prepare the basis state and run every
+fused tile pass of the plan.  The 8 GiB state is larger than L2, so no L2
+flush is needed between steps.
+
+Printed JSON line (rank 0):
+  value      gate-updates/s = gates / device time per step (state resident in HBM)
+  e2e        the same metric through cirq_gb300.Simulator.simulate() -- circuit
+             in, final state vector out in host memory (H2D of the matrix pool
+             and D2H of the 8 GiB state inside the timed region)
+  roofline   dominant kernel k_tile_pass: algorithmic bytes per launch
+             (16 B x 2^30: one read + one write of the state) / mean launch time
+  cpu_baseline  the reference's numpy cirq.Simulator on a bounded gate sample
+  fusion_sweep  gate-updates/s for fusion width k = 1..5
+
+`--impl reference` times the reference (cirq.Simulator, complex64) on the
+host cores instead and prints the reference line.  Under torchrun with N > 1
+every rank simulates its own replica (replicas only: the workload has no
+cross-GPU exchange on one-GPU machines); value = N x gates / max time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "30q gate-updates/s & % HBM peak; 24q adjoint grads/s vs plain param-shift"
+UNIT = "gate-updates/s"
+
+
+def _cirq():
+    from cirq_gb300._cirq_env import ensure_cirq
+
+    return ensure_cirq((os.path.join(ROOT, "baseline", "_ref"),))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks/throttle reasons while the timed region runs."""
+
+    Q = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        return {
+            "sm_mhz": statistics.median(sm),
+            "sm_max_mhz": mx,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def build_workload(n: int, depth: int, seed: int):
+    from cirq_gb300 import workloads
+
+    circuit = workloads.random_layer_circuit(n, depth, seed)
+    return circuit, len(list(circuit.all_operations()))
+
+
+def compile_plan(circuit, planner):
+    cirq = _cirq()
+    from cirq_gb300.program import CompiledCircuit, split_measurements
+
+    body, _ = split_measurements(circuit)
+    qubits = sorted(circuit.all_qubits())
+    return CompiledCircuit(body, qubits, dm=False, planner=planner, resolvers=[cirq.ParamResolver({})])
+
+
+def device_steps(eng, compiled, steps: int, warmup: int, pass_timing: bool):
+    """Times `steps` simulations with the state resident in HBM.
+
+    Returns (ms per step, mean tile-pass launch ms, tile-pass launches per step,
+    kernel launches per step)."""
+    nbits = compiled.nbits
+    state = eng.alloc(8 << nbits)
+    pool = eng.upload(compiled.plan.pool)
+    plan = compiled.plan
+
+    from cirq_gb300._lib import check
+
+    def one():
+        check(eng.lib.gbq_sv_set_basis(eng.ctx, state.ptr, nbits, 0), "gbq_sv_set_basis")
+        check(
+            eng.lib.gbq_run(
+                eng.ctx, state.ptr, nbits, plan.passes.ctypes.data, len(plan.passes),
+                plan.ops.ctypes.data, len(plan.ops), pool.ptr,
+            ),
+            "gbq_run",
+        )
+
+    for _ in range(warmup):
+        one()
+    eng.sync()
+    if pass_timing:
+        eng.set_pass_timing(True)
+    l0 = eng.launches()
+    eng.event(0)
+    for _ in range(steps):
+        one()
+    eng.event(1)
+    ms = eng.elapsed_ms(0, 1)
+    launches = (eng.launches() - l0) / steps
+    pass_ms, pass_n = (0.0, 0)
+    if pass_timing:
+        pass_ms, pass_n = eng.pass_timing()
+        eng.set_pass_timing(False)
+    state.free()
+    pool.free()
+    mean_pass = pass_ms / pass_n if pass_n else None
+    return ms / steps, mean_pass, (pass_n / steps if pass_n else plan.npasses), launches
+
+
+def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
+    """Times Simulator.simulate() end to end: returns (s per step, h2d bytes, d2h bytes)."""
+    import cirq_gb300
+
+    sim = cirq_gb300.Simulator(**planner_kwargs)
+    for _ in range(warmup):
+        r = sim.simulate(circuit)
+        _ = r.final_state_vector
+        del r
+    times = []
+    vec_bytes = 0
+    for _ in range(steps):
+        t = time.perf_counter()
+        r = sim.simulate(circuit)
+        vec = r.final_state_vector
+        times.append(time.perf_counter() - t)
+        vec_bytes = vec.nbytes
+        del r, vec
+    compiled = next(iter(sim._cache.values()))
+    return float(np.mean(times)), int(compiled.plan.pool.nbytes), int(vec_bytes)
+
+
+# ---------------------------------------------------------------------------
+# reference (numpy cirq.Simulator) timing on a bounded gate sample
+def reference_gate_rates(n: int, circuit, sample_1q: int = 2, sample_2q: int = 1, repeat: int = 1):
+    """Seconds per PhasedXZ and per CZ of the reference cirq.Simulator(complex64)
+    on a dense n-qubit state (split_untangled_states=False, so no product-state
+    shortcut).  Returns (s_per_1q, s_per_2q, sample description)."""
+    cirq = _cirq()
+    qubits = sorted(circuit.all_qubits())
+    ops = list(circuit.all_operations())
+    ones = [op for op in ops if len(op.qubits) == 1][:sample_1q]
+    twos = [op for op in ops if len(op.qubits) == 2][:sample_2q]
+    sim = cirq.Simulator(dtype=np.complex64, split_untangled_states=False)
+    init = np.full(2**n, 2.0 ** (-n / 2), dtype=np.complex64)
+
+    def timed(opl):
+        c = cirq.Circuit(opl)
+        best = None
+        for _ in range(repeat):
+            t = time.perf_counter()
+            sim.simulate(c, qubit_order=qubits, initial_state=init)
+            dt = time.perf_counter() - t
+            best = dt if best is None else min(best, dt)
+        return best
+
+    t_empty = timed([cirq.I(qubits[0])])  # state setup + result assembly
+    t1 = max(timed(ones) - t_empty, 1e-9) / max(len(ones), 1)
+    t2 = max(timed(twos) - t_empty, 1e-9) / max(len(twos), 1)
+    desc = (
+        f"{len(ones)} PhasedXZ + {len(twos)} CZ of the workload on a dense {n}-qubit complex64 "
+        f"state, setup subtracted; rate extrapolated to the workload's gate mix"
+    )
+    return t1, t2, desc
+
+
+def reference_rate(n, circuit):
+    ops = list(circuit.all_operations())
+    n1 = sum(1 for op in ops if len(op.qubits) == 1)
+    n2 = len(ops) - n1
+    t1, t2, desc = reference_gate_rates(n, circuit)
+    secs = n1 * t1 + n2 * t2
+    return len(ops) / secs, secs, desc
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    circuit, ngates = build_workload(args.n, args.depth, args.seed)
+    vals = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        v, secs, desc = reference_rate(args.n, circuit)
+        if i >= args.warmup:
+            vals.append(v)
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * ngates / v,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64",
+        "data": "synthetic",
+        "config": {"workload": f"random-layer circuit {args.n}q depth {args.depth} ({ngates} gates), seed {args.seed}"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "reference",
+                         "sample": desc + " (numpy path is single-threaded)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tile-bits", type=int, default=12)
+    ap.add_argument("--kmax", type=int, default=4)
+    ap.add_argument("--budget", type=float, default=40.0)
+    ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    _cirq()
+    from cirq_gb300.engine import Engine
+    from cirq_gb300.planner import Planner
+
+    eng = Engine.get(local)
+    circuit, ngates = build_workload(args.n, args.depth, args.seed)
+    planner = Planner(tile_bits=args.tile_bits, kmax=args.kmax, budget=args.budget)
+    t0 = time.perf_counter()
+    compiled = compile_plan(circuit, planner)
+    plan_s = time.perf_counter() - t0
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    barrier()
+    with ClockSampler(local) as clocks:
+        ms_step, pass_ms, passes_per_step, launches = device_steps(
+            eng, compiled, args.steps, args.warmup, pass_timing=True
+        )
+    barrier()
+    if dist is not None:
+        import torch
+
+        t = torch.tensor([ms_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * ngates / (ms_step / 1e3)
+
+    peak, peak_kind = peaks()
+    alg_bytes = 16 * (1 << compiled.nbits)
+    achieved = alg_bytes / (pass_ms / 1e3) / 1e9 if pass_ms else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "tile_pass_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        if tj.get("nbits") and tj.get("dram_bytes_per_launch"):
+            traffic = tj["dram_bytes_per_launch"] * (1 << compiled.nbits) / (1 << tj["nbits"])
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        kw = dict(tile_bits=args.tile_bits, fusion_max_qubits=args.kmax, pass_budget=args.budget)
+        e2e_s, h2d, d2h = e2e_steps(circuit, kw, steps=min(args.steps, 3), warmup=1)
+        e2e = {"value": ngates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "s_per_step": e2e_s}
+
+    sweep = None
+    if not args.no_sweep and rank == 0:
+        sweep = {}
+        for k in range(1, 6):
+            pk = Planner(tile_bits=args.tile_bits, kmax=k, budget=args.budget)
+            ck = compile_plan(circuit, pk)
+            msk, pmk, ppk, _ = device_steps(eng, ck, 2, 1, pass_timing=True)
+            sweep[str(k)] = {
+                "gate_updates_per_s": ngates / (msk / 1e3),
+                "passes": int(ck.plan.npasses),
+                "ms_per_step": msk,
+                "hbm_frac": (16 * (1 << ck.nbits) / (pmk / 1e3) / 1e9) / peak if pmk else None,
+            }
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        try:
+            v, secs, desc = reference_rate(args.n, circuit)
+            cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "reference",
+                   "sample": desc + " (numpy path is single-threaded)"}
+        except MemoryError as e:  # pragma: no cover
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "reference", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "c64",
+            "data": "synthetic",
+            "config": {
+                "workload": f"random-layer circuit {args.n}q depth {args.depth} ({ngates} gates), seed {args.seed}",
+                "state_bytes": 8 << compiled.nbits,
+                "l2": "state (8 GiB) larger than L2; no flush needed",
+                "tile_bits": args.tile_bits,
+                "fusion_max_qubits": args.kmax,
+                "pass_budget": args.budget,
+                "passes_per_step": int(compiled.plan.npasses),
+                "fused_ops": int(len(compiled.plan.ops)),
+                "plan_seconds": round(plan_s, 3),
+                "parallelism": f"replicas x{world}",
+            },
+            "hbm_frac": (achieved / peak) if achieved else None,
+            "roofline": {
+                "kernel": "k_tile_pass",
+                "bound": "hbm",
+                "achieved": achieved,
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "mean_launch_ms": pass_ms,
+                "launches_per_step": passes_per_step,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            },
+            "gpu_launches": int(round(launches * args.steps)),
+            "clocks": clocks.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "fusion_sweep": sweep,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -161,6 +161,10 @@ SIGNATURES = {
     "gbq_device_info": [_P, _P, _P, _P],
     "gbq_set_graphs": [_P, _I],
     "gbq_launch_count": [_P, _P],
+    "gbq_event_record": [_P, _I],
+    "gbq_event_elapsed": [_P, _I, _I, _P],
+    "gbq_set_pass_timing": [_P, _I],
+    "gbq_pass_timing": [_P, _P, _P],
     "gbq_alloc": [_P, _SZ, _P],
     "gbq_free": [_P, _P],
     "gbq_host_alloc": [_SZ, _P],

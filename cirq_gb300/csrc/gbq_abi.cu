@@ -170,6 +170,19 @@ static int build_tile_info(const gbq_pass& p, const gbq_op* ops, int nops, int n
   return GBQ_OK;
 }
 
+static int timed_pair(Ctx* c, std::pair<cudaEvent_t, cudaEvent_t>& ev) {
+  if (!c->event_pool.empty()) {
+    ev = c->event_pool.back();
+    c->event_pool.pop_back();
+    return GBQ_OK;
+  }
+  cudaError_t e = cudaEventCreate(&ev.first);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  e = cudaEventCreate(&ev.second);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  return GBQ_OK;
+}
+
 static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pass* passes,
                       int npasses, const gbq_op* ops, int nops, const float2* mats,
                       double* partial) {
@@ -184,8 +197,18 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
     a.ti.mats = mats;
     a.ti.partial = partial;
     memcpy(a.ops, ops + passes[q].op_begin, sizeof(gbq_op) * passes[q].op_count);
+    std::pair<cudaEvent_t, cudaEvent_t> ev;
+    if (c->pass_timing) {
+      rc = timed_pair(c, ev);
+      if (rc) return rc;
+      cudaEventRecord(ev.first, c->stream);
+    }
     rc = launch_pass(c, a, dual);
     if (rc) return rc;
+    if (c->pass_timing) {
+      cudaEventRecord(ev.second, c->stream);
+      c->timed.push_back(ev);
+    }
   }
   return GBQ_OK;
 }
@@ -246,6 +269,16 @@ int gbq_ctx_destroy(gbq_ctx* c) {
   cudaStreamSynchronize(c->stream);
   if (c->scratch) cudaFree(c->scratch);
   if (c->host_scratch) cudaFreeHost(c->host_scratch);
+  for (auto& ev : c->timed) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  for (auto& ev : c->event_pool) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  for (auto& ev : c->events)
+    if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(c->stream);
   delete c;
   return GBQ_OK;
@@ -276,6 +309,58 @@ int gbq_set_graphs(gbq_ctx* c, int enable) {
 int gbq_launch_count(gbq_ctx* c, int64_t* out) {
   if (!c || !out) return arg_fail("null argument");
   *out = c->launches;
+  return GBQ_OK;
+}
+
+int gbq_event_record(gbq_ctx* c, int slot) {
+  CHECK_CTX(c);
+  if (slot < 0 || slot >= 16) return arg_fail("event slot out of range (0..15)");
+  cudaError_t e;
+  if (!c->events[slot]) {
+    e = cudaEventCreate(&c->events[slot]);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  }
+  e = cudaEventRecord(c->events[slot], c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+  return GBQ_OK;
+}
+
+int gbq_event_elapsed(gbq_ctx* c, int a, int b, float* ms) {
+  CHECK_CTX(c);
+  if (a < 0 || a >= 16 || b < 0 || b >= 16 || !c->events[a] || !c->events[b] || !ms)
+    return arg_fail("gbq_event_elapsed: events not recorded");
+  cudaError_t e = cudaEventSynchronize(c->events[b]);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize");
+  e = cudaEventElapsedTime(ms, c->events[a], c->events[b]);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
+  return GBQ_OK;
+}
+
+int gbq_pass_timing(gbq_ctx* c, double* total_ms, int64_t* launches) {
+  CHECK_CTX(c);
+  for (auto& ev : c->timed) {
+    cudaError_t e = cudaEventSynchronize(ev.second);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize");
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev.first, ev.second);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
+    c->timed_ms += ms;
+    c->timed_launches += 1;
+    c->event_pool.push_back(ev);
+  }
+  c->timed.clear();
+  if (total_ms) *total_ms = c->timed_ms;
+  if (launches) *launches = c->timed_launches;
+  return GBQ_OK;
+}
+
+int gbq_set_pass_timing(gbq_ctx* c, int enable) {
+  CHECK_CTX(c);
+  int rc = gbq_pass_timing(c, nullptr, nullptr);  // drain pending events
+  if (rc) return rc;
+  c->pass_timing = enable != 0;
+  c->timed_ms = 0.0;
+  c->timed_launches = 0;
   return GBQ_OK;
 }
 

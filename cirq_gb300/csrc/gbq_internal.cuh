@@ -5,6 +5,8 @@
 #include <stdint.h>
 
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/cirq_gb300.h"
 
@@ -48,6 +50,13 @@ struct Ctx {
   size_t scratch_bytes = 0;
   void* host_scratch = nullptr;  // pinned
   size_t host_scratch_bytes = 0;
+  cudaEvent_t events[16] = {};
+  // per-launch tile-pass timing
+  bool pass_timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;  // pending (start, stop)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> event_pool;
+  double timed_ms = 0.0;
+  int64_t timed_launches = 0;
 };
 
 int ensure_scratch(Ctx* c, size_t bytes);

@@ -151,6 +151,24 @@ class Engine:
         check(self.lib.gbq_launch_count(self.ctx, ctypes.byref(v)))
         return v.value
 
+    # ---- timing ----------------------------------------------------------
+    def event(self, slot: int) -> None:
+        check(self.lib.gbq_event_record(self.ctx, slot), "gbq_event_record")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = ctypes.c_float()
+        check(self.lib.gbq_event_elapsed(self.ctx, a, b, ctypes.byref(v)), "gbq_event_elapsed")
+        return v.value
+
+    def set_pass_timing(self, enable: bool) -> None:
+        check(self.lib.gbq_set_pass_timing(self.ctx, int(enable)), "gbq_set_pass_timing")
+
+    def pass_timing(self) -> tuple[float, int]:
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(self.lib.gbq_pass_timing(self.ctx, ctypes.byref(ms), ctypes.byref(n)), "gbq_pass_timing")
+        return ms.value, n.value
+
     # ---- state vectors -------------------------------------------------
     def new_state(self, nbits: int, basis: int = 0, initial: np.ndarray | None = None) -> DeviceBuffer:
         buf = self.alloc(8 * (1 << nbits))

@@ -253,8 +253,14 @@ class CompiledCircuit:
         sub = {j: batch[i][:1] for j, i in enumerate(keep)}
         self.plan = self.planner.plan(gates, self.nbits, batch=sub)
 
+    @property
+    def parameterized(self) -> bool:
+        return any(self.sources[i].const is None for i in self.kept)
+
     def pool(self, resolvers) -> np.ndarray:
         """complex64 (P, pool_len) matrix pools for the resolvers."""
+        if not self.parameterized:
+            return np.broadcast_to(self.plan.pool, (len(resolvers), len(self.plan.pool)))
         batch = self.gate_batch(resolvers)
         sub = {j: np.asarray(batch[i]) for j, i in enumerate(self.kept)}
         return self.plan.pool_for(sub, len(resolvers))

@@ -105,6 +105,15 @@ int gbq_device_info(gbq_ctx* ctx, int* sm_count, size_t* free_bytes, size_t* tot
 int gbq_set_graphs(gbq_ctx* ctx, int enable);
 /* Number of kernels this context has launched (for launch accounting). */
 int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
+/* Stream-ordered timing: records CUDA event `slot` (0..15) on the context's
+ * stream; gbq_event_elapsed waits for event b and returns the ms from a to b. */
+int gbq_event_record(gbq_ctx* ctx, int slot);
+int gbq_event_elapsed(gbq_ctx* ctx, int a, int b, float* ms);
+/* Per-launch timing of tile passes: when enabled, every tile-pass launch is
+ * bracketed by CUDA events on the context's stream and its duration added to
+ * a running total (read with gbq_pass_timing, which synchronises). */
+int gbq_set_pass_timing(gbq_ctx* ctx, int enable);
+int gbq_pass_timing(gbq_ctx* ctx, double* total_ms, int64_t* launches);
 
 int gbq_alloc(gbq_ctx* ctx, size_t bytes, void** dptr);
 int gbq_free(gbq_ctx* ctx, void* dptr);
