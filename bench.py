@@ -143,7 +143,7 @@ def device_steps(eng, compiled, steps: int, warmup: int, pass_timing: bool):
 
     Returns (ms per step, mean tile-pass launch ms, tile-pass launches per step,
     kernel launches per step)."""
-    nbits = compiled.nbits
+    nbits = compiled.nbits_dev
     state = eng.alloc(8 << nbits)
     pool = eng.upload(compiled.plan.pool)
     plan = compiled.plan

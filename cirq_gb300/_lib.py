@@ -38,8 +38,8 @@ OP_DTYPE = np.dtype(
         ("pad0", "i1"),
         ("bits", "i1", (8,)),
         ("sel", "i1", (4,)),
-        ("gorder", "i1", (16,)),
         ("slot", "i4"),
+        ("pad1", "i4"),
         ("mat", "i8"),
     ],
     align=True,

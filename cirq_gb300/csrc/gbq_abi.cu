@@ -90,84 +90,151 @@ static int sync(Ctx* c, const char* what) {
   return GBQ_OK;
 }
 
-// Validates one pass and its ops against a state of nbits bits; fills `ti`.
-static int build_tile_info(const gbq_pass& p, const gbq_op* ops, int nops, int nbits,
-                           bool dual, TileInfo& ti) {
-  if (p.L < 1 || p.L > GBQ_MAX_TILE_BITS || p.L > nbits)
-    return arg_fail("pass: tile bits L=" + std::to_string(p.L) + " invalid for " +
-                    std::to_string(nbits) + "-bit state");
+// Bank-pair column (shared index mod 16) of tile bit b.
+static uint32_t bank_col(int b) { return phys_const(1u << b) & 15u; }
+
+// Converts one public op into its device form for a pass whose tile bits
+// are described by `inmask` (global bits in the tile).  The group index of a
+// dense op enumerates its non-target tile bits in this order: 4 bits whose
+// bank columns are independent (conflict-free half-warps), the other free
+// bits, then the tile bits used as selectors (so a selector is uniform over
+// a warp and the matrix loads do not diverge).
+static int convert_op(const gbq_op& op, int L, int nbits, uint64_t inmask, bool dual, OpDev& d) {
+  memset(&d, 0, sizeof(d));
+  const bool dense = op.kind == GBQ_OP_DENSE || op.kind == GBQ_OP_PROBE;
+  const bool diag = op.kind == GBQ_OP_DIAG || op.kind == GBQ_OP_PROBE_DIAG;
+  if (!dense && !diag) return arg_fail("op: unknown kind");
+  if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && !dual)
+    return arg_fail("op: probe ops need a two-state pass");
+  if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && op.slot < 0)
+    return arg_fail("op: probe slot < 0");
+  if (op.mat < 0 || (op.mat & 1)) return arg_fail("op: matrix offset must be even and >= 0");
+  d.kind = op.kind;
+  d.k = op.k;
+  d.slot = op.slot;
+  d.mat = op.mat;
+  if (dense) {
+    const int kmax = op.kind == GBQ_OP_PROBE ? 3 : GBQ_MAX_DENSE_K;
+    if (op.k < 1 || op.k > kmax || op.k > L) return arg_fail("op: dense k out of range");
+    if (op.nsel < 0 || op.nsel > 3) return arg_fail("op: nsel out of range");
+    uint32_t tmask = 0;
+    for (int j = 0; j < op.k; ++j) {
+      const int b = op.bits[j];
+      if (b < 0 || b >= L || ((tmask >> b) & 1u)) return arg_fail("op: dense target bit invalid");
+      tmask |= 1u << b;
+      d.pcol[j] = phys_const(1u << b);
+    }
+    uint32_t smask = 0;
+    for (int j = 0; j < op.nsel; ++j) {
+      const int s = op.sel[j];
+      if (s >= 0) {
+        if (s >= L) return arg_fail("op: selector tile bit out of range");
+        if ((tmask >> s) & 1u) return arg_fail("op: selector bit is a target");
+        if ((smask >> s) & 1u) return arg_fail("op: duplicate selector bit");
+        smask |= 1u << s;
+      } else {
+        const int gb = -s - 1;
+        if (gb >= nbits || ((inmask >> gb) & 1ull))
+          return arg_fail("op: selector global bit invalid (must be outside the tile)");
+      }
+    }
+    int order[GBQ_MAX_TILE_BITS];
+    int no = 0;
+    uint32_t basis[4] = {0, 0, 0, 0};
+    int nbasis = 0;
+    uint32_t used = tmask | smask;
+    for (int b = 0; b < L && nbasis < 4; ++b) {
+      if ((used >> b) & 1u) continue;
+      uint32_t v = bank_col(b);
+      for (int i = 0; i < nbasis; ++i)
+        if ((v ^ basis[i]) < v) v ^= basis[i];
+      if (!v) continue;
+      basis[nbasis++] = v;
+      // keep the basis sorted descending so the reduction above is valid
+      for (int i = nbasis - 1; i > 0 && basis[i] > basis[i - 1]; --i) {
+        const uint32_t t = basis[i];
+        basis[i] = basis[i - 1];
+        basis[i - 1] = t;
+      }
+      order[no++] = b;
+      used |= 1u << b;
+    }
+    for (int b = 0; b < L; ++b)
+      if (!((used >> b) & 1u)) order[no++] = b;
+    for (int j = 0; j < op.nsel; ++j)
+      if (op.sel[j] >= 0) order[no++] = op.sel[j];
+    if (no != L - op.k) return arg_fail("op: internal group order error");
+    for (int i = 0; i < no; ++i) d.gcol[i] = phys_const(1u << order[i]);
+    d.nsel = op.nsel;
+    for (int j = 0; j < op.nsel; ++j) {
+      const int s = op.sel[j];
+      if (s >= 0) {
+        int pos = -1;
+        for (int i = 0; i < no; ++i)
+          if (order[i] == s) pos = i;
+        d.selg[j] = (int8_t)pos;
+      } else {
+        d.selg[j] = (int8_t)s;
+      }
+    }
+  } else {
+    if (op.k < 1 || op.k > GBQ_MAX_DIAG_K) return arg_fail("op: diag k out of range");
+    for (int j = 0; j < 8; ++j) d.dext[j] = -1;
+    for (int j = 0; j < op.k; ++j) {
+      const int s = op.bits[j];
+      if (s >= 0) {
+        if (s >= L) return arg_fail("op: diag tile bit out of range");
+        if (d.dcol[s]) return arg_fail("op: duplicate diag bit");
+        d.dcol[s] = (uint16_t)(1u << j);
+      } else {
+        const int gb = -s - 1;
+        if (gb >= nbits || ((inmask >> gb) & 1ull)) return arg_fail("op: diag global bit invalid");
+        d.dext[j] = (int8_t)gb;
+      }
+    }
+  }
+  return GBQ_OK;
+}
+
+// Validates one pass against a state of nbits bits; fills `ti` (not the
+// pointers) and the tile-membership mask.
+static int pass_geometry(const gbq_pass& p, int nops, int nbits, TileInfo& ti, uint64_t& inmask) {
+  if (p.L < GBQ_MIN_TILE_BITS || p.L > GBQ_MAX_TILE_BITS || p.L > nbits)
+    return arg_fail("pass: tile bits L=" + std::to_string(p.L) + " invalid for a " +
+                    std::to_string(nbits) + "-bit state (need 10 <= L <= min(13, nbits))");
   if (p.m < 1 || p.m > p.L) return arg_fail("pass: contiguous bits m out of range");
   if (p.op_count < 0 || p.op_count > GBQ_MAX_OPS_PER_PASS)
     return arg_fail("pass: op_count out of range (max 64)");
   if (p.op_begin < 0 || p.op_begin + p.op_count > nops) return arg_fail("pass: ops out of range");
-  uint64_t inmask = (p.m >= 64) ? ~0ull : ((1ull << p.m) - 1ull);
+  inmask = (1ull << p.m) - 1ull;
+  memset(&ti, 0, sizeof(ti));
+  for (int b = 0; b < p.m; ++b) ti.gw[b] = 1ull << b;
   for (int j = 0; j < p.L - p.m; ++j) {
     const int b = p.hi[j];
     if (b < p.m || b >= nbits) return arg_fail("pass: tile high bit out of range");
     if ((inmask >> b) & 1ull) return arg_fail("pass: duplicate tile bit");
     inmask |= 1ull << b;
+    ti.gw[p.m + j] = 1ull << b;
   }
-  memset(&ti, 0, sizeof(ti));
   ti.nbits = nbits;
   ti.L = p.L;
   ti.m = p.m;
   ti.nops = p.op_count;
   ti.ntiles = (int64_t)1 << (nbits - p.L);
-  for (int j = 0; j < 16; ++j) ti.hi[j] = p.hi[j];
   int c = 0;
   for (int b = 0; b < nbits; ++b)
     if (!((inmask >> b) & 1ull)) ti.nt[c++] = (int8_t)b;
-  for (int o = 0; o < p.op_count; ++o) {
-    const gbq_op& op = ops[p.op_begin + o];
-    const bool dense = op.kind == GBQ_OP_DENSE || op.kind == GBQ_OP_PROBE;
-    const bool diag = op.kind == GBQ_OP_DIAG || op.kind == GBQ_OP_PROBE_DIAG;
-    if (!dense && !diag) return arg_fail("op: unknown kind");
-    if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && !dual)
-      return arg_fail("op: probe ops need a two-state pass");
-    if (op.mat < 0 || (op.mat & 1)) return arg_fail("op: matrix offset must be even and >= 0");
-    if (dense) {
-      const int kmax = op.kind == GBQ_OP_PROBE ? 3 : GBQ_MAX_DENSE_K;
-      if (op.k < 1 || op.k > kmax || op.k > p.L) return arg_fail("op: dense k out of range");
-      if (op.nsel < 0 || op.nsel > 3) return arg_fail("op: nsel out of range");
-      uint32_t used = 0;
-      for (int j = 0; j < op.k; ++j) {
-        if (op.bits[j] < 0 || op.bits[j] >= p.L || ((used >> op.bits[j]) & 1u))
-          return arg_fail("op: dense target bit invalid");
-        used |= 1u << op.bits[j];
-      }
-      for (int j = 0; j < p.L - op.k; ++j) {
-        if (op.gorder[j] < 0 || op.gorder[j] >= p.L || ((used >> op.gorder[j]) & 1u))
-          return arg_fail("op: group order invalid");
-        used |= 1u << op.gorder[j];
-      }
-      for (int j = 0; j < op.nsel; ++j) {
-        const int s = op.sel[j];
-        if (s >= 0) {
-          if (s >= p.L) return arg_fail("op: selector tile bit out of range");
-          for (int t = 0; t < op.k; ++t)
-            if (op.bits[t] == s) return arg_fail("op: selector bit is a target");
-        } else {
-          const int gb = -s - 1;
-          if (gb >= nbits || ((inmask >> gb) & 1ull))
-            return arg_fail("op: selector global bit invalid (must be outside the tile)");
-        }
-      }
-    } else {
-      if (op.k < 1 || op.k > GBQ_MAX_DIAG_K) return arg_fail("op: diag k out of range");
-      for (int j = 0; j < op.k; ++j) {
-        const int s = op.bits[j];
-        if (s >= 0) {
-          if (s >= p.L) return arg_fail("op: diag tile bit out of range");
-        } else {
-          const int gb = -s - 1;
-          if (gb >= nbits || ((inmask >> gb) & 1ull)) return arg_fail("op: diag global bit invalid");
-        }
-      }
-    }
-    if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && op.slot < 0)
-      return arg_fail("op: probe slot < 0");
-  }
   return GBQ_OK;
+}
+
+static int launch_pass(Ctx* c, const PassArgs& a, bool dual) {
+  switch (a.ti.L) {
+    case 10: return launch_pass_l10(c, a, dual);
+    case 11: return launch_pass_l11(c, a, dual);
+    case 12: return launch_pass_l12(c, a, dual);
+    case 13: return launch_pass_l13(c, a, dual);
+    default: return arg_fail("pass: unsupported tile width");
+  }
 }
 
 static int timed_pair(Ctx* c, std::pair<cudaEvent_t, cudaEvent_t>& ev) {
@@ -190,13 +257,17 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
   PassArgs a;
   for (int q = 0; q < npasses; ++q) {
     memset(&a, 0, sizeof(a));
-    int rc = build_tile_info(passes[q], ops, nops, nbits, dual, a.ti);
+    uint64_t inmask = 0;
+    int rc = pass_geometry(passes[q], nops, nbits, a.ti, inmask);
     if (rc) return rc;
+    for (int o = 0; o < passes[q].op_count; ++o) {
+      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual, a.ops[o]);
+      if (rc) return rc;
+    }
     a.psi = psi;
     a.lam = lam;
     a.ti.mats = mats;
     a.ti.partial = partial;
-    memcpy(a.ops, ops + passes[q].op_begin, sizeof(gbq_op) * passes[q].op_count);
     std::pair<cudaEvent_t, cudaEvent_t> ev;
     if (c->pass_timing) {
       rc = timed_pair(c, ev);
@@ -669,19 +740,32 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   if (npoints == 0) return GBQ_OK;
   if (max_nbits < 1 || max_nbits > 30) return arg_fail("gbq_batch_expect: max_nbits out of range (1..30)");
   if (!mats) return arg_fail("gbq_batch_expect: null matrix pool");
-  // validate every point's program on the host
+  // validate every point's program on the host and convert each pass's ops
+  std::vector<OpDev> dops((size_t)(nops ? nops : 1));
+  std::vector<char> converted((size_t)(npasses ? npasses : 1), 0);
   TileInfo ti;
   for (int p = 0; p < npoints; ++p) {
     const gbq_point& pt = points[p];
-    if (pt.nbits < 1 || pt.nbits > max_nbits) return arg_fail("gbq_batch_expect: point width out of range");
+    if (pt.nbits < 12 || pt.nbits > max_nbits)
+      return arg_fail("gbq_batch_expect: point width out of range (12 <= nbits <= max_nbits)");
     if (pt.pass_begin < 0 || pt.pass_count < 0 || pt.pass_begin + pt.pass_count > npasses)
       return arg_fail("gbq_batch_expect: point passes out of range");
     if (pt.term_begin < 0 || pt.term_count < 0 || pt.term_begin + pt.term_count > nterms)
       return arg_fail("gbq_batch_expect: point terms out of range");
     if (pt.mat_base < 0 || (pt.mat_base & 1)) return arg_fail("gbq_batch_expect: mat_base must be even");
     for (int q = 0; q < pt.pass_count; ++q) {
-      int rc = build_tile_info(passes[pt.pass_begin + q], ops, nops, pt.nbits, false, ti);
+      const gbq_pass& ps = passes[pt.pass_begin + q];
+      if (ps.L != 12) return arg_fail("gbq_batch_expect: batch passes must use 12-bit tiles");
+      uint64_t inmask = 0;
+      int rc = pass_geometry(ps, nops, pt.nbits, ti, inmask);
       if (rc) return rc;
+      for (int o = 0; o < ps.op_count; ++o) {
+        OpDev d;
+        rc = convert_op(ops[ps.op_begin + o], ps.L, pt.nbits, inmask, false, d);
+        if (rc) return rc;
+        if (!converted[pt.pass_begin + q]) dops[ps.op_begin + o] = d;
+      }
+      converted[pt.pass_begin + q] = 1;
     }
     int rc = validate_terms(terms + pt.term_begin, pt.term_count, pt.nbits);
     if (rc) return rc;
@@ -692,7 +776,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t b_points = al((size_t)npoints * sizeof(gbq_point));
   const size_t b_passes = al((size_t)(npasses ? npasses : 1) * sizeof(gbq_pass));
-  const size_t b_ops = al((size_t)(nops ? nops : 1) * sizeof(gbq_op));
+  const size_t b_ops = al((size_t)(nops ? nops : 1) * sizeof(OpDev));
   const size_t b_terms = al((size_t)(nterms ? nterms : 1) * sizeof(gbq_pauli));
   const size_t b_out = al((size_t)npoints * 2 * sizeof(double));
   const size_t b_counter = 256;
@@ -702,7 +786,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   char* base = reinterpret_cast<char*>(c->scratch);
   gbq_point* d_points = reinterpret_cast<gbq_point*>(base);
   gbq_pass* d_passes = reinterpret_cast<gbq_pass*>(base + b_points);
-  gbq_op* d_ops = reinterpret_cast<gbq_op*>(base + b_points + b_passes);
+  OpDev* d_ops = reinterpret_cast<OpDev*>(base + b_points + b_passes);
   gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(base + b_points + b_passes + b_ops);
   double* d_out = reinterpret_cast<double*>(base + b_points + b_passes + b_ops + b_terms);
   int* d_counter = reinterpret_cast<int*>(base + b_points + b_passes + b_ops + b_terms + b_out);
@@ -715,7 +799,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(passes)");
   }
   if (nops) {
-    e = cudaMemcpyAsync(d_ops, ops, (size_t)nops * sizeof(gbq_op), cudaMemcpyHostToDevice, c->stream);
+    e = cudaMemcpyAsync(d_ops, dops.data(), (size_t)nops * sizeof(OpDev), cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(ops)");
   }
   if (nterms) {

@@ -1,0 +1,126 @@
+// Persistent batch kernel: many parameter points (possibly of different
+// widths) in one launch.  Replaces the per-resolver loop of
+// SimulatesIntermediateState.simulate_sweep_iter (cirq-core/cirq/sim/simulator.py:558-605)
+// that feeds Simulator.simulate_expectation_values_sweep_iter
+// (cirq-core/cirq/sim/sparse_simulator.py:193-218).
+//
+// Each CTA repeatedly claims the next point with an atomic counter (no CTA
+// ever waits for another), simulates it alone in its own scratch slot with
+// the same 12-bit tile code as the single-state kernels, and writes the
+// point's expectation value <psi| sum_t c_t P_t |psi>.
+
+#include "gbq_tile.cuh"
+
+namespace gbq {
+
+constexpr int kBatchTile = 12;
+
+__global__ void __launch_bounds__(kThreads, 2)
+    k_batch(const gbq_point* __restrict__ points, int npoints, const gbq_pass* __restrict__ passes,
+            const OpDev* __restrict__ ops, const float2* __restrict__ mats,
+            const gbq_pauli* __restrict__ terms, float2* slots, int64_t slot_stride, int* counter,
+            double* out) {
+  constexpr int LT = kBatchTile;
+  extern __shared__ float4 smraw[];
+  __shared__ double red[kThreads / 32];
+  __shared__ TileInfo ti;
+  __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
+  __shared__ uint64_t soff[1 << (LT - 9)];
+  __shared__ int s_point;
+  float2* sm = reinterpret_cast<float2*>(smraw);
+  float2* psi = slots + (int64_t)blockIdx.x * slot_stride;
+  for (;;) {
+    if (threadIdx.x == 0) s_point = atomicAdd(counter, 1);
+    __syncthreads();
+    const int p = s_point;
+    __syncthreads();
+    if (p >= npoints) break;
+    const gbq_point pt = points[p];
+    const uint64_t dim = 1ull << pt.nbits;
+    for (uint64_t i = threadIdx.x; i < dim; i += kThreads) psi[i] = make_float2(i == 0 ? 1.f : 0.f, 0.f);
+    __syncthreads();
+    for (int q = 0; q < pt.pass_count; ++q) {
+      const gbq_pass& ps = passes[pt.pass_begin + q];
+      if (threadIdx.x == 0) {
+        ti.mats = mats + pt.mat_base;
+        ti.partial = nullptr;
+        ti.nbits = pt.nbits;
+        ti.L = ps.L;
+        ti.m = ps.m;
+        ti.nops = ps.op_count;
+        ti.ntiles = 1ll << (pt.nbits - ps.L);
+        uint64_t inmask = (1ull << ps.m) - 1ull;
+        for (int b = 0; b < ps.m; ++b) ti.gw[b] = 1ull << b;
+        for (int j = 0; j < ps.L - ps.m; ++j) {
+          ti.gw[ps.m + j] = 1ull << ps.hi[j];
+          inmask |= 1ull << ps.hi[j];
+        }
+        int c = 0;
+        for (int b = 0; b < pt.nbits; ++b)
+          if (!((inmask >> b) & 1ull)) ti.nt[c++] = (int8_t)b;
+      }
+      {
+        const int nwords = ps.op_count * (int)(sizeof(OpDev) / 4);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + ps.op_begin);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
+        for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
+      }
+      __syncthreads();
+      uint64_t off_t;
+      uint32_t ph_t;
+      pair_setup<LT>(ti, soff, off_t, ph_t);
+      __syncthreads();
+      for (int64_t tile = 0; tile < ti.ntiles; ++tile) {
+        const uint64_t gbase = tile_base(ti, tile);
+        load_tile<LT>(psi, sm, gbase, off_t, ph_t, soff);
+        __syncthreads();
+        run_ops<LT, 5, false>(ti, sops, sm, nullptr, gbase, tile, red);
+        store_tile<LT>(psi, sm, gbase, off_t, ph_t, soff);
+        __syncthreads();
+      }
+    }
+    // <psi| sum_t coef_t P_t |psi>, P_t = i^ny X^x Z^zy (sign on the input index)
+    double re_acc = 0.0, im_acc = 0.0;
+    for (int t = 0; t < pt.term_count; ++t) {
+      const gbq_pauli tp = terms[pt.term_begin + t];
+      float sre = 0.f, sim = 0.f;
+      for (uint64_t i = threadIdx.x; i < dim; i += kThreads) {
+        const uint64_t j = i ^ tp.x;
+        const float2 a = psi[i], b = psi[j];
+        const float sg = (__popcll(j & tp.zy) & 1) ? -1.f : 1.f;
+        sre += sg * fmaf(a.x, b.x, a.y * b.y);
+        sim += sg * fmaf(a.x, b.y, -a.y * b.x);
+      }
+      double cr = tp.coef, ci = 0.0;
+      const int ny = tp.ny & 3;
+      if (ny == 1) { ci = cr; cr = 0.0; }
+      else if (ny == 2) { cr = -cr; }
+      else if (ny == 3) { ci = -cr; cr = 0.0; }
+      re_acc += cr * sre - ci * sim;
+      im_acc += cr * sim + ci * sre;
+    }
+    cta_sum_store(re_acc, out + 2 * p, red);
+    cta_sum_store(im_acc, out + 2 * p + 1, red);
+  }
+}
+
+int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
+                 const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
+                 float2* slots, int nslots, int* d_counter, double* d_out) {
+  const int smem = (1 << kBatchTile) * (int)sizeof(float2);
+  static bool attr = false;
+  cudaError_t e;
+  if (!attr) {
+    e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_batch)");
+    attr = true;
+  }
+  k_batch<<<nslots, kThreads, smem, c->stream>>>(d_points, npoints, d_passes, d_ops, mats, d_terms,
+                                                 slots, (int64_t)1 << max_nbits, d_counter, d_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
+
+}  // namespace gbq

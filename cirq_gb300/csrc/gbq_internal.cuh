@@ -12,27 +12,73 @@
 
 namespace gbq {
 
-constexpr int kThreads = 512;  // threads per tile CTA (16 warps)
+constexpr int kThreads = 256;  // threads per tile CTA (8 warps)
+constexpr int kMinTile = GBQ_MIN_TILE_BITS;
+constexpr int kMaxTile = GBQ_MAX_TILE_BITS;
 
-// Tile geometry of one pass (shared by the per-pass and the batch kernels).
+// ---- shared-memory swizzle ------------------------------------------------------
+// Tile amplitude i is stored at phys(i) = i ^ swz(i).  swz XORs one 4-bit
+// column vector per tile bit >= 4 into bits 0..3; the columns below are
+// distinct, nonzero and not unit vectors, so for any op there are 4 group
+// bits whose columns (together with the unit columns of tile bits 0..3) are
+// independent -- a half-warp spread over them hits 16 distinct bank pairs.
+constexpr uint32_t kSwzV[10] = {3, 5, 6, 9, 10, 12, 7, 11, 13, 14};
+__host__ __device__ constexpr uint32_t swz_row(int r) {
+  uint32_t m = 0;
+  for (int b = 0; b < 10; ++b)
+    if ((kSwzV[b] >> r) & 1) m |= 1u << (b + 4);
+  return m;
+}
+constexpr uint32_t kSwzRow0 = swz_row(0), kSwzRow1 = swz_row(1), kSwzRow2 = swz_row(2),
+                   kSwzRow3 = swz_row(3);
+
+__host__ __device__ constexpr uint32_t parity_const(uint32_t x) {
+  uint32_t p = 0;
+  while (x) {
+    p ^= x & 1u;
+    x >>= 1;
+  }
+  return p;
+}
+
+// phys() for constants and host code (no intrinsics, folds at compile time)
+__host__ __device__ constexpr uint32_t phys_const(uint32_t i) {
+  return i ^ (parity_const(i & kSwzRow0) | (parity_const(i & kSwzRow1) << 1) |
+              (parity_const(i & kSwzRow2) << 2) | (parity_const(i & kSwzRow3) << 3));
+}
+
+// Device form of one op, derived on the host from the public gbq_op.
+struct OpDev {
+  int8_t kind, k, nsel, pad0;
+  int8_t selg[4];     // selector s: group-index bit (>= 0) or -(global bit)-1
+  uint32_t pcol[5];   // shared-index column of each target bit
+  uint32_t gcol[13];  // shared-index column of each group-index bit
+  uint16_t dcol[13];  // diag: table-index contribution of each tile bit
+  int8_t dext[8];     // diag: global bit feeding table bit j, or -1
+  int32_t slot;
+  int32_t pad1;
+  int64_t mat;
+};
+
+// Tile geometry of one pass.
 struct TileInfo {
-  const float2* mats;     // matrix / table pool (op.mat is relative to it)
-  double* partial;        // probe partials [slot][tile]
-  int64_t ntiles;         // 2^(nbits - L)
+  const float2* mats;  // matrix / table pool (op.mat is relative to it)
+  double* partial;     // probe partials [slot][tile]
+  int64_t ntiles;      // 2^(nbits - L)
   int32_t nbits;
   int32_t L;
   int32_t m;
   int32_t nops;
-  int8_t hi[16];          // global bit of tile bit m + j
-  int8_t nt[64];          // global bits NOT in the tile, ascending (nbits - L entries)
+  uint64_t gw[GBQ_MAX_TILE_BITS];  // global weight (1 << global bit) of each tile bit
+  int8_t nt[64];                   // global bits not in the tile, ascending
 };
 
 // Kernel arguments of one tile pass, passed by value (__grid_constant__).
 struct PassArgs {
   float2* psi;
-  float2* lam;            // second state (two-state passes only)
+  float2* lam;  // second state (two-state passes only)
   TileInfo ti;
-  gbq_op ops[GBQ_MAX_OPS_PER_PASS];
+  OpDev ops[GBQ_MAX_OPS_PER_PASS];
 };
 
 // Error plumbing (gbq_abi.cu).
@@ -45,13 +91,11 @@ struct Ctx {
   int sm_count = 0;
   bool use_graphs = false;
   int64_t launches = 0;
-  // scratch buffers owned by the context (grown on demand)
-  void* scratch = nullptr;
+  void* scratch = nullptr;  // device scratch, grown on demand
   size_t scratch_bytes = 0;
   void* host_scratch = nullptr;  // pinned
   size_t host_scratch_bytes = 0;
   cudaEvent_t events[16] = {};
-  // per-launch tile-pass timing
   bool pass_timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;  // pending (start, stop)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> event_pool;
@@ -62,10 +106,13 @@ struct Ctx {
 int ensure_scratch(Ctx* c, size_t bytes);
 int ensure_host_scratch(Ctx* c, size_t bytes);
 
-// Launchers implemented in the .cu files.
-int launch_pass(Ctx* c, const PassArgs& a, bool dual);
+// Launchers (one translation unit per tile width).
+int launch_pass_l10(Ctx* c, const PassArgs& a, bool dual);
+int launch_pass_l11(Ctx* c, const PassArgs& a, bool dual);
+int launch_pass_l12(Ctx* c, const PassArgs& a, bool dual);
+int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
-                 const gbq_op* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
+                 const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
                  float2* slots, int nslots, int* d_counter, double* d_out);
 
 }  // namespace gbq

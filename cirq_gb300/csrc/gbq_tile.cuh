@@ -1,0 +1,418 @@
+// Tile-pass device code (included by the per-tile-width translation units).
+//
+// One launch = one pass over the state.  A persistent grid of CTAs walks the
+// tiles; each tile is 2^LT amplitudes: tile bits 0..m-1 are the global index
+// bits 0..m-1 (contiguous runs, read with 128-bit loads) and tile bits
+// m..LT-1 are global bits chosen by the host planner.  The tile is staged in
+// shared memory, every op of the pass is applied there, and it is written
+// back in place: HBM traffic per pass is one read and one write of the state
+// whatever the number of ops.
+//
+// Replaces the numpy passes of the reference, one per operation:
+// linalg.targeted_left_multiply (cirq-core/cirq/linalg/transformations.py:105-172),
+// linalg.apply_matrix_to_slices (transformations.py:310-380), the gates'
+// own _apply_unitary_ (cirq-core/cirq/ops/common_gates.py:123-134, 658-669,
+// 1072-1082) and the Kraus/unitary channel paths
+// (cirq-core/cirq/protocols/apply_channel_protocol.py:274-356).
+//
+// Addressing: amplitude i of the tile lives at shared index phys(i) =
+// i ^ swz(i) (see gbq_internal.cuh).  phys is linear over GF(2), so the
+// shared index of any group member is an XOR of per-bit "columns" that the
+// host precomputes for every op (OpDev::pcol for target bits, OpDev::gcol
+// for group-index bits).  A thread therefore finds all its addresses with a
+// handful of XORs, and group-index bits 0..3 (the lanes of a half-warp) are
+// chosen so that a half-warp touches 16 distinct 8-byte bank pairs.
+
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbq_internal.cuh"
+
+namespace gbq {
+
+__device__ __forceinline__ uint32_t phys_dev(uint32_t i) {
+  uint32_t s = (__popc(i & kSwzRow0) & 1) | ((__popc(i & kSwzRow1) & 1) << 1) |
+               ((__popc(i & kSwzRow2) & 1) << 2) | ((__popc(i & kSwzRow3) & 1) << 3);
+  return i ^ s;
+}
+
+__device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of v stored to *out by thread 0 (all threads must call).
+__device__ __forceinline__ void cta_sum_store(double v, double* out, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < kThreads / 32 ? red[lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0) *out = v;
+  }
+  __syncthreads();
+}
+
+// global offset of tile index i (XOR of the global weights of its bits)
+template <int LT>
+__device__ __forceinline__ uint64_t lin_off(const TileInfo& ti, uint32_t i) {
+  uint64_t r = 0;
+#pragma unroll
+  for (int b = 0; b < LT; ++b)
+    if ((i >> b) & 1u) r ^= ti.gw[b];
+  return r;
+}
+
+__device__ __forceinline__ uint64_t tile_base(const TileInfo& ti, int64_t tile) {
+  uint64_t g = 0;
+  const int nnt = ti.nbits - ti.L;
+  for (int j = 0; j < nnt; ++j) g |= (uint64_t)((tile >> j) & 1) << ti.nt[j];
+  return g;
+}
+
+// ---- dense k-bit op (and dense probe) ---------------------------------------------
+template <int K, int LT, bool DUAL, bool PROBE>
+__device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, float2* smA,
+                                         float2* smB, uint64_t gbase, int64_t tile,
+                                         double* red) {
+  constexpr int D = 1 << K;
+  constexpr int NG = 1 << (LT - K);
+  constexpr int W = NG >= kThreads ? NG / kThreads : 1;
+  constexpr int R0 = NG >= kThreads ? 1 : kThreads / NG;
+  constexpr int R = R0 > D ? D : R0;
+  constexpr int RPI = D / R;
+  constexpr int NTB = (LT - K) < 8 ? (LT - K) : 8;
+  constexpr int NWB = (LT - K) > 8 ? (LT - K) - 8 : 0;
+  const int t = threadIdx.x;
+  const bool active = (R == 1) || (t < NG * R);
+
+  uint32_t pbt = 0;
+#pragma unroll
+  for (int b = 0; b < NTB; ++b)
+    if ((t >> b) & 1) pbt ^= op.gcol[b];
+  uint32_t poff[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int b = 0; b < K; ++b)
+      if ((j >> b) & 1) o ^= op.pcol[b];
+    poff[j] = o;
+  }
+  const int r0 = (R == 1) ? 0 : (t >> (LT - K)) * RPI;
+
+  float2 va[W][D];
+  float2 vb[DUAL ? W : 1][DUAL ? D : 1];
+  uint32_t pb[W];
+  const float2* mp[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    uint32_t p = pbt;
+#pragma unroll
+    for (int b = 0; b < NWB; ++b)
+      if ((w >> b) & 1) p ^= op.gcol[8 + b];
+    pb[w] = p;
+    const uint32_t g = (R == 1) ? (uint32_t)(t + w * kThreads) : (uint32_t)(t & (NG - 1));
+    uint32_t sel = 0;
+    for (int s = 0; s < op.nsel; ++s) {
+      const int c = op.selg[s];
+      const uint32_t bit = c >= 0 ? (g >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
+      sel |= bit << s;
+    }
+    mp[w] = ti.mats + op.mat + (int64_t)sel * (D * D);
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        va[w][j] = smA[p ^ poff[j]];
+        if constexpr (DUAL) vb[w][j] = smB[p ^ poff[j]];
+      }
+    }
+  }
+
+  if constexpr (PROBE) {
+    // Re <lam| D |psi> over this thread's rows (smA = psi, smB = lam)
+    float part = 0.f;
+    if (active) {
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          if (R > 1 && (r < r0 || r >= r0 + RPI)) continue;
+          const float2* row = mp[w] + r * D;
+          float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < D; c += 2) {
+            const float4 mm = __ldg(reinterpret_cast<const float4*>(row + c));
+            cfma(acc, make_float2(mm.x, mm.y), va[w][c]);
+            cfma(acc, make_float2(mm.z, mm.w), va[w][c + 1]);
+          }
+          part = fmaf(vb[w][r].x, acc.x, part);
+          part = fmaf(vb[w][r].y, acc.y, part);
+        }
+      }
+    }
+    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+  } else {
+    if constexpr (R > 1) __syncthreads();  // other threads still read this group
+    if (!active) return;
+    if constexpr (K <= 2) {
+      // small matrices: keep them in registers; reload only when the
+      // selector gives groups of this thread different matrices
+      float2 m[D * D];
+#pragma unroll
+      for (int e = 0; e < D * D; e += 2) {
+        const float4 mm = __ldg(reinterpret_cast<const float4*>(mp[0] + e));
+        m[e] = make_float2(mm.x, mm.y);
+        m[e + 1] = make_float2(mm.z, mm.w);
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        if (w > 0 && op.nsel) {
+#pragma unroll
+          for (int e = 0; e < D * D; e += 2) {
+            const float4 mm = __ldg(reinterpret_cast<const float4*>(mp[w] + e));
+            m[e] = make_float2(mm.x, mm.y);
+            m[e + 1] = make_float2(mm.z, mm.w);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          if (R > 1 && (r < r0 || r >= r0 + RPI)) continue;
+          float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < D; ++c) cfma(acc, m[r * D + c], va[w][c]);
+          smA[pb[w] ^ poff[r]] = acc;
+          if constexpr (DUAL) {
+            float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < D; ++c) cfma(accb, m[r * D + c], vb[w][c]);
+            smB[pb[w] ^ poff[r]] = accb;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          if (R > 1 && (r < r0 || r >= r0 + RPI)) continue;
+          const float2* row = mp[w] + r * D;
+          float2 acc = make_float2(0.f, 0.f);
+          float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < D; c += 2) {
+            const float4 mm = __ldg(reinterpret_cast<const float4*>(row + c));
+            cfma(acc, make_float2(mm.x, mm.y), va[w][c]);
+            cfma(acc, make_float2(mm.z, mm.w), va[w][c + 1]);
+            if constexpr (DUAL) {
+              cfma(accb, make_float2(mm.x, mm.y), vb[w][c]);
+              cfma(accb, make_float2(mm.z, mm.w), vb[w][c + 1]);
+            }
+          }
+          smA[pb[w] ^ poff[r]] = acc;
+          if constexpr (DUAL) smB[pb[w] ^ poff[r]] = accb;
+        }
+      }
+    }
+  }
+}
+
+// ---- diagonal op (and diagonal probe) ------------------------------------------------
+template <int LT, bool DUAL, bool PROBE>
+__device__ __forceinline__ void op_diag(const TileInfo& ti, const OpDev& op, float2* smA,
+                                        float2* smB, uint64_t gbase, int64_t tile, double* red) {
+  constexpr int A = (1 << LT) / kThreads;  // amplitude i = t + j * kThreads
+  const int t = threadIdx.x;
+  uint32_t it = 0;
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+    if ((t >> b) & 1) it ^= op.dcol[b];
+  uint32_t ext = 0;
+  for (int j = 0; j < op.k; ++j)
+    if (op.dext[j] >= 0) ext |= (uint32_t)((gbase >> op.dext[j]) & 1u) << j;
+  it ^= ext;
+  const uint32_t pt = phys_dev((uint32_t)t);
+  const float2* tab = ti.mats + op.mat;
+  float part = 0.f;
+#pragma unroll
+  for (int j = 0; j < A; ++j) {
+    uint32_t ij = it;
+#pragma unroll
+    for (int b = 0; b < LT - 8; ++b)
+      if ((j >> b) & 1) ij ^= op.dcol[8 + b];
+    const uint32_t p = pt ^ phys_const((uint32_t)j * kThreads);
+    const float2 d = __ldg(tab + ij);
+    if constexpr (PROBE) {
+      const float2 y = cmul(d, smA[p]);
+      const float2 l = smB[p];
+      part = fmaf(l.x, y.x, fmaf(l.y, y.y, part));
+    } else {
+      smA[p] = cmul(d, smA[p]);
+      if constexpr (DUAL) smB[p] = cmul(d, smB[p]);
+    }
+  }
+  if constexpr (PROBE)
+    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+}
+
+// KMAX: widest dense op the kernel variant contains (2 or 5); narrower
+// variants keep register pressure (and spills) down for the common case.
+template <int LT, int KMAX, bool DUAL>
+__device__ __forceinline__ void dispatch(const TileInfo& ti, const OpDev& op, float2* smA,
+                                         float2* smB, uint64_t gbase, int64_t tile, double* red) {
+  switch (op.kind * 8 + op.k) {
+    case GBQ_OP_DENSE * 8 + 1: op_dense<1, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red); break;
+    case GBQ_OP_DENSE * 8 + 2: op_dense<2, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red); break;
+    case GBQ_OP_DENSE * 8 + 3:
+      if constexpr (KMAX >= 3) op_dense<3, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      break;
+    case GBQ_OP_DENSE * 8 + 4:
+      if constexpr (KMAX >= 4) op_dense<4, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      break;
+    case GBQ_OP_DENSE * 8 + 5:
+      if constexpr (KMAX >= 5) op_dense<5, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      break;
+    default:
+      if (op.kind == GBQ_OP_DIAG) {
+        op_diag<LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      } else if constexpr (DUAL) {
+        if (op.kind == GBQ_OP_PROBE_DIAG) {
+          op_diag<LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+        } else if (op.kind == GBQ_OP_PROBE) {
+          if (op.k == 1) op_dense<1, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+          else if (op.k == 2) op_dense<2, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+          else if constexpr (KMAX >= 3) {
+            if (op.k == 3) op_dense<3, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+          }
+        }
+      }
+      break;
+  }
+}
+
+// Loads tile `tile` (base index gbase) of `src` into shared memory.
+template <int LT>
+__device__ __forceinline__ void load_tile(const float2* __restrict__ src, float2* sm, uint64_t gbase,
+                                          uint64_t off_t, uint32_t ph_t, const uint64_t* soff) {
+  constexpr int NJ = 1 << (LT - 9);  // float4 pairs per thread
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const uint64_t off = gbase | off_t | soff[j];
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(src + off));
+    const uint32_t p = ph_t ^ phys_const((uint32_t)j * (2 * kThreads));
+    sm[p] = make_float2(v.x, v.y);
+    sm[p ^ 1u] = make_float2(v.z, v.w);
+  }
+}
+
+template <int LT>
+__device__ __forceinline__ void store_tile(float2* __restrict__ dst, const float2* sm, uint64_t gbase,
+                                           uint64_t off_t, uint32_t ph_t, const uint64_t* soff) {
+  constexpr int NJ = 1 << (LT - 9);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const uint64_t off = gbase | off_t | soff[j];
+    const uint32_t p = ph_t ^ phys_const((uint32_t)j * (2 * kThreads));
+    const float2 x = sm[p], y = sm[p ^ 1u];
+    __stcs(reinterpret_cast<float4*>(dst + off), make_float4(x.x, x.y, y.x, y.y));
+  }
+}
+
+// Per-launch setup shared by the pass and batch kernels: the thread's part of
+// its float4 offsets (pairs p = t + j * kThreads <-> tile index 2p).
+template <int LT>
+__device__ __forceinline__ void pair_setup(const TileInfo& ti, uint64_t* soff, uint64_t& off_t,
+                                           uint32_t& ph_t) {
+  constexpr int NJ = 1 << (LT - 9);
+  if (threadIdx.x < NJ) soff[threadIdx.x] = lin_off<LT>(ti, (uint32_t)threadIdx.x * (2 * kThreads));
+  off_t = lin_off<LT>(ti, (uint32_t)threadIdx.x << 1);
+  ph_t = phys_dev((uint32_t)threadIdx.x << 1);
+}
+
+template <int LT, int KMAX, bool DUAL>
+__device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, float2* smA,
+                                        float2* smB, uint64_t gbase, int64_t tile, double* red) {
+  for (int o = 0; o < ti.nops; ++o) {
+    dispatch<LT, KMAX, DUAL>(ti, sops[o], smA, smB, gbase, tile, red);
+    __syncthreads();
+  }
+}
+
+template <int LT, int KMAX, bool DUAL>
+__global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
+  extern __shared__ float4 smraw[];
+  __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
+  __shared__ uint64_t soff[1 << (LT - 9)];
+  __shared__ double red[kThreads / 32];
+  float2* smA = reinterpret_cast<float2*>(smraw);
+  float2* smB = smA + (1 << LT);
+  {
+    const int nwords = a.ti.nops * (int)(sizeof(OpDev) / 4);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.ops);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
+    for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
+  }
+  uint64_t off_t;
+  uint32_t ph_t;
+  pair_setup<LT>(a.ti, soff, off_t, ph_t);
+  __syncthreads();
+  for (int64_t tile = blockIdx.x; tile < a.ti.ntiles; tile += gridDim.x) {
+    const uint64_t gbase = tile_base(a.ti, tile);
+    load_tile<LT>(a.psi, smA, gbase, off_t, ph_t, soff);
+    if constexpr (DUAL) load_tile<LT>(a.lam, smB, gbase, off_t, ph_t, soff);
+    __syncthreads();
+    run_ops<LT, KMAX, DUAL>(a.ti, sops, smA, smB, gbase, tile, red);
+    store_tile<LT>(a.psi, smA, gbase, off_t, ph_t, soff);
+    if constexpr (DUAL) store_tile<LT>(a.lam, smB, gbase, off_t, ph_t, soff);
+    __syncthreads();
+  }
+}
+
+template <int LT, int KMAX, bool DUAL>
+int launch_tile_pass(Ctx* c, const PassArgs& a) {
+  const int smem = (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
+  static int blocks_per_sm = -1;
+  cudaError_t e;
+  if (blocks_per_sm < 0) {
+    e = cudaFuncSetAttribute(k_tile_pass<LT, KMAX, DUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_tile_pass)");
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_pass<LT, KMAX, DUAL>, kThreads, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    blocks_per_sm = nb > 0 ? nb : 1;
+  }
+  int64_t grid = (int64_t)c->sm_count * blocks_per_sm;
+  if (grid > a.ti.ntiles) grid = a.ti.ntiles;
+  k_tile_pass<LT, KMAX, DUAL><<<(unsigned)grid, kThreads, smem, c->stream>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_tile_pass launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
+
+// Widest dense (or dense-probe) op of a pass.
+inline int pass_kmax(const PassArgs& a) {
+  int k = 1;
+  for (int o = 0; o < a.ti.nops; ++o)
+    if ((a.ops[o].kind == GBQ_OP_DENSE || a.ops[o].kind == GBQ_OP_PROBE) && a.ops[o].k > k)
+      k = a.ops[o].k;
+  return k;
+}
+
+}  // namespace gbq

@@ -1,0 +1,12 @@
+// Tile-pass kernels for 10-bit tiles (see gbq_tile.cuh).
+#include "gbq_tile.cuh"
+
+namespace gbq {
+
+int launch_pass_l10(Ctx* c, const PassArgs& a, bool dual) {
+  if (dual) return launch_tile_pass<10, 5, true>(c, a);
+  if (pass_kmax(a) <= 2) return launch_tile_pass<10, 2, false>(c, a);
+  return launch_tile_pass<10, 5, false>(c, a);
+}
+
+}  // namespace gbq

@@ -170,15 +170,22 @@ class Engine:
         return ms.value, n.value
 
     # ---- state vectors -------------------------------------------------
-    def new_state(self, nbits: int, basis: int = 0, initial: np.ndarray | None = None) -> DeviceBuffer:
-        buf = self.alloc(8 * (1 << nbits))
+    def new_state(
+        self, nbits: int, basis: int = 0, initial: np.ndarray | None = None, nbits_dev: int | None = None
+    ) -> DeviceBuffer:
+        """A 2^nbits_dev buffer holding |basis> or `initial` (2^nbits amplitudes)
+        in its first 2^nbits entries and zeros above."""
+        nbits_dev = max(nbits, nbits_dev or nbits)
+        buf = self.alloc(8 * (1 << nbits_dev))
         if initial is not None:
             arr = np.ascontiguousarray(np.asarray(initial, dtype=np.complex64).reshape(-1))
             if arr.size != 1 << nbits:
                 raise ValueError(f"initial state has {arr.size} amplitudes, expected {1 << nbits}")
+            if nbits_dev > nbits:
+                check(self.lib.gbq_sv_set_basis(self.ctx, buf.ptr, nbits_dev, 0), "gbq_sv_set_basis")
             buf.upload(arr)
         else:
-            check(self.lib.gbq_sv_set_basis(self.ctx, buf.ptr, nbits, int(basis)), "gbq_sv_set_basis")
+            check(self.lib.gbq_sv_set_basis(self.ctx, buf.ptr, nbits_dev, int(basis)), "gbq_sv_set_basis")
         return buf
 
     def run(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer | None = None) -> None:

@@ -37,35 +37,10 @@ import numpy as np
 from cirq_gb300 import _lib
 from cirq_gb300.ir import BitGate
 
-# Swizzle column vectors of tile bits 4..13 (must match gbq_tile.cu kSwzV).
-SWZ_V = (3, 5, 6, 9, 10, 12, 7, 11, 13, 14)
-
 MAX_OPS = 64
 MAX_DIAG_BITS = 8
 MAX_SEL = 3
-
-
-def swz_vec(tile_bit: int) -> int:
-    return 1 << tile_bit if tile_bit < 4 else SWZ_V[tile_bit - 4]
-
-
-def group_order(L: int, targets: Sequence[int]) -> list[int]:
-    """Tile bits of the group index: 4 bank-independent lane bits first."""
-    free = [b for b in range(L) if b not in targets]
-    lanes: list[int] = []
-    basis: list[int] = []  # GF(2) basis, reduced
-    for b in free:
-        v = swz_vec(b)
-        for e in basis:
-            v = min(v, v ^ e)
-        if v:
-            basis.append(v)
-            basis.sort(reverse=True)
-            lanes.append(b)
-            if len(lanes) == 4:
-                break
-    rest = [b for b in free if b not in lanes]
-    return lanes + rest
+MIN_TILE_BITS = 10  # the engine's narrowest tile; narrower registers are padded
 
 
 # ---------------------------------------------------------------- fused ops
@@ -253,8 +228,8 @@ class Planner:
     ):
         if not 1 <= kmax <= 5:
             raise ValueError("fusion width kmax must be in 1..5")
-        if not 1 <= tile_bits <= 13:
-            raise ValueError("tile_bits must be in 1..13")
+        if not MIN_TILE_BITS <= tile_bits <= 13:
+            raise ValueError(f"tile_bits must be in {MIN_TILE_BITS}..13")
         self.tile_bits = tile_bits
         self.low_bits = low_bits
         self.kmax = kmax
@@ -264,7 +239,10 @@ class Planner:
     # ------------------------------------------------------------------
     def plan(self, gates: Sequence[BitGate], nbits: int, batch: dict | None = None) -> Plan:
         """Plans `gates`; `batch` optionally gives (P, d, d) matrices per gate index
-        (default: each gate's own matrix, P = 1)."""
+        (default: each gate's own matrix, P = 1).  nbits >= 10 (pad narrower
+        registers with unused high bits)."""
+        if nbits < MIN_TILE_BITS:
+            raise ValueError(f"plan width must be >= {MIN_TILE_BITS} bits (pad narrower registers)")
         if batch is None:
             batch = {i: g.matrix[None] for i, g in enumerate(gates)}
         L = min(self.tile_bits, nbits)
@@ -505,8 +483,6 @@ class Planner:
                     r["nsel"] = len(op.sl)
                     r["bits"][:k] = tbits
                     r["sel"][: len(op.sl)] = [code(b) for b in op.sl]
-                    go = group_order(pp.L, tbits)
-                    r["gorder"][: len(go)] = go
                     data = op.M[0].reshape(-1)
                     layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2])))
                 else:

@@ -26,7 +26,7 @@ import numpy as np
 
 from cirq_gb300._cirq_env import ensure_cirq
 from cirq_gb300.ir import BitGate, UnsupportedOperation, is_diagonal
-from cirq_gb300.planner import Plan, Planner
+from cirq_gb300.planner import MIN_TILE_BITS, Plan, Planner
 
 
 def _cirq():
@@ -168,6 +168,8 @@ class CompiledCircuit:
         self.n = len(qubits)
         self.dm = dm
         self.nbits = 2 * self.n if dm else self.n
+        # device width: narrow registers run padded with |0> high bits
+        self.nbits_dev = max(self.nbits, MIN_TILE_BITS)
         index = {q: i for i, q in enumerate(self.qubits)}
         n = self.n
         self.sources: list[OpSource] = []
@@ -251,7 +253,7 @@ class CompiledCircuit:
         self.kept = keep
         gates = [self.gates[i] for i in keep]
         sub = {j: batch[i][:1] for j, i in enumerate(keep)}
-        self.plan = self.planner.plan(gates, self.nbits, batch=sub)
+        self.plan = self.planner.plan(gates, self.nbits_dev, batch=sub)
 
     @property
     def parameterized(self) -> bool:

@@ -144,11 +144,10 @@ class _GpuSimulatorBase:
     def _evolve(self, compiled: CompiledCircuit, pool_row: np.ndarray, initial_state):
         """Allocates the initial state on the device and runs the program."""
         eng = self.engine
-        nbits = compiled.nbits
         state = self._initial_device_state(compiled, initial_state)
         if compiled.plan.npasses:
             pool_dev = eng.upload(np.ascontiguousarray(pool_row))
-            eng.run(state, nbits, compiled.plan, pool_dev)
+            eng.run(state, compiled.nbits_dev, compiled.plan, pool_dev)
         return state
 
     def _measure_terminal(self, state, compiled, meas_ops) -> dict[str, np.ndarray]:
@@ -284,11 +283,11 @@ class Simulator(
         if isinstance(initial_state, (int, np.integer)):
             if not 0 <= int(initial_state) < 2**n:
                 raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
-            return eng.new_state(n, basis=int(initial_state))
+            return eng.new_state(n, basis=int(initial_state), nbits_dev=compiled.nbits_dev)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("cirq_gb300.Simulator takes raw initial states, not SimulationState")
         vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
-        return eng.new_state(n, initial=vec)
+        return eng.new_state(n, initial=vec, nbits_dev=compiled.nbits_dev)
 
     def simulate_sweep_iter(
         self,
@@ -400,11 +399,11 @@ class DensityMatrixSimulator(
             if not 0 <= int(initial_state) < 2**n:
                 raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
             i = int(initial_state)
-            return eng.new_state(2 * n, basis=(i << n) | i)
+            return eng.new_state(2 * n, basis=(i << n) | i, nbits_dev=compiled.nbits_dev)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("takes raw initial states, not SimulationState")
         rho = cirq.to_valid_density_matrix(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
-        return eng.new_state(2 * n, initial=rho.reshape(-1))
+        return eng.new_state(2 * n, initial=rho.reshape(-1), nbits_dev=compiled.nbits_dev)
 
     def simulate_sweep_iter(
         self,

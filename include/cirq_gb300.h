@@ -59,6 +59,7 @@ typedef struct gbq_ctx gbq_ctx;
 
 #define GBQ_MAX_OPS_PER_PASS 64
 #define GBQ_MAX_TILE_BITS 13
+#define GBQ_MIN_TILE_BITS 10 /* states narrower than this are padded with |0> bits */
 #define GBQ_MAX_DENSE_K 5
 #define GBQ_MAX_DIAG_K 8
 
@@ -69,8 +70,8 @@ typedef struct gbq_op {
   int8_t pad0;
   int8_t bits[8];    /* dense/probe: tile bit of matrix-index bit j; diag: bit codes */
   int8_t sel[4];     /* selector bit codes; matrix number = sum sel_j << j       */
-  int8_t gorder[16]; /* dense/probe: tile bit of group-index bit j (L-k entries) */
   int32_t slot;      /* probe: output slot                                       */
+  int32_t pad1;
   int64_t mat;       /* offset (in gbq_c64) of the first matrix/table in the pool */
 } gbq_op;
 
@@ -135,7 +136,10 @@ int gbq_sv_set_basis(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t index);
  * (cirq-core/cirq/linalg/transformations.py:105-172, 310-380), and for
  * density matrices protocols.apply_channel
  * (cirq-core/cirq/protocols/apply_channel_protocol.py:168-356).
- * mats is a device pool of matrices/tables referenced by gbq_op.mat. */
+ * mats is a device pool of matrices/tables referenced by gbq_op.mat.
+ * Every pass has GBQ_MIN_TILE_BITS <= L <= min(nbits, GBQ_MAX_TILE_BITS), so
+ * nbits >= GBQ_MIN_TILE_BITS: narrower registers are simulated inside a
+ * 2^GBQ_MIN_TILE_BITS buffer whose extra (high) bits stay |0>. */
 int gbq_run(gbq_ctx* ctx, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
             const gbq_op* ops, int nops, const gbq_c64* mats);
 
