@@ -18,8 +18,13 @@ TOL = 1e-5  # max amplitude error for complex64
 @pytest.mark.parametrize("n,d,s", [(10, 20, 1), (12, 8, 2), (5, 6, 3)])
 @pytest.mark.parametrize(
     "cfg",
-    [dict(), dict(tile_bits=8, fusion_max_qubits=3, pass_budget=20), dict(tile_bits=6, fusion_max_qubits=2, pass_budget=8),
-     dict(tile_bits=7, fusion_max_qubits=5, pass_budget=200), dict(tile_bits=10, fusion_max_qubits=1, pass_budget=10)],
+    [
+        dict(),
+        dict(tile_bits=10, fusion_max_qubits=3, pass_budget=20),
+        dict(tile_bits=10, fusion_max_qubits=2, pass_budget=8),
+        dict(tile_bits=11, fusion_max_qubits=5, pass_budget=200),
+        dict(tile_bits=13, fusion_max_qubits=1, pass_budget=10),
+    ],
 )
 def test_layers_vs_golden(n, d, s, cfg):
     c = workloads.random_layer_circuit(n, d, s)
