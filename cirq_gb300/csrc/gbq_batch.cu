@@ -26,8 +26,10 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ TileInfo ti;
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t soff[1 << (LT - 9)];
+  __shared__ uint64_t slo[1 << (LT - 8)];
   __shared__ int s_point;
-  float2* sm = reinterpret_cast<float2*>(smraw);
+  constexpr int TS = 1 << LT;
+  float2* buf = reinterpret_cast<float2*>(smraw);  // [2][TS]
   float2* psi = slots + (int64_t)blockIdx.x * slot_stride;
   for (;;) {
     if (threadIdx.x == 0) s_point = atomicAdd(counter, 1);
@@ -66,18 +68,27 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
       }
       __syncthreads();
-      uint64_t off_t;
-      uint32_t ph_t;
-      pair_setup<LT>(ti, soff, off_t, ph_t);
+      const TileSetup ts = tile_setup<LT>(ti, soff, slo);
       __syncthreads();
+      // every global write of the previous pass is visible here: the whole
+      // pass ran in this CTA and ended with __syncthreads()
+      load_tile_async<LT>(psi, buf, tile_base(ti, 0), ts.lo_t, ts.lp_t, slo);
+      cp_async_commit();
+      int cur = 0;
       for (int64_t tile = 0; tile < ti.ntiles; ++tile) {
+        if (tile + 1 < ti.ntiles)
+          load_tile_async<LT>(psi, buf + (cur ^ 1) * TS, tile_base(ti, tile + 1), ts.lo_t, ts.lp_t, slo);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();
         const uint64_t gbase = tile_base(ti, tile);
-        load_tile<LT>(psi, sm, gbase, off_t, ph_t, soff);
+        run_ops<LT, 5, false>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
+        store_tile<LT>(psi, buf + cur * TS, gbase, ts.off_t, ts.ph_t, soff);
         __syncthreads();
-        run_ops<LT, 5, false>(ti, sops, sm, nullptr, gbase, tile, red);
-        store_tile<LT>(psi, sm, gbase, off_t, ph_t, soff);
-        __syncthreads();
+        cur ^= 1;
       }
+      cp_async_wait<0>();
+      __syncthreads();
     }
     // <psi| sum_t coef_t P_t |psi>, P_t = i^ny X^x Z^zy (sign on the input index)
     double re_acc = 0.0, im_acc = 0.0;
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
                  const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
                  float2* slots, int nslots, int* d_counter, double* d_out) {
-  const int smem = (1 << kBatchTile) * (int)sizeof(float2);
+  const int smem = 2 * (1 << kBatchTile) * (int)sizeof(float2);
   static bool attr = false;
   cudaError_t e;
   if (!attr) {

@@ -116,6 +116,19 @@ __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, fl
   }
   const int r0 = (R == 1) ? 0 : (t >> (LT - K)) * RPI;
 
+  // selector value = part fixed by the thread index / tile base, plus bits
+  // carried by the group's w index (group-index bits >= 8)
+  uint32_t sel_t = 0;
+  int wsh[3] = {-1, -1, -1};
+  const uint32_t gt = (R == 1) ? (uint32_t)t : (uint32_t)(t & (NG - 1));
+  for (int s = 0; s < op.nsel; ++s) {
+    const int c = op.selg[s];
+    if (c < 0) sel_t |= (uint32_t)((gbase >> (-c - 1)) & 1u) << s;
+    else if (c < 8 || R > 1) sel_t |= ((gt >> c) & 1u) << s;
+    else wsh[s] = c - 8;
+  }
+  const float2* mbase = ti.mats + op.mat;
+
   float2 va[W][D];
   float2 vb[DUAL ? W : 1][DUAL ? D : 1];
   uint32_t pb[W];
@@ -127,14 +140,13 @@ __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, fl
     for (int b = 0; b < NWB; ++b)
       if ((w >> b) & 1) p ^= op.gcol[8 + b];
     pb[w] = p;
-    const uint32_t g = (R == 1) ? (uint32_t)(t + w * kThreads) : (uint32_t)(t & (NG - 1));
-    uint32_t sel = 0;
-    for (int s = 0; s < op.nsel; ++s) {
-      const int c = op.selg[s];
-      const uint32_t bit = c >= 0 ? (g >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
-      sel |= bit << s;
+    uint32_t sel = sel_t;
+    if (W > 1) {
+#pragma unroll
+      for (int s = 0; s < 3; ++s)
+        if (wsh[s] >= 0) sel |= (((uint32_t)w >> wsh[s]) & 1u) << s;
     }
-    mp[w] = ti.mats + op.mat + (int64_t)sel * (D * D);
+    mp[w] = mbase + (int64_t)sel * (D * D);
     if (active) {
 #pragma unroll
       for (int j = 0; j < D; ++j) {
@@ -305,18 +317,30 @@ __device__ __forceinline__ void dispatch(const TileInfo& ti, const OpDev& op, fl
   }
 }
 
-// Loads tile `tile` (base index gbase) of `src` into shared memory.
+// ---- tile load (asynchronous) / store -------------------------------------------------
+// Loads: amplitude i = t + j * kThreads of the tile (a warp copies 32
+// consecutive amplitudes = 256 contiguous bytes) with 8-byte cp.async, so the
+// next tile streams into the second shared buffer while the current one is
+// being processed.
+__device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc) {
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 template <int LT>
-__device__ __forceinline__ void load_tile(const float2* __restrict__ src, float2* sm, uint64_t gbase,
-                                          uint64_t off_t, uint32_t ph_t, const uint64_t* soff) {
-  constexpr int NJ = 1 << (LT - 9);  // float4 pairs per thread
+__device__ __forceinline__ void load_tile_async(const float2* __restrict__ src, float2* sm,
+                                                uint64_t gbase, uint64_t lo_t, uint32_t lp_t,
+                                                const uint64_t* slo) {
+  constexpr int NA = 1 << (LT - 8);  // amplitudes per thread
 #pragma unroll
-  for (int j = 0; j < NJ; ++j) {
-    const uint64_t off = gbase | off_t | soff[j];
-    const float4 v = __ldcs(reinterpret_cast<const float4*>(src + off));
-    const uint32_t p = ph_t ^ phys_const((uint32_t)j * (2 * kThreads));
-    sm[p] = make_float2(v.x, v.y);
-    sm[p ^ 1u] = make_float2(v.z, v.w);
+  for (int j = 0; j < NA; ++j) {
+    const uint64_t off = gbase | lo_t | slo[j];
+    cp_async8(sm + (lp_t ^ phys_const((uint32_t)j * kThreads)), src + off);
   }
 }
 
@@ -333,15 +357,29 @@ __device__ __forceinline__ void store_tile(float2* __restrict__ dst, const float
   }
 }
 
-// Per-launch setup shared by the pass and batch kernels: the thread's part of
-// its float4 offsets (pairs p = t + j * kThreads <-> tile index 2p).
+// Per-launch setup shared by the pass and batch kernels.  Stores: float4
+// pairs p = t + j * kThreads <-> tile index 2p.  Loads: amplitude
+// i = t + j * kThreads.  Only the thread part is per-thread; the j parts are
+// shared tables.
+struct TileSetup {
+  uint64_t off_t;  // store: global offset of tile index 2t
+  uint32_t ph_t;   // store: shared index of tile index 2t
+  uint64_t lo_t;   // load: global offset of tile index t
+  uint32_t lp_t;   // load: shared index of tile index t
+};
+
 template <int LT>
-__device__ __forceinline__ void pair_setup(const TileInfo& ti, uint64_t* soff, uint64_t& off_t,
-                                           uint32_t& ph_t) {
+__device__ __forceinline__ TileSetup tile_setup(const TileInfo& ti, uint64_t* soff, uint64_t* slo) {
   constexpr int NJ = 1 << (LT - 9);
+  constexpr int NA = 1 << (LT - 8);
   if (threadIdx.x < NJ) soff[threadIdx.x] = lin_off<LT>(ti, (uint32_t)threadIdx.x * (2 * kThreads));
-  off_t = lin_off<LT>(ti, (uint32_t)threadIdx.x << 1);
-  ph_t = phys_dev((uint32_t)threadIdx.x << 1);
+  if (threadIdx.x < NA) slo[threadIdx.x] = lin_off<LT>(ti, (uint32_t)threadIdx.x * kThreads);
+  TileSetup s;
+  s.off_t = lin_off<LT>(ti, (uint32_t)threadIdx.x << 1);
+  s.ph_t = phys_dev((uint32_t)threadIdx.x << 1);
+  s.lo_t = lin_off<LT>(ti, (uint32_t)threadIdx.x);
+  s.lp_t = phys_dev((uint32_t)threadIdx.x);
+  return s;
 }
 
 template <int LT, int KMAX, bool DUAL>
@@ -353,39 +391,61 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
   }
 }
 
+// Two shared buffers per state: tile i is processed in one while tile i+1
+// streams into the other (cp.async groups, waited with wait_group 1).
 template <int LT, int KMAX, bool DUAL>
-__global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
+__global__ void __launch_bounds__(kThreads, KMAX <= 2 ? 3 : 2)
+    k_tile_pass(const __grid_constant__ PassArgs a) {
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t soff[1 << (LT - 9)];
+  __shared__ uint64_t slo[1 << (LT - 8)];
   __shared__ double red[kThreads / 32];
-  float2* smA = reinterpret_cast<float2*>(smraw);
-  float2* smB = smA + (1 << LT);
+  constexpr int TS = 1 << LT;
+  float2* buf = reinterpret_cast<float2*>(smraw);  // [2][DUAL ? 2 : 1][TS]
   {
     const int nwords = a.ti.nops * (int)(sizeof(OpDev) / 4);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.ops);
     uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
     for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
   }
-  uint64_t off_t;
-  uint32_t ph_t;
-  pair_setup<LT>(a.ti, soff, off_t, ph_t);
+  const TileSetup ts = tile_setup<LT>(a.ti, soff, slo);
   __syncthreads();
-  for (int64_t tile = blockIdx.x; tile < a.ti.ntiles; tile += gridDim.x) {
-    const uint64_t gbase = tile_base(a.ti, tile);
-    load_tile<LT>(a.psi, smA, gbase, off_t, ph_t, soff);
-    if constexpr (DUAL) load_tile<LT>(a.lam, smB, gbase, off_t, ph_t, soff);
-    __syncthreads();
-    run_ops<LT, KMAX, DUAL>(a.ti, sops, smA, smB, gbase, tile, red);
-    store_tile<LT>(a.psi, smA, gbase, off_t, ph_t, soff);
-    if constexpr (DUAL) store_tile<LT>(a.lam, smB, gbase, off_t, ph_t, soff);
-    __syncthreads();
+  constexpr int NS = DUAL ? 2 : 1;
+  int64_t tile = blockIdx.x;
+  if (tile < a.ti.ntiles) {
+    const uint64_t gb = tile_base(a.ti, tile);
+    load_tile_async<LT>(a.psi, buf, gb, ts.lo_t, ts.lp_t, slo);
+    if constexpr (DUAL) load_tile_async<LT>(a.lam, buf + TS, gb, ts.lo_t, ts.lp_t, slo);
   }
+  cp_async_commit();
+  int cur = 0;
+  for (; tile < a.ti.ntiles; tile += gridDim.x) {
+    const int64_t next = tile + gridDim.x;
+    float2* nb = buf + (cur ^ 1) * NS * TS;
+    if (next < a.ti.ntiles) {
+      const uint64_t gn = tile_base(a.ti, next);
+      load_tile_async<LT>(a.psi, nb, gn, ts.lo_t, ts.lp_t, slo);
+      if constexpr (DUAL) load_tile_async<LT>(a.lam, nb + TS, gn, ts.lo_t, ts.lp_t, slo);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    float2* smA = buf + cur * NS * TS;
+    float2* smB = smA + TS;
+    const uint64_t gbase = tile_base(a.ti, tile);
+    run_ops<LT, KMAX, DUAL>(a.ti, sops, smA, smB, gbase, tile, red);
+    store_tile<LT>(a.psi, smA, gbase, ts.off_t, ts.ph_t, soff);
+    if constexpr (DUAL) store_tile<LT>(a.lam, smB, gbase, ts.off_t, ts.ph_t, soff);
+    __syncthreads();
+    cur ^= 1;
+  }
+  cp_async_wait<0>();
 }
 
 template <int LT, int KMAX, bool DUAL>
 int launch_tile_pass(Ctx* c, const PassArgs& a) {
-  const int smem = (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
+  const int smem = 2 * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
   static int blocks_per_sm = -1;
   cudaError_t e;
   if (blocks_per_sm < 0) {
