@@ -778,7 +778,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   const size_t b_passes = al((size_t)(npasses ? npasses : 1) * sizeof(gbq_pass));
   const size_t b_ops = al((size_t)(nops ? nops : 1) * sizeof(OpDev));
   const size_t b_terms = al((size_t)(nterms ? nterms : 1) * sizeof(gbq_pauli));
-  const size_t b_out = al((size_t)npoints * 2 * sizeof(double));
+  const size_t b_out = al((size_t)(nterms ? nterms : 1) * 2 * sizeof(double));
   const size_t b_counter = 256;
   const size_t head = b_points + b_passes + b_ops + b_terms + b_out + b_counter;
   int rc = ensure_scratch(c, head + slot_bytes * nslots);
@@ -808,10 +808,12 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   }
   e = cudaMemsetAsync(d_counter, 0, sizeof(int), c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(counter)");
+  e = cudaMemsetAsync(d_out, 0, (size_t)(nterms ? nterms : 1) * 2 * sizeof(double), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(out)");
   rc = launch_batch(c, d_points, npoints, d_passes, d_ops, reinterpret_cast<const float2*>(mats),
                     d_terms, max_nbits, slots, nslots, d_counter, d_out);
   if (rc) return rc;
-  e = cudaMemcpyAsync(out, d_out, (size_t)npoints * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  e = cudaMemcpyAsync(out, d_out, (size_t)nterms * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(out)");
   return sync(c, "gbq_batch_expect");
 }

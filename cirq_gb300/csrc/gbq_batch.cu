@@ -6,8 +6,8 @@
 //
 // Each CTA repeatedly claims the next point with an atomic counter (no CTA
 // ever waits for another), simulates it alone in its own scratch slot with
-// the same 12-bit tile code as the single-state kernels, and writes the
-// point's expectation value <psi| sum_t c_t P_t |psi>.
+// the same 12-bit tile code as the single-state kernels, and writes
+// c_t <psi|P_t|psi> for each of the point's Pauli terms.
 
 #include "gbq_tile.cuh"
 
@@ -90,8 +90,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       cp_async_wait<0>();
       __syncthreads();
     }
-    // <psi| sum_t coef_t P_t |psi>, P_t = i^ny X^x Z^zy (sign on the input index)
-    double re_acc = 0.0, im_acc = 0.0;
+    // per term: coef_t <psi|P_t|psi>, P_t = i^ny X^x Z^zy (sign on the input index)
     for (int t = 0; t < pt.term_count; ++t) {
       const gbq_pauli tp = terms[pt.term_begin + t];
       float sre = 0.f, sim = 0.f;
@@ -107,11 +106,10 @@ __global__ void __launch_bounds__(kThreads, 2)
       if (ny == 1) { ci = cr; cr = 0.0; }
       else if (ny == 2) { cr = -cr; }
       else if (ny == 3) { ci = -cr; cr = 0.0; }
-      re_acc += cr * sre - ci * sim;
-      im_acc += cr * sim + ci * sre;
+      const int64_t o = 2 * ((int64_t)pt.term_begin + t);
+      cta_sum_store(cr * sre - ci * sim, out + o, red);
+      cta_sum_store(cr * sim + ci * sre, out + o + 1, red);
     }
-    cta_sum_store(re_acc, out + 2 * p, red);
-    cta_sum_store(im_acc, out + 2 * p + 1, red);
   }
 }
 

@@ -5,8 +5,8 @@ namespace gbq {
 
 int launch_pass_l11(Ctx* c, const PassArgs& a, bool dual) {
   if (dual) {
-    set_error("two-state passes support tile widths 10 and 12 only");
-    return GBQ_ERR_ARG;
+    if (pass_kmax(a) <= 2) return launch_tile_pass<11, 2, true>(c, a);
+    return launch_tile_pass<11, 5, true>(c, a);
   }
   if (pass_kmax(a) <= 2) return launch_tile_pass<11, 2, false>(c, a);
   return launch_tile_pass<11, 5, false>(c, a);

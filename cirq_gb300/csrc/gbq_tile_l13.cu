@@ -5,7 +5,7 @@ namespace gbq {
 
 int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual) {
   if (dual) {
-    set_error("two-state passes support tile widths 10 and 12 only");
+    set_error("two-state passes support tile widths 10 to 12");
     return GBQ_ERR_ARG;
   }
   if (pass_kmax(a) <= 2) return launch_tile_pass<13, 2, false>(c, a);

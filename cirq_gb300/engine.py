@@ -312,7 +312,8 @@ class Engine:
         check(self.lib.gbq_reduce_slots(self.ctx, partial.ptr, nslots, int(ntiles), out.ptr), "gbq_reduce_slots")
 
     def batch_expect(self, points, passes, ops, pool_dev, terms, max_nbits) -> np.ndarray:
-        out = np.zeros(2 * len(points), dtype=np.float64)
+        """Per-term complex values coef_j <P_j> of every point's term block."""
+        out = np.zeros(2 * max(len(terms), 1), dtype=np.float64)
         check(
             self.lib.gbq_batch_expect(
                 self.ctx,

@@ -33,8 +33,11 @@ class BitGate:
     bits: tuple[int, ...]
     matrix: np.ndarray  # complex128, (2^k, 2^k)
     diagonal: bool
-    # adjoint bookkeeping: index of the source gate in the translated list
+    # bookkeeping: index of the source gate in the translated list
     tag: Any = None
+    # probe slot: >= 0 marks a gradient probe Re<lam|matrix|psi> (two-state
+    # programs only); probes are never fused with other gates
+    probe: int = -1
 
     @property
     def k(self) -> int:

@@ -75,6 +75,23 @@ class _Diag:
         return 1 + ovh
 
 
+@dataclasses.dataclass
+class _Probe:
+    bits: list  # global bits, matrix bit j <-> bits[j]
+    M: np.ndarray  # (P, 2^k, 2^k) probe matrix D
+    diagonal: bool
+    slot: int
+    recipe: list
+
+    kind = "probe"
+
+    def touches(self):
+        return set(self.bits)
+
+    def cost(self, ovh):
+        return (1 if self.diagonal else 2 ** len(self.bits)) + ovh
+
+
 def _sub_index(size_bits: int, pos: Sequence[int]) -> tuple[np.ndarray, np.ndarray]:
     idx = np.arange(2**size_bits)
     sub = np.zeros_like(idx)
@@ -206,6 +223,13 @@ class Plan:
                 for step in recipe:
                     M = _Replayer.dense_step(M, step, gates)
                 out[:, off : off + ns * d * d] = M.reshape(npoints, -1)
+            elif kind in ("probe", "probe_diag"):
+                (b,) = shape
+                G = np.asarray(gates[recipe[0][1]])
+                if kind == "probe_diag":
+                    out[:, off : off + 2**b] = np.diagonal(G, axis1=1, axis2=2)
+                else:
+                    out[:, off : off + 4**b] = G.reshape(npoints, -1)
             else:
                 (b,) = shape
                 D = np.ones((npoints, 1), dtype=np.complex128)
@@ -304,10 +328,12 @@ class Planner:
     def _fusion_choice(self, g: BitGate, gi: int, ops, last, S):
         """Returns (delta_cost, action...) for adding gate g to the pass."""
         bits = list(g.bits)
+        if g.probe >= 0:
+            return ((1 if g.diagonal else 2 ** len(bits)) + self.ovh, "new_probe")
         c = max((last.get(b, -1) for b in bits), default=-1)
         new_cost = (2 ** len(bits) if not g.diagonal else 1) + self.ovh
         if not g.diagonal:
-            if c >= 0:
+            if c >= 0 and ops[c].kind != "probe":
                 op = ops[c]
                 if op.kind == "dense":
                     tg = list(op.tg)
@@ -335,6 +361,8 @@ class Planner:
         best = None
         for d in range(len(ops) - 1, lo - 1, -1):
             op = ops[d]
+            if op.kind == "probe":
+                continue
             if op.kind == "dense":
                 tg = list(op.tg)
                 sl = list(op.sl)
@@ -371,7 +399,11 @@ class Planner:
         action = plan[1]
         G = batch[gi]
         bits = list(g.bits)
-        if action == "new_dense":
+        if action == "new_probe":
+            op = _Probe(bits=bits, M=G.copy(), diagonal=g.diagonal, slot=g.probe, recipe=[("probe", gi)])
+            ops.append(op)
+            idx = len(ops) - 1
+        elif action == "new_dense":
             op = _Dense(tg=bits, sl=[], M=G[:, None].copy(), recipe=[("init_dense", gi, len(bits))])
             ops.append(op)
             idx = len(ops) - 1
@@ -485,6 +517,19 @@ class Planner:
                     r["sel"][: len(op.sl)] = [code(b) for b in op.sl]
                     data = op.M[0].reshape(-1)
                     layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2])))
+                elif op.kind == "probe":
+                    r["slot"] = op.slot
+                    r["k"] = len(op.bits)
+                    if op.diagonal:
+                        r["kind"] = _lib.OP_PROBE_DIAG
+                        r["bits"][: len(op.bits)] = [code(b) for b in op.bits]
+                        data = np.diagonal(op.M[0]).copy()
+                        layout.append(("probe_diag", op.recipe, off, (len(op.bits),)))
+                    else:
+                        r["kind"] = _lib.OP_PROBE
+                        r["bits"][: len(op.bits)] = [tile_of[b] for b in op.bits]
+                        data = op.M[0].reshape(-1)
+                        layout.append(("probe", op.recipe, off, (len(op.bits),)))
                 else:
                     r["kind"] = _lib.OP_DIAG
                     r["k"] = len(op.bits)

@@ -205,10 +205,12 @@ int gbq_sv_inner(gbq_ctx* ctx, const gbq_c64* a, const gbq_c64* b, int nbits, do
  * feeding Simulator.simulate_expectation_values_sweep_iter
  * (cirq-core/cirq/sim/sparse_simulator.py:193-218).
  * Point p runs passes [pass_begin, pass_begin+pass_count) of `passes`, with
- * op.mat offsets relative to mat_base, on a 2^nbits state held in scratch
- * slot (CTA) memory, then evaluates the diagonal observable sum_t coef_t
- * Z^{zy_t} given by its Pauli terms; out[2p], out[2p+1] = (re, im) of <obs>.
- * Host arrays: points, passes, ops, terms.  Device array: mats. */
+ * op.mat offsets relative to mat_base, on a 2^nbits state held in one CTA's
+ * scratch slot (all passes use 12-bit tiles, so nbits >= 12), then writes
+ * out[2j], out[2j+1] = (re, im) of coef_j <psi|P_j|psi> for each of its terms
+ * j in [term_begin, term_begin+term_count).  Terms of different points must
+ * not overlap.  Host arrays: points, passes, ops, terms.  Device array: mats.
+ */
 typedef struct gbq_point {
   int32_t nbits;
   int32_t pass_begin;
