@@ -158,17 +158,20 @@ def expectation_of_circuit(circuit, observable, resolver, qubit_order=None) -> c
 
 
 def finite_difference_gradient(
-    circuit, observable, symbols: Sequence[Any], values: Sequence[float], h: float = 1e-3
+    circuit, observable, symbols: Sequence[Any], values: Sequence[float], h: float = 1e-3, indices=None
 ) -> np.ndarray:
-    """Central differences (E(theta+h e_i) - E(theta-h e_i)) / 2h at complex128."""
-    grad = np.zeros(len(symbols))
-    base = dict(zip(symbols, values))
-    for i, s in enumerate(symbols):
+    """Central differences (E(theta+h e_i) - E(theta-h e_i)) / 2h at complex128,
+    for the parameters in `indices` (all by default)."""
+    idx = list(range(len(symbols))) if indices is None else list(indices)
+    grad = np.zeros(len(idx))
+    base = dict(zip(symbols, [float(v) for v in values]))
+    for k, i in enumerate(idx):
+        s = symbols[i]
         plus = dict(base)
         minus = dict(base)
         plus[s] = base[s] + h
         minus[s] = base[s] - h
         ep = expectation_of_circuit(circuit, observable, plus).real
         em = expectation_of_circuit(circuit, observable, minus).real
-        grad[i] = (ep - em) / (2 * h)
+        grad[k] = (ep - em) / (2 * h)
     return grad

@@ -35,7 +35,7 @@ def test_hea_vs_oracle_fd(n, layers):
     r = dict(zip(symbols, values))
     assert abs(E - expectation_of_circuit(circuit, ham, r).real) < TOL
     idx = [0, 1, n, 2 * n - 1, len(symbols) - 1]
-    fd = finite_difference_gradient(circuit, ham, [symbols[i] for i in idx], [values[i] for i in idx], h=1e-3)
+    fd = finite_difference_gradient(circuit, ham, symbols, values, h=1e-3, indices=idx)
     np.testing.assert_allclose(g[idx], fd, atol=TOL)
 
 
