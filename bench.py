@@ -204,6 +204,22 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
     return float(np.mean(times)), int(compiled.plan.pool.nbytes), int(vec_bytes)
 
 
+def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's time (every rank gets it); identity without torch.distributed."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_replica: float, ms_step: float, world: int) -> float:
+    """Whole-job throughput of `world` independent replicas timed by the slowest."""
+    return world * units_per_replica / (ms_step / 1e3)
+
+
 # ---------------------------------------------------------------------------
 # reference (numpy cirq.Simulator) timing on a bounded gate sample
 def reference_gate_rates(n: int, circuit, sample_1q: int = 2, sample_2q: int = 1, repeat: int = 1):
@@ -337,13 +353,8 @@ def main():
             eng, compiled, args.steps, args.warmup, pass_timing=True
         )
     barrier()
-    if dist is not None:
-        import torch
-
-        t = torch.tensor([ms_step], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * ngates / (ms_step / 1e3)
+    ms_step = max_over_ranks(ms_step, dist, device=f"cuda:{local}")
+    value = replica_value(ngates, ms_step, world)
 
     peak, peak_kind = peaks()
     alg_bytes = 16 * (1 << compiled.nbits)

@@ -240,13 +240,24 @@ class CompiledCircuit:
 
     def _plan_resolvers(self, resolvers):
         batch = self.gate_batch(resolvers)
+        # a parameterised gate is planned as diagonal only if it is diagonal at
+        # generic parameter values too, not just at the given points (X**t is
+        # the identity at t = 0); a dense op handles any matrix
+        cirq = _cirq()
+        rs = np.random.RandomState(1234)
+        syms = sorted(
+            {s for src in self.sources if src.const is None for s in cirq.parameter_symbols(src.op)}, key=str
+        )
+        generic = [cirq.ParamResolver({s: float(rs.uniform(0.1, 0.9)) for s in syms}) for _ in range(2)]
         keep = []
         for i, g in enumerate(self.gates):
             m = np.asarray(batch[i])
             d = m.shape[-1]
             g.matrix = m[0]
-            # diagonal only if diagonal at every point (a dense op handles any matrix)
-            g.diagonal = bool(all(is_diagonal(m[p]) for p in range(m.shape[0])))
+            mats = [m[p] for p in range(m.shape[0])]
+            if self.sources[i].const is None:
+                mats += list(self.sources[i].matrices(generic))
+            g.diagonal = bool(all(is_diagonal(x) for x in mats))
             ident = self.sources[i].const is not None and np.array_equal(m[0], np.eye(d))
             if not ident:
                 keep.append(i)

@@ -28,7 +28,7 @@ def test_struct_layouts_match_numpy_mirrors():
         _lib.PAULI_DTYPE.itemsize,
         _lib.POINT_DTYPE.itemsize,
     )
-    assert _lib.OP_DTYPE.fields["mat"][1] == 40
+    assert _lib.OP_DTYPE.fields["mat"][1] == 24
     assert lib.gbq_version() == 1
 
 

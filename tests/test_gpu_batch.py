@@ -26,7 +26,7 @@ def test_batch_qaoa_vs_golden():
 
 def test_batch_mixed_widths_vs_oracle():
     jobs, want = [], []
-    for n, npts in [(12, 6), (14, 5), (16, 4), (13, 3)]:
+    for n, npts in [(12, 6), (14, 5), (16, 4), (10, 3)]:
         circuit, gammas, betas, obs, edges = workloads.qaoa_circuit(n, 4, seed=n)
         pts = workloads.qaoa_points(4, npts, seed=100 + n)
         res = _resolvers(gammas, betas, pts)

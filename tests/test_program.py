@@ -1,0 +1,96 @@
+"""Host-side compilation: planner encoding checked with the CPU emulator
+against the reference's golden states (no GPU needed)."""
+
+import numpy as np
+import pytest
+import sympy
+
+import cirq
+from cirq_gb300 import workloads
+from cirq_gb300.planner import Planner
+from cirq_gb300.program import CompiledCircuit, split_measurements
+from emulator import run_program
+from oracle.circuits import simulate_density_matrix, simulate_state_vector
+
+GOLD = np.load(__file__.replace("test_program.py", "golden/golden.npz"))
+
+PLANNERS = [
+    Planner(tile_bits=10, kmax=3, budget=20),
+    Planner(tile_bits=12, kmax=4),
+    Planner(tile_bits=10, kmax=2, budget=8),
+    Planner(tile_bits=11, kmax=5, budget=100),
+    Planner(tile_bits=13, kmax=1, budget=6),
+]
+
+
+def _emulate(compiled, resolver=None, initial=0):
+    nb = compiled.nbits_dev
+    psi = np.zeros(2**nb, complex)
+    psi[initial] = 1
+    pool = compiled.pool([resolver or cirq.ParamResolver({})])[0].astype(np.complex128)
+    return run_program(psi, nb, compiled.plan.passes, compiled.plan.ops, pool)
+
+
+@pytest.mark.parametrize("planner", PLANNERS, ids=lambda p: f"L{p.tile_bits}k{p.kmax}b{p.budget}")
+@pytest.mark.parametrize("n,d,s", [(10, 20, 1), (12, 8, 2), (5, 6, 3)])
+def test_layers_plan_vs_golden(planner, n, d, s):
+    c = workloads.random_layer_circuit(n, d, s)
+    body, _ = split_measurements(c)
+    cc = CompiledCircuit(body, sorted(c.all_qubits()), dm=False, planner=planner, resolvers=[cirq.ParamResolver({})])
+    out = _emulate(cc)
+    np.testing.assert_allclose(out[: 2**n], GOLD[f"layers_n{n}_d{d}_s{s}_c128"], atol=1e-6)
+    assert np.abs(out[2**n :]).max(initial=0) == 0
+
+
+def test_gate_zoo_plan_vs_golden():
+    import make_zoo
+
+    zoo = make_zoo.gate_zoo()
+    body, _ = split_measurements(zoo)
+    for planner in PLANNERS:
+        cc = CompiledCircuit(body, sorted(zoo.all_qubits()), dm=False, planner=planner, resolvers=[cirq.ParamResolver({})])
+        np.testing.assert_allclose(_emulate(cc)[:32], GOLD["zoo_c128"], atol=1e-6)
+
+
+def test_density_plan_vs_golden():
+    c = workloads.noisy_layer_circuit(4, 4, seed=2, p=0.05, gamma=0.1)
+    body, _ = split_measurements(c)
+    for planner in PLANNERS:
+        cc = CompiledCircuit(body, sorted(c.all_qubits()), dm=True, planner=planner, resolvers=[cirq.ParamResolver({})])
+        out = _emulate(cc)[: 4**4].reshape(16, 16)
+        np.testing.assert_allclose(out, GOLD["dm_noisy_n4_d4"], atol=1e-6)
+
+
+def test_sweep_replay_matches_per_point_planning():
+    """Pools replayed from one plan equal the states of per-point simulation,
+    including points where a parameterised gate degenerates (X**0 = I)."""
+    t, u = sympy.symbols("t u")
+    q = cirq.LineQubit.range(11)
+    c = cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.X(q[0]) ** t,
+        cirq.ZZPowGate(exponent=u).on(q[1], q[9]),
+        cirq.CZ(q[0], q[10]) ** t,
+        cirq.rx(u).on(q[5]),
+        cirq.CNOT(q[5], q[3]),
+    )
+    pts = [{t: 0.0, u: 0.0}, {t: 1.0, u: 0.5}, {t: 0.3, u: -1.7}]
+    res = [cirq.ParamResolver(p) for p in pts]
+    cc = CompiledCircuit(split_measurements(c)[0], q, dm=False, planner=Planner(tile_bits=10), resolvers=res[:1])
+    for r in res:
+        want = simulate_state_vector(c, r)
+        np.testing.assert_allclose(_emulate(cc, r)[: 2**11], want, atol=1e-6)
+
+
+def test_unsupported_operations_raise():
+    q = cirq.LineQubit.range(6)
+    with pytest.raises(NotImplementedError):
+        CompiledCircuit([cirq.MatrixGate(cirq.testing.random_unitary(64)).on(*q)], q, dm=False,
+                        planner=Planner(), resolvers=[cirq.ParamResolver({})])
+    with pytest.raises(NotImplementedError):
+        CompiledCircuit([cirq.depolarize(0.1).on(q[0])], q, dm=False, planner=Planner(),
+                        resolvers=[cirq.ParamResolver({})])
+    qt = cirq.LineQid.range(2, dimension=3)
+    with pytest.raises(NotImplementedError):
+        CompiledCircuit([cirq.MatrixGate(np.eye(3), qid_shape=(3,)).on(qt[0])], qt, dm=False,
+                        planner=Planner(), resolvers=[cirq.ParamResolver({})])
