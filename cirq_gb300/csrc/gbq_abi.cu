@@ -99,20 +99,118 @@ static uint32_t bank_col(int b) { return phys_const(1u << b) & 15u; }
 // bank columns are independent (conflict-free half-warps), the other free
 // bits, then the tile bits used as selectors (so a selector is uniform over
 // a warp and the matrix loads do not diverge).
-static int convert_op(const gbq_op& op, int L, int nbits, uint64_t inmask, bool dual, OpDev& d) {
+// Register layout in force while converting the ops of one pass:
+// reg[p] = tile bit of register position p, nreg = 0 outside a phase.
+struct LayoutState {
+  int nreg = 0;
+  int reg[5] = {0, 0, 0, 0, 0};
+};
+
+// Thread-bit order of a layout: 4 bank-independent bits first.
+static void thread_bit_order(int L, uint32_t regmask, int* order, int& no) {
+  no = 0;
+  uint32_t basis[4] = {0, 0, 0, 0};
+  int nbasis = 0;
+  uint32_t used = regmask;
+  for (int b = 0; b < L && nbasis < 4; ++b) {
+    if ((used >> b) & 1u) continue;
+    uint32_t v = phys_const(1u << b) & 15u;
+    for (int i = 0; i < nbasis; ++i)
+      if ((v ^ basis[i]) < v) v ^= basis[i];
+    if (!v) continue;
+    basis[nbasis++] = v;
+    for (int i = nbasis - 1; i > 0 && basis[i] > basis[i - 1]; --i) {
+      const uint32_t t = basis[i];
+      basis[i] = basis[i - 1];
+      basis[i - 1] = t;
+    }
+    order[no++] = b;
+    used |= 1u << b;
+  }
+  for (int b = 0; b < L; ++b)
+    if (!((used >> b) & 1u)) order[no++] = b;
+}
+
+static int convert_op(const gbq_op& op, int L, int nbits, uint64_t inmask, bool dual, OpDev& d,
+                      LayoutState& lay) {
   memset(&d, 0, sizeof(d));
-  const bool dense = op.kind == GBQ_OP_DENSE || op.kind == GBQ_OP_PROBE;
-  const bool diag = op.kind == GBQ_OP_DIAG || op.kind == GBQ_OP_PROBE_DIAG;
-  if (!dense && !diag) return arg_fail("op: unknown kind");
-  if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && !dual)
-    return arg_fail("op: probe ops need a two-state pass");
-  if ((op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG) && op.slot < 0)
-    return arg_fail("op: probe slot < 0");
+  const int kind = op.kind;
+  const bool reg = kind == GBQ_OP_RDENSE || kind == GBQ_OP_RDIAG || kind == GBQ_OP_RPROBE ||
+                   kind == GBQ_OP_RPROBE_DIAG;
+  if (kind == GBQ_OP_LAYOUT) {
+    const int R = L - 8;
+    if (L > 12) return arg_fail("op: register layouts need tile widths 10..12");
+    if (op.k != R) return arg_fail("op: a layout names exactly L - 8 register bits");
+    uint32_t regmask = 0;
+    for (int p = 0; p < R; ++p) {
+      const int b = op.bits[p];
+      if (b < 0 || b >= L || ((regmask >> b) & 1u)) return arg_fail("op: layout bit invalid");
+      regmask |= 1u << b;
+      d.pcol[p] = phys_const(1u << b);
+      d.rbits[p] = (int8_t)b;
+      lay.reg[p] = b;
+    }
+    lay.nreg = R;
+    int order[GBQ_MAX_TILE_BITS];
+    int no = 0;
+    thread_bit_order(L, regmask, order, no);
+    if (no != 8) return arg_fail("op: internal layout error");
+    for (int j = 0; j < 8; ++j) {
+      d.gcol[j] = phys_const(1u << order[j]);
+      d.tcol[j] = (uint16_t)(1u << order[j]);
+    }
+    d.kind = (int8_t)kind;
+    d.k = (int8_t)R;
+    return GBQ_OK;
+  }
+  if (reg && lay.nreg == 0) return arg_fail("op: register op outside a register layout");
+  if (!reg) lay.nreg = 0;  // a plain op ends the phase
+  const bool dense = kind == GBQ_OP_DENSE || kind == GBQ_OP_PROBE;
+  const bool diag = kind == GBQ_OP_DIAG || kind == GBQ_OP_PROBE_DIAG;
+  const bool rdense = kind == GBQ_OP_RDENSE || kind == GBQ_OP_RPROBE;
+  const bool rdiag = kind == GBQ_OP_RDIAG || kind == GBQ_OP_RPROBE_DIAG;
+  const bool probe = kind == GBQ_OP_PROBE || kind == GBQ_OP_PROBE_DIAG || kind == GBQ_OP_RPROBE ||
+                     kind == GBQ_OP_RPROBE_DIAG;
+  if (!dense && !diag && !rdense && !rdiag) return arg_fail("op: unknown kind");
+  if (probe && !dual) return arg_fail("op: probe ops need a two-state pass");
+  if (probe && op.slot < 0) return arg_fail("op: probe slot < 0");
   if (op.mat < 0 || (op.mat & 1)) return arg_fail("op: matrix offset must be even and >= 0");
   d.kind = op.kind;
   d.k = op.k;
   d.slot = op.slot;
   d.mat = op.mat;
+  for (int p = 0; p < lay.nreg; ++p) d.rbits[p] = (int8_t)lay.reg[p];
+  if (rdense) {
+    const int kmax = kind == GBQ_OP_RPROBE ? 3 : 4;
+    if (op.k < 1 || op.k > kmax || op.k > lay.nreg) return arg_fail("op: register dense k out of range");
+    if (op.nsel < 0 || op.nsel > 3) return arg_fail("op: nsel out of range");
+    int mask = 0, lastpos = -1;
+    for (int j = 0; j < op.k; ++j) {
+      int pos = -1;
+      for (int p = 0; p < lay.nreg; ++p)
+        if (lay.reg[p] == op.bits[j]) pos = p;
+      if (pos < 0) return arg_fail("op: register op target is not a register bit");
+      if (pos <= lastpos) return arg_fail("op: register op targets must ascend in register position");
+      lastpos = pos;
+      mask |= 1 << pos;
+    }
+    d.rmask = (int8_t)mask;
+    d.nsel = op.nsel;
+    for (int j = 0; j < op.nsel; ++j) {
+      const int sb = op.sel[j];
+      if (sb >= 0) {
+        if (sb >= L) return arg_fail("op: selector tile bit out of range");
+        for (int p = 0; p < lay.nreg; ++p)
+          if (lay.reg[p] == sb) return arg_fail("op: register op selector is a register bit");
+      } else {
+        const int gb = -sb - 1;
+        if (gb >= nbits || ((inmask >> gb) & 1ull))
+          return arg_fail("op: selector global bit invalid (must be outside the tile)");
+      }
+      d.selg[j] = (int8_t)sb;
+    }
+    return GBQ_OK;
+  }
   if (dense) {
     const int kmax = op.kind == GBQ_OP_PROBE ? 3 : GBQ_MAX_DENSE_K;
     if (op.k < 1 || op.k > kmax || op.k > L) return arg_fail("op: dense k out of range");
@@ -178,6 +276,7 @@ static int convert_op(const gbq_op& op, int L, int nbits, uint64_t inmask, bool 
       }
     }
   } else {
+    // plain and register diagonal ops share the table encoding
     if (op.k < 1 || op.k > GBQ_MAX_DIAG_K) return arg_fail("op: diag k out of range");
     for (int j = 0; j < 8; ++j) d.dext[j] = -1;
     for (int j = 0; j < op.k; ++j) {
@@ -260,8 +359,9 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
     uint64_t inmask = 0;
     int rc = pass_geometry(passes[q], nops, nbits, a.ti, inmask);
     if (rc) return rc;
+    LayoutState lay;
     for (int o = 0; o < passes[q].op_count; ++o) {
-      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual, a.ops[o]);
+      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual, a.ops[o], lay);
       if (rc) return rc;
     }
     a.psi = psi;
@@ -759,9 +859,10 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
       uint64_t inmask = 0;
       int rc = pass_geometry(ps, nops, pt.nbits, ti, inmask);
       if (rc) return rc;
+      LayoutState lay;
       for (int o = 0; o < ps.op_count; ++o) {
         OpDev d;
-        rc = convert_op(ops[ps.op_begin + o], ps.L, pt.nbits, inmask, false, d);
+        rc = convert_op(ops[ps.op_begin + o], ps.L, pt.nbits, inmask, false, d, lay);
         if (rc) return rc;
         if (!converted[pt.pass_begin + q]) dops[ps.op_begin + o] = d;
       }

@@ -49,12 +49,16 @@ __host__ __device__ constexpr uint32_t phys_const(uint32_t i) {
 
 // Device form of one op, derived on the host from the public gbq_op.
 struct OpDev {
-  int8_t kind, k, nsel, pad0;
-  int8_t selg[4];     // selector s: group-index bit (>= 0) or -(global bit)-1
-  uint32_t pcol[5];   // shared-index column of each target bit
-  uint32_t gcol[13];  // shared-index column of each group-index bit
+  int8_t kind, k, nsel, rmask;  // rmask: register-op target positions
+  int8_t selg[4];     // selector s: group-index bit (dense) or tile bit (register
+                      // ops), >= 0; or -(global bit)-1
+  uint32_t pcol[5];   // shared-index column of each target / register bit
+  uint32_t gcol[13];  // shared-index column of each group-index / thread bit
   uint16_t dcol[13];  // diag: table-index contribution of each tile bit
+  uint16_t tcol[8];   // layout: tile-index column of each thread bit
   int8_t dext[8];     // diag: global bit feeding table bit j, or -1
+  int8_t rbits[5];    // layout: tile bit of each register position
+  int8_t pad2[3];
   int32_t slot;
   int32_t pad1;
   int64_t mat;

@@ -282,14 +282,18 @@ __device__ __forceinline__ void op_diag(const TileInfo& ti, const OpDev& op, flo
     cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
 }
 
-// KMAX: widest dense op the kernel variant contains (2 or 5); narrower
-// variants keep register pressure (and spills) down for the common case.
+// KMAX: widest shared-memory dense op the kernel variant contains (0 or 5);
+// the KMAX = 0 variant (register phases only) keeps register pressure down.
 template <int LT, int KMAX, bool DUAL>
 __device__ __forceinline__ void dispatch(const TileInfo& ti, const OpDev& op, float2* smA,
                                          float2* smB, uint64_t gbase, int64_t tile, double* red) {
   switch (op.kind * 8 + op.k) {
-    case GBQ_OP_DENSE * 8 + 1: op_dense<1, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red); break;
-    case GBQ_OP_DENSE * 8 + 2: op_dense<2, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red); break;
+    case GBQ_OP_DENSE * 8 + 1:
+      if constexpr (KMAX >= 1) op_dense<1, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      break;
+    case GBQ_OP_DENSE * 8 + 2:
+      if constexpr (KMAX >= 2) op_dense<2, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
+      break;
     case GBQ_OP_DENSE * 8 + 3:
       if constexpr (KMAX >= 3) op_dense<3, LT, DUAL, false>(ti, op, smA, smB, gbase, tile, red);
       break;
@@ -306,10 +310,10 @@ __device__ __forceinline__ void dispatch(const TileInfo& ti, const OpDev& op, fl
         if (op.kind == GBQ_OP_PROBE_DIAG) {
           op_diag<LT, true, true>(ti, op, smA, smB, gbase, tile, red);
         } else if (op.kind == GBQ_OP_PROBE) {
-          if (op.k == 1) op_dense<1, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
-          else if (op.k == 2) op_dense<2, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
-          else if constexpr (KMAX >= 3) {
-            if (op.k == 3) op_dense<3, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+          if constexpr (KMAX >= 3) {
+            if (op.k == 1) op_dense<1, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+            else if (op.k == 2) op_dense<2, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
+            else if (op.k == 3) op_dense<3, LT, true, true>(ti, op, smA, smB, gbase, tile, red);
           }
         }
       }
@@ -382,20 +386,284 @@ __device__ __forceinline__ TileSetup tile_setup(const TileInfo& ti, uint64_t* so
   return s;
 }
 
+// ---- register phases -------------------------------------------------------------
+// Inside a phase every thread owns A = 2^R amplitudes (R = LT - 8) that
+// differ only in the R register bits of the current layout; register ops act
+// on them in registers, with no shared-memory traffic and no barrier.
+
+__host__ __device__ constexpr int popc_const(int x) { return x ? (x & 1) + popc_const(x >> 1) : 0; }
+// Deposits the low bits of x into the set positions of mask.
+__host__ __device__ constexpr int dep_const(int x, int mask) {
+  int r = 0, i = 0;
+  for (int b = 0; b < 8; ++b)
+    if ((mask >> b) & 1) {
+      if ((x >> i) & 1) r |= 1 << b;
+      ++i;
+    }
+  return r;
+}
+
+template <int LT, bool DUAL>
+struct RegState {
+  static constexpr int R = LT - 8;
+  static constexpr int A = 1 << R;
+  float2 v[A];
+  float2 w[DUAL ? A : 1];
+  uint32_t phys_t;  // shared index of slot 0
+  uint32_t pc[R];   // shared-index column of register position p
+  uint32_t tidx;    // tile index of slot 0 (thread bits only)
+};
+
+template <int LT, bool DUAL>
+__device__ __forceinline__ uint32_t slot_phys(const RegState<LT, DUAL>& st, int s) {
+  uint32_t p = st.phys_t;
+#pragma unroll
+  for (int b = 0; b < RegState<LT, DUAL>::R; ++b)
+    if ((s >> b) & 1) p ^= st.pc[b];
+  return p;
+}
+
+template <int LT, bool DUAL>
+__device__ __forceinline__ void phase_enter(RegState<LT, DUAL>& st, const OpDev& op,
+                                            const float2* smA, const float2* smB) {
+  constexpr int R = RegState<LT, DUAL>::R;
+  const int t = threadIdx.x;
+  uint32_t ph = 0, ti = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if ((t >> j) & 1) {
+      ph ^= op.gcol[j];
+      ti ^= op.tcol[j];
+    }
+  st.phys_t = ph;
+  st.tidx = ti;
+#pragma unroll
+  for (int p = 0; p < R; ++p) st.pc[p] = op.pcol[p];
+#pragma unroll
+  for (int s = 0; s < RegState<LT, DUAL>::A; ++s) {
+    const uint32_t a = slot_phys(st, s);
+    st.v[s] = smA[a];
+    if constexpr (DUAL) st.w[s] = smB[a];
+  }
+}
+
+template <int LT, bool DUAL>
+__device__ __forceinline__ void phase_exit(const RegState<LT, DUAL>& st, float2* smA, float2* smB) {
+#pragma unroll
+  for (int s = 0; s < RegState<LT, DUAL>::A; ++s) {
+    const uint32_t a = slot_phys(st, s);
+    smA[a] = st.v[s];
+    if constexpr (DUAL) smB[a] = st.w[s];
+  }
+}
+
+template <int LT, bool DUAL>
+__device__ __forceinline__ const float2* reg_matrix(const TileInfo& ti, const OpDev& op,
+                                                    const RegState<LT, DUAL>& st, uint64_t gbase,
+                                                    int dd) {
+  uint32_t sel = 0;
+  for (int s = 0; s < op.nsel; ++s) {
+    const int c = op.selg[s];
+    const uint32_t bit = c >= 0 ? (st.tidx >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
+    sel |= bit << s;
+  }
+  return ti.mats + op.mat + (int64_t)sel * dd;
+}
+
+// Dense op (or dense probe) on the register positions in MASK.
+template <int MASK, int LT, bool DUAL, bool PROBE>
+__device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
+                                          RegState<LT, DUAL>& st, uint64_t gbase, int64_t tile,
+                                          double* red) {
+  constexpr int R = RegState<LT, DUAL>::R;
+  constexpr int A = RegState<LT, DUAL>::A;
+  constexpr int K = popc_const(MASK);
+  constexpr int D = 1 << K;
+  constexpr int NG = A / D;
+  constexpr int REST = (A - 1) & ~MASK;
+  const float2* mp = reg_matrix(ti, op, st, gbase, D * D);
+  float part = 0.f;
+  if constexpr (K <= 2) {
+    float2 m[D * D];
+#pragma unroll
+    for (int e = 0; e < D * D; e += 2) {
+      const float4 mm = __ldg(reinterpret_cast<const float4*>(mp + e));
+      m[e] = make_float2(mm.x, mm.y);
+      m[e + 1] = make_float2(mm.z, mm.w);
+    }
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_const(g, REST);
+      float2 in[D];
+      float2 inb[DUAL ? D : 1];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        in[j] = st.v[s0 | dep_const(j, MASK)];
+        if constexpr (DUAL) inb[j] = st.w[s0 | dep_const(j, MASK)];
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; ++c) cfma(acc, m[r * D + c], in[c]);
+        if constexpr (PROBE) {
+          const float2 l = st.w[s0 | dep_const(r, MASK)];
+          part = fmaf(l.x, acc.x, fmaf(l.y, acc.y, part));
+        } else {
+          st.v[s0 | dep_const(r, MASK)] = acc;
+          if constexpr (DUAL) {
+            float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < D; ++c) cfma(accb, m[r * D + c], inb[c]);
+            st.w[s0 | dep_const(r, MASK)] = accb;
+          }
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_const(g, REST);
+      float2 in[D];
+      float2 inb[DUAL ? D : 1];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        in[j] = st.v[s0 | dep_const(j, MASK)];
+        if constexpr (DUAL) inb[j] = st.w[s0 | dep_const(j, MASK)];
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        const float2* row = mp + r * D;
+        float2 acc = make_float2(0.f, 0.f);
+        float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; c += 2) {
+          const float4 mm = __ldg(reinterpret_cast<const float4*>(row + c));
+          cfma(acc, make_float2(mm.x, mm.y), in[c]);
+          cfma(acc, make_float2(mm.z, mm.w), in[c + 1]);
+          if constexpr (DUAL && !PROBE) {
+            cfma(accb, make_float2(mm.x, mm.y), inb[c]);
+            cfma(accb, make_float2(mm.z, mm.w), inb[c + 1]);
+          }
+        }
+        if constexpr (PROBE) {
+          const float2 l = st.w[s0 | dep_const(r, MASK)];
+          part = fmaf(l.x, acc.x, fmaf(l.y, acc.y, part));
+        } else {
+          st.v[s0 | dep_const(r, MASK)] = acc;
+          if constexpr (DUAL) st.w[s0 | dep_const(r, MASK)] = accb;
+        }
+      }
+    }
+  }
+  if constexpr (PROBE)
+    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+  (void)R;
+}
+
+// Diagonal op (or diagonal probe) in registers; bits may be register,
+// thread or out-of-tile bits.
+template <int LT, bool DUAL, bool PROBE>
+__device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
+                                         RegState<LT, DUAL>& st, uint64_t gbase, int64_t tile,
+                                         double* red) {
+  constexpr int R = RegState<LT, DUAL>::R;
+  constexpr int A = RegState<LT, DUAL>::A;
+  uint32_t base = 0;
+  for (int j = 0; j < op.k; ++j)
+    if (op.dext[j] >= 0) base |= (uint32_t)((gbase >> op.dext[j]) & 1u) << j;
+#pragma unroll
+  for (int b = 0; b < LT; ++b)
+    if ((st.tidx >> b) & 1u) base ^= op.dcol[b];
+  uint32_t rc[R];
+#pragma unroll
+  for (int p = 0; p < R; ++p) rc[p] = op.dcol[op.rbits[p]];
+  const float2* tab = ti.mats + op.mat;
+  float part = 0.f;
+#pragma unroll
+  for (int s = 0; s < A; ++s) {
+    uint32_t idx = base;
+#pragma unroll
+    for (int p = 0; p < R; ++p)
+      if ((s >> p) & 1) idx ^= rc[p];
+    const float2 d = __ldg(tab + idx);
+    if constexpr (PROBE) {
+      const float2 y = cmul(d, st.v[s]);
+      const float2 l = st.w[s];
+      part = fmaf(l.x, y.x, fmaf(l.y, y.y, part));
+    } else {
+      st.v[s] = cmul(d, st.v[s]);
+      if constexpr (DUAL) st.w[s] = cmul(d, st.w[s]);
+    }
+  }
+  if constexpr (PROBE)
+    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+}
+
+template <int LT, int KMAX, bool DUAL, bool PROBE, int M = 1>
+__device__ __forceinline__ void reg_dense_dispatch(const TileInfo& ti, const OpDev& op,
+                                                   RegState<LT, DUAL>& st, uint64_t gbase,
+                                                   int64_t tile, double* red) {
+  if constexpr (M < (1 << RegState<LT, DUAL>::R)) {
+    if (op.rmask == M) {
+      if constexpr (!PROBE || popc_const(M) <= 3)
+        reg_dense<M, LT, DUAL, PROBE>(ti, op, st, gbase, tile, red);
+    } else {
+      reg_dense_dispatch<LT, KMAX, DUAL, PROBE, M + 1>(ti, op, st, gbase, tile, red);
+    }
+  }
+}
+
 template <int LT, int KMAX, bool DUAL>
 __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, float2* smA,
                                         float2* smB, uint64_t gbase, int64_t tile, double* red) {
-  for (int o = 0; o < ti.nops; ++o) {
-    dispatch<LT, KMAX, DUAL>(ti, sops[o], smA, smB, gbase, tile, red);
-    __syncthreads();
+  if constexpr (LT <= 12) {
+    RegState<LT, DUAL> st;
+    bool in_phase = false;
+    for (int o = 0; o < ti.nops; ++o) {
+      const OpDev& op = sops[o];
+      const int kind = op.kind;
+      if (kind == GBQ_OP_LAYOUT) {
+        if (in_phase) {
+          phase_exit(st, smA, smB);
+          __syncthreads();
+        }
+        phase_enter(st, op, smA, smB);
+        in_phase = true;
+      } else if (kind == GBQ_OP_RDENSE) {
+        reg_dense_dispatch<LT, KMAX, DUAL, false>(ti, op, st, gbase, tile, red);
+      } else if (kind == GBQ_OP_RDIAG) {
+        reg_diag<LT, DUAL, false>(ti, op, st, gbase, tile, red);
+      } else if (kind == GBQ_OP_RPROBE) {
+        if constexpr (DUAL) reg_dense_dispatch<LT, KMAX, true, true>(ti, op, st, gbase, tile, red);
+      } else if (kind == GBQ_OP_RPROBE_DIAG) {
+        if constexpr (DUAL) reg_diag<LT, true, true>(ti, op, st, gbase, tile, red);
+      } else {
+        if (in_phase) {
+          phase_exit(st, smA, smB);
+          __syncthreads();
+          in_phase = false;
+        }
+        dispatch<LT, KMAX, DUAL>(ti, op, smA, smB, gbase, tile, red);
+        __syncthreads();
+      }
+    }
+    if (in_phase) {
+      phase_exit(st, smA, smB);
+      __syncthreads();
+    }
+  } else {
+    for (int o = 0; o < ti.nops; ++o) {
+      dispatch<LT, KMAX, DUAL>(ti, sops[o], smA, smB, gbase, tile, red);
+      __syncthreads();
+    }
   }
 }
 
 // Two shared buffers per state: tile i is processed in one while tile i+1
 // streams into the other (cp.async groups, waited with wait_group 1).
 template <int LT, int KMAX, bool DUAL>
-__global__ void __launch_bounds__(kThreads, KMAX <= 2 ? 3 : 2)
-    k_tile_pass(const __grid_constant__ PassArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t soff[1 << (LT - 9)];
@@ -466,12 +734,13 @@ int launch_tile_pass(Ctx* c, const PassArgs& a) {
   return GBQ_OK;
 }
 
-// Widest dense (or dense-probe) op of a pass.
+// Widest shared-memory dense (or dense-probe) op of a pass (0 if none).
 inline int pass_kmax(const PassArgs& a) {
-  int k = 1;
-  for (int o = 0; o < a.ti.nops; ++o)
-    if ((a.ops[o].kind == GBQ_OP_DENSE || a.ops[o].kind == GBQ_OP_PROBE) && a.ops[o].k > k)
-      k = a.ops[o].k;
+  int k = 0;
+  for (int o = 0; o < a.ti.nops; ++o) {
+    const int kind = a.ops[o].kind;
+    if ((kind == GBQ_OP_DENSE || kind == GBQ_OP_PROBE) && a.ops[o].k > k) k = a.ops[o].k;
+  }
   return k;
 }
 

@@ -5,10 +5,10 @@ namespace gbq {
 
 int launch_pass_l10(Ctx* c, const PassArgs& a, bool dual) {
   if (dual) {
-    if (pass_kmax(a) <= 2) return launch_tile_pass<10, 2, true>(c, a);
+    if (pass_kmax(a) == 0) return launch_tile_pass<10, 0, true>(c, a);
     return launch_tile_pass<10, 5, true>(c, a);
   }
-  if (pass_kmax(a) <= 2) return launch_tile_pass<10, 2, false>(c, a);
+  if (pass_kmax(a) == 0) return launch_tile_pass<10, 0, false>(c, a);
   return launch_tile_pass<10, 5, false>(c, a);
 }
 

@@ -4,8 +4,11 @@
 namespace gbq {
 
 int launch_pass_l12(Ctx* c, const PassArgs& a, bool dual) {
-  if (dual) return launch_tile_pass<12, 5, true>(c, a);
-  if (pass_kmax(a) <= 2) return launch_tile_pass<12, 2, false>(c, a);
+  if (dual) {
+    if (pass_kmax(a) == 0) return launch_tile_pass<12, 0, true>(c, a);
+    return launch_tile_pass<12, 5, true>(c, a);
+  }
+  if (pass_kmax(a) == 0) return launch_tile_pass<12, 0, false>(c, a);
   return launch_tile_pass<12, 5, false>(c, a);
 }
 

@@ -216,12 +216,14 @@ class Plan:
         Returns complex64 (P, pool_len).
         """
         out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
-        for kind, recipe, off, shape in self.layout:
+        for kind, recipe, off, shape, perm in self.layout:
             if kind == "dense":
                 ns, d = shape
                 M = np.broadcast_to(np.eye(1, dtype=np.complex128), (npoints, 1, 1, 1)).copy()
                 for step in recipe:
                     M = _Replayer.dense_step(M, step, gates)
+                if perm is not None:
+                    M = M[:, :, perm[:, None], perm[None, :]]
                 out[:, off : off + ns * d * d] = M.reshape(npoints, -1)
             elif kind in ("probe", "probe_diag"):
                 (b,) = shape
@@ -229,6 +231,8 @@ class Plan:
                 if kind == "probe_diag":
                     out[:, off : off + 2**b] = np.diagonal(G, axis1=1, axis2=2)
                 else:
+                    if perm is not None:
+                        G = G[:, perm[:, None], perm[None, :]]
                     out[:, off : off + 4**b] = G.reshape(npoints, -1)
             else:
                 (b,) = shape
@@ -249,6 +253,7 @@ class Planner:
         kmax: int = 4,
         budget: float = 40.0,
         op_overhead: float = 1.0,
+        use_registers: bool = True,
     ):
         if not 1 <= kmax <= 5:
             raise ValueError("fusion width kmax must be in 1..5")
@@ -259,6 +264,7 @@ class Planner:
         self.kmax = kmax
         self.budget = budget
         self.ovh = op_overhead
+        self.use_registers = use_registers
 
     # ------------------------------------------------------------------
     def plan(self, gates: Sequence[BitGate], nbits: int, batch: dict | None = None) -> Plan:
@@ -482,16 +488,75 @@ class Planner:
         ops[idx] = op
         return op
 
+    # ---- register phases ---------------------------------------------------------
+    def _phases(self, pp: PassPlan) -> list:
+        """Splits a pass's ops into register phases.
+
+        Returns a list of items ("layout", [register bits]) or ("op", op, reg)
+        where reg tells whether the op runs on registers.  A phase is a run of
+        consecutive ops whose dense targets fit R = L - 8 register bits and
+        whose selector bits stay out of them; diagonal ops join any phase."""
+        R = pp.L - 8 if (self.use_registers and pp.L <= 12) else 0
+        tile = set(range(pp.m)) | set(pp.hi)
+        ops = pp.ops
+        items = []
+
+        def targets(op):
+            if op.kind == "dense":
+                return list(op.tg)
+            if op.kind == "probe" and not op.diagonal:
+                return list(op.bits)
+            return []
+
+        def eligible(op):
+            if op.kind == "dense":
+                return len(op.tg) <= min(R, 4)
+            if op.kind == "probe" and not op.diagonal:
+                return len(op.bits) <= min(R, 3)
+            return R > 0
+
+        def local_sels(op):
+            return [b for b in getattr(op, "sl", []) if b in tile]
+
+        i = 0
+        while i < len(ops):
+            if not R or not eligible(ops[i]) or not targets(ops[i]):
+                if R and eligible(ops[i]) and items and items[-1][0] == "op" and items[-1][2]:
+                    items.append(("op", ops[i], True))  # diagonal op inside the open phase
+                else:
+                    items.append(("op", ops[i], False))
+                i += 1
+                continue
+            rb: list = []
+            sels: set = set()
+            j = i
+            while j < len(ops) and eligible(ops[j]):
+                need = [b for b in targets(ops[j]) if b not in rb]
+                nsel = sels | set(local_sels(ops[j]))
+                if len(rb) + len(need) > R or any(b in nsel for b in rb + need):
+                    break
+                rb += need
+                sels = nsel
+                j += 1
+            free = [b for b in sorted(tile, reverse=True) if b not in rb and b not in sels]
+            rb += free[: R - len(rb)]
+            items.append(("layout", rb))
+            for o in ops[i:j]:
+                items.append(("op", o, True))
+            i = j
+        return items
+
     # ---- emission -----------------------------------------------------------
     def _emit(self, pass_plans, nbits, ngates) -> Plan:
+        phased = [self._phases(pp) for pp in pass_plans]
         passes = np.zeros(len(pass_plans), dtype=_lib.PASS_DTYPE)
-        nops = sum(len(pp.ops) for pp in pass_plans)
+        nops = sum(len(items) for items in phased)
         ops = np.zeros(nops, dtype=_lib.OP_DTYPE)
         layout = []
         chunks = []
         off = 0
         oi = 0
-        for q, pp in enumerate(pass_plans):
+        for q, (pp, items) in enumerate(zip(pass_plans, phased)):
             tile_of = {b: b for b in range(pp.m)}
             for j, b in enumerate(pp.hi):
                 tile_of[b] = pp.m + j
@@ -499,50 +564,75 @@ class Planner:
             rec["L"] = pp.L
             rec["m"] = pp.m
             rec["op_begin"] = oi
-            rec["op_count"] = len(pp.ops)
+            rec["op_count"] = len(items)
             rec["hi"][: len(pp.hi)] = pp.hi
 
             def code(b):
                 return tile_of[b] if b in tile_of else -(b + 1)
 
-            for op in pp.ops:
+            rb_cur: list = []
+            for item in items:
                 r = ops[oi]
+                oi += 1
+                if item[0] == "layout":
+                    rb_cur = item[1]
+                    r["kind"] = _lib.OP_LAYOUT
+                    r["k"] = len(rb_cur)
+                    r["bits"][: len(rb_cur)] = [tile_of[b] for b in rb_cur]
+                    continue
+                _, op, reg = item
+                perm = None
                 if op.kind == "dense":
-                    k = len(op.tg)
-                    tbits = [tile_of[b] for b in op.tg]
-                    r["kind"] = _lib.OP_DENSE
+                    tg = list(op.tg)
+                    if reg:
+                        order = sorted(range(len(tg)), key=lambda j: rb_cur.index(tg[j]))
+                        if order != list(range(len(tg))):
+                            perm = _bit_perm_index(order)
+                        tg = [tg[o] for o in order]
+                    k = len(tg)
+                    r["kind"] = _lib.OP_RDENSE if reg else _lib.OP_DENSE
                     r["k"] = k
                     r["nsel"] = len(op.sl)
-                    r["bits"][:k] = tbits
+                    r["bits"][:k] = [tile_of[b] for b in tg]
                     r["sel"][: len(op.sl)] = [code(b) for b in op.sl]
-                    data = op.M[0].reshape(-1)
-                    layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2])))
+                    data = op.M[0]
+                    if perm is not None:
+                        data = data[:, perm[:, None], perm[None, :]]
+                    data = data.reshape(-1)
+                    layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2]), perm))
                 elif op.kind == "probe":
                     r["slot"] = op.slot
                     r["k"] = len(op.bits)
                     if op.diagonal:
-                        r["kind"] = _lib.OP_PROBE_DIAG
+                        r["kind"] = _lib.OP_RPROBE_DIAG if reg else _lib.OP_PROBE_DIAG
                         r["bits"][: len(op.bits)] = [code(b) for b in op.bits]
                         data = np.diagonal(op.M[0]).copy()
-                        layout.append(("probe_diag", op.recipe, off, (len(op.bits),)))
+                        layout.append(("probe_diag", op.recipe, off, (len(op.bits),), None))
                     else:
-                        r["kind"] = _lib.OP_PROBE
-                        r["bits"][: len(op.bits)] = [tile_of[b] for b in op.bits]
-                        data = op.M[0].reshape(-1)
-                        layout.append(("probe", op.recipe, off, (len(op.bits),)))
+                        bits = list(op.bits)
+                        M0 = op.M[0]
+                        if reg:
+                            order = sorted(range(len(bits)), key=lambda j: rb_cur.index(bits[j]))
+                            if order != list(range(len(bits))):
+                                perm = _bit_perm_index(order)
+                                M0 = M0[perm[:, None], perm[None, :]]
+                            bits = [bits[o] for o in order]
+                        r["kind"] = _lib.OP_RPROBE if reg else _lib.OP_PROBE
+                        r["bits"][: len(bits)] = [tile_of[b] for b in bits]
+                        data = M0.reshape(-1)
+                        layout.append(("probe", op.recipe, off, (len(op.bits),), perm))
                 else:
-                    r["kind"] = _lib.OP_DIAG
+                    r["kind"] = _lib.OP_RDIAG if reg else _lib.OP_DIAG
                     r["k"] = len(op.bits)
                     r["bits"][: len(op.bits)] = [code(b) for b in op.bits]
                     data = op.d[0]
-                    layout.append(("diag", op.recipe, off, (len(op.bits),)))
+                    layout.append(("diag", op.recipe, off, (len(op.bits),), None))
                 r["mat"] = off
-                chunks.append(data.astype(np.complex64))
+                chunks.append(np.asarray(data).astype(np.complex64))
                 off += len(data)
                 if off & 1:
                     chunks.append(np.zeros(1, np.complex64))
                     off += 1
-                oi += 1
         pool = np.concatenate(chunks) if chunks else np.zeros(2, np.complex64)
         return Plan(
             nbits=nbits,
@@ -554,6 +644,19 @@ class Planner:
             layout=layout,
             pool_len=max(off, 2),
         )
+
+
+def _bit_perm_index(order) -> np.ndarray:
+    """Index map for reordering matrix-index bits: new bit q = old bit order[q]."""
+    k = len(order)
+    idx = np.zeros(2**k, dtype=np.int64)
+    for i2 in range(2**k):
+        i = 0
+        for q in range(k):
+            if (i2 >> q) & 1:
+                i |= 1 << order[q]
+        idx[i2] = i
+    return idx
 
 
 def _diag_to_dense_matrix(d: np.ndarray, bits, tg, sl) -> np.ndarray:

@@ -56,6 +56,19 @@ typedef struct gbq_ctx gbq_ctx;
 #define GBQ_OP_DIAG 1       /* 2^k-entry diagonal on k bit codes               */
 #define GBQ_OP_PROBE 2      /* two-state passes: Re<lam|D|psi> on k tile bits  */
 #define GBQ_OP_PROBE_DIAG 3 /* two-state passes: Re<lam|diag(d)|psi>, bit codes */
+/* Register phases.  A LAYOUT op makes bits[0..R-1] (R = L - 8) the
+ * "register bits" of the tile: every thread then holds the 2^R amplitudes
+ * that differ only in those bits in registers, and the R* ops that follow
+ * act on registers without shared-memory traffic or barriers, until the
+ * next LAYOUT or a plain (shared-memory) op.  R* ops compute exactly what
+ * their plain counterparts compute; their extra constraints: RDENSE/RPROBE
+ * targets are register bits listed in ascending register position (bits[j]
+ * is register bit number <= bits[j+1]'s), selectors are not register bits. */
+#define GBQ_OP_LAYOUT 4
+#define GBQ_OP_RDENSE 5
+#define GBQ_OP_RDIAG 6
+#define GBQ_OP_RPROBE 7
+#define GBQ_OP_RPROBE_DIAG 8
 
 #define GBQ_MAX_OPS_PER_PASS 64
 #define GBQ_MAX_TILE_BITS 13

@@ -25,7 +25,11 @@ def run_program(state, nbits, passes, ops, pool):
             op = ops[o]
             k = int(op["k"])
             base = int(op["mat"])
-            if op["kind"] == 0:  # dense
+            kind = int(op["kind"])
+            if kind == 4:  # layout: changes where amplitudes live, not their values
+                continue
+            kind = {5: 0, 6: 1}.get(kind, kind)  # register ops compute what plain ops do
+            if kind == 0:  # dense
                 tg = [tile_to_global[int(b)] for b in op["bits"][:k]]
                 nsel = int(op["nsel"])
                 sg = [_global_bit(int(c), tile_to_global) for c in op["sel"][:nsel]]
@@ -47,7 +51,7 @@ def run_program(state, nbits, passes, ops, pool):
                             off |= 1 << b
                     out += mats[sel, sub, c] * psi[clear | off]
                 psi = out
-            elif op["kind"] == 1:  # diag
+            elif kind == 1:  # diag
                 bits = [_global_bit(int(c), tile_to_global) for c in op["bits"][:k]]
                 tab = pool[base : base + 2**k]
                 sub = np.zeros_like(idx)
