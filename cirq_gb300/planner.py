@@ -535,9 +535,17 @@ class Planner:
                 nsel = sels | set(local_sels(ops[j]))
                 if len(rb) + len(need) > R or any(b in nsel for b in rb + need):
                     break
+                # the layout must still be completable with non-selector bits
+                spare = len(tile - nsel - set(rb) - set(need))
+                if spare < R - len(rb) - len(need):
+                    break
                 rb += need
                 sels = nsel
                 j += 1
+            if j == i:  # cannot open a phase for this op: run it from shared memory
+                items.append(("op", ops[i], False))
+                i += 1
+                continue
             free = [b for b in sorted(tile, reverse=True) if b not in rb and b not in sels]
             rb += free[: R - len(rb)]
             items.append(("layout", rb))

@@ -94,3 +94,31 @@ def test_unsupported_operations_raise():
     with pytest.raises(NotImplementedError):
         CompiledCircuit([cirq.MatrixGate(np.eye(3), qid_shape=(3,)).on(qt[0])], qt, dm=False,
                         planner=Planner(), resolvers=[cirq.ParamResolver({})])
+
+
+def test_register_layouts_are_complete():
+    """Every LAYOUT op names exactly L - 8 distinct register bits, none of which
+    is a selector of a register op in its phase (the engine rejects others)."""
+    from cirq_gb300 import adjoint
+
+    circuit, symbols, values = workloads.hea_circuit(12, 3, seed=12)
+    ham = workloads.random_pauli_hamiltonian(12, 30, seed=13)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    c2 = workloads.random_layer_circuit(16, 12, seed=1)
+    cc = CompiledCircuit(split_measurements(c2)[0], sorted(c2.all_qubits()), dm=False,
+                         planner=Planner(tile_bits=12), resolvers=[cirq.ParamResolver({})])
+    for plan in (prog.forward.plan, prog.reverse, cc.plan):
+        for p in plan.passes:
+            L = int(p["L"])
+            regs = None
+            for o in plan.ops[p["op_begin"] : p["op_begin"] + p["op_count"]]:
+                if o["kind"] == 4:
+                    regs = [int(b) for b in o["bits"][: int(o["k"])]]
+                    assert len(regs) == L - 8 and len(set(regs)) == L - 8
+                elif o["kind"] in (5, 7):
+                    pos = [regs.index(int(b)) for b in o["bits"][: int(o["k"])]]
+                    assert pos == sorted(pos)
+                    for c in o["sel"][: int(o["nsel"])]:
+                        assert int(c) not in regs
+                elif o["kind"] in (0, 1, 2, 3):
+                    regs = None
