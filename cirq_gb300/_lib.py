@@ -173,6 +173,7 @@ SIGNATURES = {
     "gbq_h2d": [_P, _P, _P, _SZ],
     "gbq_d2h": [_P, _P, _P, _SZ],
     "gbq_sv_set_basis": [_P, _P, _I, _U64],
+    "gbq_validate_program": [_I, _P, _I, _P, _I, _I],
     "gbq_run": [_P, _P, _I, _P, _I, _P, _I, _P],
     "gbq_run_dual": [_P, _P, _P, _I, _P, _I, _P, _I, _P, _P],
     "gbq_reduce_slots": [_P, _P, _I, _I64, _P],
@@ -239,6 +240,17 @@ def check(rc: int, what: str = "") -> None:
     if rc == ERR_UNSUPPORTED:
         raise NotImplementedError(f"{what}: {msg}" if what else msg)
     raise GpuError(f"{what}: {msg}" if what else msg)
+
+
+def validate_program(plan, dual: bool = False) -> None:
+    """Runs the engine's host-side program checks (no GPU needed); raises on error."""
+    lib = load()
+    check(
+        lib.gbq_validate_program(
+            plan.nbits, plan.passes.ctypes.data, len(plan.passes), plan.ops.ctypes.data, len(plan.ops), int(dual)
+        ),
+        "gbq_validate_program",
+    )
 
 
 def ptr(a: np.ndarray | None) -> int | None:

@@ -596,6 +596,23 @@ int gbq_sv_set_basis(gbq_ctx* c, gbq_c64* state, int nbits, uint64_t index) {
   return do_set_basis(c, reinterpret_cast<float2*>(state), nbits, index);
 }
 
+int gbq_validate_program(int nbits, const gbq_pass* passes, int npasses, const gbq_op* ops,
+                         int nops, int dual) {
+  if (nbits < 1 || nbits > 40) return arg_fail("gbq_validate_program: bad width");
+  if (npasses < 0 || (npasses && (!passes || !ops))) return arg_fail("gbq_validate_program: null program");
+  PassArgs* a = new PassArgs();
+  int rc = GBQ_OK;
+  for (int q = 0; q < npasses && rc == GBQ_OK; ++q) {
+    uint64_t inmask = 0;
+    rc = pass_geometry(passes[q], nops, nbits, a->ti, inmask);
+    LayoutState lay;
+    for (int o = 0; rc == GBQ_OK && o < passes[q].op_count; ++o)
+      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual != 0, a->ops[o], lay);
+  }
+  delete a;
+  return rc;
+}
+
 int gbq_run(gbq_ctx* c, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
             const gbq_op* ops, int nops, const gbq_c64* mats) {
   CHECK_CTX(c);

@@ -37,7 +37,7 @@ import numpy as np
 from cirq_gb300 import _lib
 from cirq_gb300.ir import BitGate
 
-MAX_OPS = 64
+MAX_OPS = 32  # fused ops per pass; register layouts at most double the engine's count (<= 64)
 MAX_DIAG_BITS = 8
 MAX_SEL = 3
 MIN_TILE_BITS = 10  # the engine's narrowest tile; narrower registers are padded

@@ -156,6 +156,11 @@ int gbq_sv_set_basis(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t index);
 int gbq_run(gbq_ctx* ctx, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
             const gbq_op* ops, int nops, const gbq_c64* mats);
 
+/* Checks a program against a state of nbits bits exactly as gbq_run /
+ * gbq_run_dual (dual != 0) do before launching, without touching a GPU. */
+int gbq_validate_program(int nbits, const gbq_pass* passes, int npasses, const gbq_op* ops,
+                         int nops, int dual);
+
 /* Two-state reverse sweep for adjoint differentiation (no reference
  * counterpart: the reference has no gradient code).  Dense/diag ops are
  * applied to both psi and lam; probe ops add Re<lam|D|psi> of each tile to

@@ -24,6 +24,9 @@ PLANNERS = [
 
 
 def _emulate(compiled, resolver=None, initial=0):
+    from cirq_gb300 import _lib
+
+    _lib.validate_program(compiled.plan)  # the engine's own pre-launch checks
     nb = compiled.nbits_dev
     psi = np.zeros(2**nb, complex)
     psi[initial] = 1
@@ -107,7 +110,11 @@ def test_register_layouts_are_complete():
     c2 = workloads.random_layer_circuit(16, 12, seed=1)
     cc = CompiledCircuit(split_measurements(c2)[0], sorted(c2.all_qubits()), dm=False,
                          planner=Planner(tile_bits=12), resolvers=[cirq.ParamResolver({})])
+    from cirq_gb300 import _lib
+
+    _lib.validate_program(prog.reverse, dual=True)
     for plan in (prog.forward.plan, prog.reverse, cc.plan):
+        _lib.validate_program(plan, dual=plan is prog.reverse)
         for p in plan.passes:
             L = int(p["L"])
             regs = None
