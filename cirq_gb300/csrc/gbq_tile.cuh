@@ -660,8 +660,11 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
   }
 }
 
-// Two shared buffers per state: tile i is processed in one while tile i+1
-// streams into the other (cp.async groups, waited with wait_group 1).
+// Three shared buffers per state: tile i is processed in one while tiles
+// i+1 and i+2 stream into the others (cp.async groups, wait_group 2), so the
+// memory system stays busy while the CTA computes.
+constexpr int kStages = 3;
+
 template <int LT, int KMAX, bool DUAL>
 __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
   extern __shared__ float4 smraw[];
@@ -670,7 +673,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   __shared__ uint64_t slo[1 << (LT - 8)];
   __shared__ double red[kThreads / 32];
   constexpr int TS = 1 << LT;
-  float2* buf = reinterpret_cast<float2*>(smraw);  // [2][DUAL ? 2 : 1][TS]
+  constexpr int NS = DUAL ? 2 : 1;
+  float2* buf = reinterpret_cast<float2*>(smraw);  // [kStages][NS][TS]
   {
     const int nwords = a.ti.nops * (int)(sizeof(OpDev) / 4);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.ops);
@@ -679,25 +683,31 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   }
   const TileSetup ts = tile_setup<LT>(a.ti, soff, slo);
   __syncthreads();
-  constexpr int NS = DUAL ? 2 : 1;
-  int64_t tile = blockIdx.x;
-  if (tile < a.ti.ntiles) {
-    const uint64_t gb = tile_base(a.ti, tile);
-    load_tile_async<LT>(a.psi, buf, gb, ts.lo_t, ts.lp_t, slo);
-    if constexpr (DUAL) load_tile_async<LT>(a.lam, buf + TS, gb, ts.lo_t, ts.lp_t, slo);
+  const int64_t step = gridDim.x;
+  // prologue: the first kStages - 1 tiles
+#pragma unroll
+  for (int s = 0; s < kStages - 1; ++s) {
+    const int64_t tl = blockIdx.x + s * step;
+    if (tl < a.ti.ntiles) {
+      const uint64_t gb = tile_base(a.ti, tl);
+      float2* b = buf + s * NS * TS;
+      load_tile_async<LT>(a.psi, b, gb, ts.lo_t, ts.lp_t, slo);
+      if constexpr (DUAL) load_tile_async<LT>(a.lam, b + TS, gb, ts.lo_t, ts.lp_t, slo);
+    }
+    cp_async_commit();
   }
-  cp_async_commit();
   int cur = 0;
-  for (; tile < a.ti.ntiles; tile += gridDim.x) {
-    const int64_t next = tile + gridDim.x;
-    float2* nb = buf + (cur ^ 1) * NS * TS;
-    if (next < a.ti.ntiles) {
-      const uint64_t gn = tile_base(a.ti, next);
+  for (int64_t tile = blockIdx.x; tile < a.ti.ntiles; tile += step) {
+    const int64_t ahead = tile + (kStages - 1) * step;
+    const int slot_ahead = (cur + kStages - 1) % kStages;
+    if (ahead < a.ti.ntiles) {
+      const uint64_t gn = tile_base(a.ti, ahead);
+      float2* nb = buf + slot_ahead * NS * TS;
       load_tile_async<LT>(a.psi, nb, gn, ts.lo_t, ts.lp_t, slo);
       if constexpr (DUAL) load_tile_async<LT>(a.lam, nb + TS, gn, ts.lo_t, ts.lp_t, slo);
     }
     cp_async_commit();
-    cp_async_wait<1>();
+    cp_async_wait<kStages - 1>();
     __syncthreads();
     float2* smA = buf + cur * NS * TS;
     float2* smB = smA + TS;
@@ -706,14 +716,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
     store_tile<LT>(a.psi, smA, gbase, ts.off_t, ts.ph_t, soff);
     if constexpr (DUAL) store_tile<LT>(a.lam, smB, gbase, ts.off_t, ts.ph_t, soff);
     __syncthreads();
-    cur ^= 1;
+    cur = (cur + 1) % kStages;
   }
   cp_async_wait<0>();
 }
 
 template <int LT, int KMAX, bool DUAL>
 int launch_tile_pass(Ctx* c, const PassArgs& a) {
-  const int smem = 2 * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
+  const int smem = kStages * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
   static int blocks_per_sm = -1;
   cudaError_t e;
   if (blocks_per_sm < 0) {
