@@ -27,6 +27,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 
 #include "gbq_internal.cuh"
 
@@ -660,13 +662,12 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
   }
 }
 
-// Three shared buffers per state: tile i is processed in one while tiles
-// i+1 and i+2 stream into the others (cp.async groups, wait_group 2), so the
-// memory system stays busy while the CTA computes.
-constexpr int kStages = 3;
-
-template <int LT, int KMAX, bool DUAL>
+// STAGES shared buffers per state: tile i is processed in one while the next
+// STAGES - 1 tiles stream into the others (cp.async groups), so the memory
+// system stays busy while the CTA computes.
+template <int LT, int KMAX, bool DUAL, int STAGES>
 __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
+  constexpr int kStages = STAGES;
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t soff[1 << (LT - 9)];
@@ -721,27 +722,47 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   cp_async_wait<0>();
 }
 
-template <int LT, int KMAX, bool DUAL>
-int launch_tile_pass(Ctx* c, const PassArgs& a) {
-  const int smem = kStages * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
+template <int LT, int KMAX, bool DUAL, int STAGES>
+int launch_tile_pass_stages(Ctx* c, const PassArgs& a) {
+  const int smem = STAGES * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
   static int blocks_per_sm = -1;
   cudaError_t e;
   if (blocks_per_sm < 0) {
-    e = cudaFuncSetAttribute(k_tile_pass<LT, KMAX, DUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
+    e = cudaFuncSetAttribute(k_tile_pass<LT, KMAX, DUAL, STAGES>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_tile_pass)");
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_pass<LT, KMAX, DUAL>, kThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_pass<LT, KMAX, DUAL, STAGES>,
+                                                      kThreads, smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     blocks_per_sm = nb > 0 ? nb : 1;
+    if (getenv("GBQ_DEBUG"))
+      fprintf(stderr, "k_tile_pass<L=%d,K=%d,dual=%d,stages=%d>: %d blocks/SM, %d B smem\n", LT, KMAX,
+              (int)DUAL, STAGES, blocks_per_sm, smem);
   }
   int64_t grid = (int64_t)c->sm_count * blocks_per_sm;
   if (grid > a.ti.ntiles) grid = a.ti.ntiles;
-  k_tile_pass<LT, KMAX, DUAL><<<(unsigned)grid, kThreads, smem, c->stream>>>(a);
+  k_tile_pass<LT, KMAX, DUAL, STAGES><<<(unsigned)grid, kThreads, smem, c->stream>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_tile_pass launch");
   c->launches += 1;
   return GBQ_OK;
+}
+
+// Pipeline depth: 2 by default; GBQ_STAGES=3 selects three buffers.
+inline int pipeline_stages() {
+  static int st = -1;
+  if (st < 0) {
+    const char* e = getenv("GBQ_STAGES");
+    st = (e && atoi(e) == 3) ? 3 : 2;
+  }
+  return st;
+}
+
+template <int LT, int KMAX, bool DUAL>
+int launch_tile_pass(Ctx* c, const PassArgs& a) {
+  if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3>(c, a);
+  return launch_tile_pass_stages<LT, KMAX, DUAL, 2>(c, a);
 }
 
 // Widest shared-memory dense (or dense-probe) op of a pass (0 if none).
