@@ -25,8 +25,6 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ double red[kThreads / 32];
   __shared__ TileInfo ti;
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
-  __shared__ uint64_t soff[1 << (LT - 9)];
-  __shared__ uint64_t slo[1 << (LT - 8)];
   __shared__ int s_point;
   constexpr int TS = 1 << LT;
   float2* buf = reinterpret_cast<float2*>(smraw);  // [2][TS]
@@ -68,22 +66,22 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
       }
       __syncthreads();
-      const TileSetup ts = tile_setup<LT>(ti, soff, slo);
+      const TileSetup ts = tile_setup<LT>(ti);
       __syncthreads();
       // every global write of the previous pass is visible here: the whole
       // pass ran in this CTA and ended with __syncthreads()
-      load_tile_async<LT>(psi, buf, tile_base(ti, 0), ts.lo_t, ts.lp_t, slo);
+      load_tile_async<LT>(ti, psi, buf, tile_base(ti, 0), ts.lo_t, ts.lp_t);
       cp_async_commit();
       int cur = 0;
       for (int64_t tile = 0; tile < ti.ntiles; ++tile) {
         if (tile + 1 < ti.ntiles)
-          load_tile_async<LT>(psi, buf + (cur ^ 1) * TS, tile_base(ti, tile + 1), ts.lo_t, ts.lp_t, slo);
+          load_tile_async<LT>(ti, psi, buf + (cur ^ 1) * TS, tile_base(ti, tile + 1), ts.lo_t, ts.lp_t);
         cp_async_commit();
         cp_async_wait<1>();
         __syncthreads();
         const uint64_t gbase = tile_base(ti, tile);
         run_ops<LT, 5, false>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
-        store_tile<LT>(psi, buf + cur * TS, gbase, ts.off_t, ts.ph_t, soff);
+        store_tile<LT>(ti, psi, buf + cur * TS, gbase, ts.off_t, ts.ph_t);
         __syncthreads();
         cur ^= 1;
       }

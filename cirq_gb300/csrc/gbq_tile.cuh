@@ -87,6 +87,20 @@ __device__ __forceinline__ uint64_t tile_base(const TileInfo& ti, int64_t tile) 
   return g;
 }
 
+// Base index of a tile from three 256-entry tables (tile-number bits 0-7,
+// 8-15, 16-23 deposited at the out-of-tile global bits), built once per
+// launch; tile numbers need at most 24 bits (states of <= 37 bits).
+constexpr int kTileTab = 256;
+__device__ __forceinline__ void tile_tables_build(const TileInfo& ti, uint64_t* tab) {
+  for (int e = threadIdx.x; e < 3 * kTileTab; e += kThreads) {
+    const int part = e / kTileTab;
+    tab[e] = tile_base(ti, (int64_t)(e % kTileTab) << (8 * part));
+  }
+}
+__device__ __forceinline__ uint64_t tile_base_fast(const uint64_t* tab, int64_t tile) {
+  return tab[tile & 255] | tab[kTileTab + ((tile >> 8) & 255)] | tab[2 * kTileTab + ((tile >> 16) & 255)];
+}
+
 // ---- dense k-bit op (and dense probe) ---------------------------------------------
 template <int K, int LT, bool DUAL, bool PROBE>
 __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, float2* smA,
@@ -338,28 +352,40 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// global offset of the tile-index bits >= `lo` of the compile-time value x
 template <int LT>
-__device__ __forceinline__ void load_tile_async(const float2* __restrict__ src, float2* sm,
-                                                uint64_t gbase, uint64_t lo_t, uint32_t lp_t,
-                                                const uint64_t* slo) {
+__device__ __forceinline__ uint64_t hi_part(const TileInfo& ti, uint32_t x) {
+  uint64_t r = 0;
+#pragma unroll
+  for (int b = 8; b < LT; ++b)
+    if ((x >> b) & 1u) r |= ti.gw[b];
+  return r;
+}
+
+template <int LT>
+__device__ __forceinline__ void load_tile_async(const TileInfo& ti, const float2* __restrict__ src,
+                                                float2* sm, uint64_t gbase, uint64_t lo_t,
+                                                uint32_t lp_t) {
   constexpr int NA = 1 << (LT - 8);  // amplitudes per thread
+  const float2* g = src + (gbase | lo_t);
 #pragma unroll
   for (int j = 0; j < NA; ++j) {
-    const uint64_t off = gbase | lo_t | slo[j];
-    cp_async8(sm + (lp_t ^ phys_const((uint32_t)j * kThreads)), src + off);
+    cp_async8(sm + (lp_t ^ phys_const((uint32_t)j * kThreads)), g + hi_part<LT>(ti, (uint32_t)j * kThreads));
   }
 }
 
 template <int LT>
-__device__ __forceinline__ void store_tile(float2* __restrict__ dst, const float2* sm, uint64_t gbase,
-                                           uint64_t off_t, uint32_t ph_t, const uint64_t* soff) {
+__device__ __forceinline__ void store_tile(const TileInfo& ti, float2* __restrict__ dst,
+                                           const float2* sm, uint64_t gbase, uint64_t off_t,
+                                           uint32_t ph_t) {
   constexpr int NJ = 1 << (LT - 9);
+  float2* g = dst + (gbase | off_t);
 #pragma unroll
   for (int j = 0; j < NJ; ++j) {
-    const uint64_t off = gbase | off_t | soff[j];
     const uint32_t p = ph_t ^ phys_const((uint32_t)j * (2 * kThreads));
     const float2 x = sm[p], y = sm[p ^ 1u];
-    __stcs(reinterpret_cast<float4*>(dst + off), make_float4(x.x, x.y, y.x, y.y));
+    __stcs(reinterpret_cast<float4*>(g + hi_part<LT>(ti, (uint32_t)j * (2 * kThreads))),
+           make_float4(x.x, x.y, y.x, y.y));
   }
 }
 
@@ -375,11 +401,7 @@ struct TileSetup {
 };
 
 template <int LT>
-__device__ __forceinline__ TileSetup tile_setup(const TileInfo& ti, uint64_t* soff, uint64_t* slo) {
-  constexpr int NJ = 1 << (LT - 9);
-  constexpr int NA = 1 << (LT - 8);
-  if (threadIdx.x < NJ) soff[threadIdx.x] = lin_off<LT>(ti, (uint32_t)threadIdx.x * (2 * kThreads));
-  if (threadIdx.x < NA) slo[threadIdx.x] = lin_off<LT>(ti, (uint32_t)threadIdx.x * kThreads);
+__device__ __forceinline__ TileSetup tile_setup(const TileInfo& ti) {
   TileSetup s;
   s.off_t = lin_off<LT>(ti, (uint32_t)threadIdx.x << 1);
   s.ph_t = phys_dev((uint32_t)threadIdx.x << 1);
@@ -670,8 +692,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   constexpr int kStages = STAGES;
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
-  __shared__ uint64_t soff[1 << (LT - 9)];
-  __shared__ uint64_t slo[1 << (LT - 8)];
+  __shared__ uint64_t ttab[3 * kTileTab];
   __shared__ double red[kThreads / 32];
   constexpr int TS = 1 << LT;
   constexpr int NS = DUAL ? 2 : 1;
@@ -682,7 +703,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
     uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
     for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
   }
-  const TileSetup ts = tile_setup<LT>(a.ti, soff, slo);
+  tile_tables_build(a.ti, ttab);
+  const TileSetup ts = tile_setup<LT>(a.ti);
   __syncthreads();
   const int64_t step = gridDim.x;
   // prologue: the first kStages - 1 tiles
@@ -690,10 +712,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   for (int s = 0; s < kStages - 1; ++s) {
     const int64_t tl = blockIdx.x + s * step;
     if (tl < a.ti.ntiles) {
-      const uint64_t gb = tile_base(a.ti, tl);
+      const uint64_t gb = tile_base_fast(ttab, tl);
       float2* b = buf + s * NS * TS;
-      load_tile_async<LT>(a.psi, b, gb, ts.lo_t, ts.lp_t, slo);
-      if constexpr (DUAL) load_tile_async<LT>(a.lam, b + TS, gb, ts.lo_t, ts.lp_t, slo);
+      load_tile_async<LT>(a.ti, a.psi, b, gb, ts.lo_t, ts.lp_t);
+      if constexpr (DUAL) load_tile_async<LT>(a.ti, a.lam, b + TS, gb, ts.lo_t, ts.lp_t);
     }
     cp_async_commit();
   }
@@ -702,20 +724,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
     const int64_t ahead = tile + (kStages - 1) * step;
     const int slot_ahead = (cur + kStages - 1) % kStages;
     if (ahead < a.ti.ntiles) {
-      const uint64_t gn = tile_base(a.ti, ahead);
+      const uint64_t gn = tile_base_fast(ttab, ahead);
       float2* nb = buf + slot_ahead * NS * TS;
-      load_tile_async<LT>(a.psi, nb, gn, ts.lo_t, ts.lp_t, slo);
-      if constexpr (DUAL) load_tile_async<LT>(a.lam, nb + TS, gn, ts.lo_t, ts.lp_t, slo);
+      load_tile_async<LT>(a.ti, a.psi, nb, gn, ts.lo_t, ts.lp_t);
+      if constexpr (DUAL) load_tile_async<LT>(a.ti, a.lam, nb + TS, gn, ts.lo_t, ts.lp_t);
     }
     cp_async_commit();
     cp_async_wait<kStages - 1>();
     __syncthreads();
     float2* smA = buf + cur * NS * TS;
     float2* smB = smA + TS;
-    const uint64_t gbase = tile_base(a.ti, tile);
+    const uint64_t gbase = tile_base_fast(ttab, tile);
     run_ops<LT, KMAX, DUAL>(a.ti, sops, smA, smB, gbase, tile, red);
-    store_tile<LT>(a.psi, smA, gbase, ts.off_t, ts.ph_t, soff);
-    if constexpr (DUAL) store_tile<LT>(a.lam, smB, gbase, ts.off_t, ts.ph_t, soff);
+    store_tile<LT>(a.ti, a.psi, smA, gbase, ts.off_t, ts.ph_t);
+    if constexpr (DUAL) store_tile<LT>(a.ti, a.lam, smB, gbase, ts.off_t, ts.ph_t);
     __syncthreads();
     cur = (cur + 1) % kStages;
   }

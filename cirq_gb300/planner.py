@@ -252,7 +252,7 @@ class Planner:
         low_bits: int = 5,
         kmax: int = 4,
         budget: float = 40.0,
-        op_overhead: float = 1.0,
+        op_overhead: float = 2.0,
         use_registers: bool = True,
     ):
         if not 1 <= kmax <= 5:
@@ -339,18 +339,27 @@ class Planner:
         c = max((last.get(b, -1) for b in bits), default=-1)
         new_cost = (2 ** len(bits) if not g.diagonal else 1) + self.ovh
         if not g.diagonal:
+            # g commutes with every op after c (none of them touches its
+            # bits), so any later dense op may absorb it; take the cheapest
+            best = None
+            for d in range(max(c, 0), len(ops)):
+                op = ops[d]
+                if op.kind != "dense":
+                    continue
+                tg = list(op.tg)
+                for b in bits:
+                    if b not in tg:
+                        tg.append(b)
+                if len(tg) > self.kmax:
+                    continue
+                delta = 2 ** len(tg) - 2 ** len(op.tg)
+                if best is None or delta < best[0] or (delta == best[0] and d > best[2]):
+                    best = (delta, "merge_dense", d)
+            if best is not None and best[0] < new_cost:
+                return best
             if c >= 0 and ops[c].kind != "probe":
                 op = ops[c]
-                if op.kind == "dense":
-                    tg = list(op.tg)
-                    for b in bits:
-                        if b not in tg:
-                            tg.append(b)
-                    if len(tg) <= self.kmax:
-                        delta = 2 ** len(tg) - 2 ** len(op.tg)
-                        if delta < new_cost:
-                            return (delta, "merge_dense", c)
-                elif op.kind == "diag":
+                if op.kind == "diag":
                     loc = [b for b in op.bits if b in S]
                     glob = [b for b in op.bits if b not in S]
                     tg = list(loc)
@@ -490,16 +499,29 @@ class Planner:
 
     # ---- register phases ---------------------------------------------------------
     def _phases(self, pp: PassPlan) -> list:
-        """Splits a pass's ops into register phases.
+        """Orders a pass's ops into register phases.
 
-        Returns a list of items ("layout", [register bits]) or ("op", op, reg)
-        where reg tells whether the op runs on registers.  A phase is a run of
-        consecutive ops whose dense targets fit R = L - 8 register bits and
-        whose selector bits stay out of them; diagonal ops join any phase."""
+        Returns items ("layout", [register bits]) or ("op", op, on_registers).
+        Ops that commute may be reordered: an op is *ready* when no earlier,
+        not yet emitted op conflicts with it (one of the two acts
+        non-diagonally on a bit the other touches).  A phase repeatedly takes
+        every ready op whose targets fit R = L - 8 register bits (growing the
+        set as needed) and whose selector bits stay out of it; diagonal ops
+        fit any phase.  Ops that cannot run on registers run from shared
+        memory between phases."""
         R = pp.L - 8 if (self.use_registers and pp.L <= 12) else 0
         tile = set(range(pp.m)) | set(pp.hi)
-        ops = pp.ops
-        items = []
+        ops = list(pp.ops)
+
+        def writes(op):
+            if op.kind == "dense":
+                return set(op.tg)
+            if op.kind == "probe" and not op.diagonal:
+                return set(op.bits)
+            return set()
+
+        def touches(op):
+            return set(op.touches())
 
         def targets(op):
             if op.kind == "dense":
@@ -508,7 +530,7 @@ class Planner:
                 return list(op.bits)
             return []
 
-        def eligible(op):
+        def reg_ok(op):
             if op.kind == "dense":
                 return len(op.tg) <= min(R, 4)
             if op.kind == "probe" and not op.diagonal:
@@ -516,42 +538,64 @@ class Planner:
             return R > 0
 
         def local_sels(op):
-            return [b for b in getattr(op, "sl", []) if b in tile]
+            return {b for b in getattr(op, "sl", []) if b in tile}
 
-        i = 0
-        while i < len(ops):
-            if not R or not eligible(ops[i]) or not targets(ops[i]):
-                if R and eligible(ops[i]) and items and items[-1][0] == "op" and items[-1][2]:
-                    items.append(("op", ops[i], True))  # diagonal op inside the open phase
-                else:
-                    items.append(("op", ops[i], False))
-                i += 1
+        def conflicts(a, b):
+            return bool(writes(a) & touches(b)) or bool(writes(b) & touches(a))
+
+        items: list = []
+        remaining = list(range(len(ops)))
+
+        def ready(i, done_set):
+            for j in remaining:
+                if j >= i:
+                    break
+                if j not in done_set and conflicts(ops[j], ops[i]):
+                    return False
+            return True
+
+        while remaining:
+            first = remaining[0]
+            if not R or not reg_ok(ops[first]) or (not targets(ops[first]) and not any(
+                    targets(ops[j]) for j in remaining)):
+                # shared-memory op (or a phase would hold no dense op)
+                items.append(("op", ops[first], False))
+                remaining.pop(0)
                 continue
             rb: list = []
             sels: set = set()
-            j = i
-            while j < len(ops) and eligible(ops[j]):
-                need = [b for b in targets(ops[j]) if b not in rb]
-                nsel = sels | set(local_sels(ops[j]))
-                if len(rb) + len(need) > R or any(b in nsel for b in rb + need):
-                    break
-                # the layout must still be completable with non-selector bits
-                spare = len(tile - nsel - set(rb) - set(need))
-                if spare < R - len(rb) - len(need):
-                    break
-                rb += need
-                sels = nsel
-                j += 1
-            if j == i:  # cannot open a phase for this op: run it from shared memory
-                items.append(("op", ops[i], False))
-                i += 1
+            phase: list = []
+            taken: set = set()
+            progress = True
+            while progress:
+                progress = False
+                for i in list(remaining):
+                    if i in taken or not reg_ok(ops[i]) or not ready(i, taken):
+                        continue
+                    need = [b for b in targets(ops[i]) if b not in rb]
+                    nsel = sels | local_sels(ops[i])
+                    if len(rb) + len(need) > R or any(b in nsel for b in rb + need):
+                        continue
+                    if len(tile - nsel - set(rb) - set(need)) < R - len(rb) - len(need):
+                        continue
+                    rb += need
+                    sels = nsel
+                    phase.append(i)
+                    taken.add(i)
+                    progress = True
+            if not phase or not any(targets(ops[i]) for i in phase):
+                # nothing dense fits a fresh phase: run the first op from shared memory
+                if phase and not any(targets(ops[i]) for i in phase):
+                    pass
+                items.append(("op", ops[first], False))
+                remaining.pop(0)
                 continue
             free = [b for b in sorted(tile, reverse=True) if b not in rb and b not in sels]
             rb += free[: R - len(rb)]
             items.append(("layout", rb))
-            for o in ops[i:j]:
-                items.append(("op", o, True))
-            i = j
+            for i in sorted(phase):
+                items.append(("op", ops[i], True))
+            remaining = [i for i in remaining if i not in taken]
         return items
 
     # ---- emission -----------------------------------------------------------
