@@ -310,7 +310,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tile-bits", type=int, default=12)
     ap.add_argument("--kmax", type=int, default=4)
-    ap.add_argument("--budget", type=float, default=40.0)
+    ap.add_argument("--budget", type=float, default=25.0)
     ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")

@@ -86,7 +86,7 @@ class _GpuSimulatorBase:
         device: int | None = None,
         fusion_max_qubits: int = 4,
         tile_bits: int = 12,
-        pass_budget: float = 40.0,
+        pass_budget: float = 25.0,
     ):
         _check_dtype(dtype)
         self._dtype = np.complex64
