@@ -206,6 +206,25 @@ int gbq_probabilities(gbq_ctx* ctx, const gbq_c64* state, int nbits, int dm, flo
  * PauliSum.expectation_from_state_vector (cirq-core/cirq/ops/linear_combinations.py:659-718). */
 int gbq_sv_expect_paulis(gbq_ctx* ctx, const gbq_c64* state, int nbits, const gbq_pauli* terms,
                          int nterms, double* out);
+/* Same values as gbq_sv_expect_paulis, for callers that cannot allocate
+ * device memory (no counterpart in the reference: Cirq's simulators run in
+ * host memory).  Such callers include code running while a stream is being
+ * captured into a CUDA graph, services whose device memory belongs to a host
+ * framework's pool, and loops that cannot afford cudaMalloc's implicit
+ * device synchronisation.  This entry point allocates nothing: its scratch
+ * is a fixed GBQ_NOALLOC_SCRATCH_BYTES array in the library's device image,
+ * present on every GPU that loads the library until the process exits, and
+ * found with cudaGetSymbolAddress the first time it is called on a device --
+ * make that first call before any stream capture.  `state` is a device
+ * array, `terms` and `out` are host arrays (2 doubles per term, as for
+ * gbq_sv_expect_paulis); work is ordered on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns after it finished.  Term lists
+ * too long for the scratch (about 1000 terms) are rejected with GBQ_ERR_ARG.
+ * All calls share the scratch: calls that overlap on the GPU race and must
+ * be serialised by the caller. */
+#define GBQ_NOALLOC_SCRATCH_BYTES (4u << 20)
+int gbq_sv_expect_paulis_noalloc(void* stream, const gbq_c64* state, int nbits,
+                                 const gbq_pauli* terms, int nterms, double* out);
 /* Density-matrix counterpart: coef_t Tr(P_t rho) for rho of nbits qubits
  * (cirq-core/cirq/ops/pauli_string.py:734-760). */
 int gbq_dm_expect_paulis(gbq_ctx* ctx, const gbq_c64* rho, int nbits, const gbq_pauli* terms,
