@@ -299,6 +299,97 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# secondary workloads (reported beside the headline number)
+def adjoint_bench(n: int = 24, layers: int = 10, terms: int = 300, reps: int = 3, ps_params: int = 16):
+    """Gradient of <H> for the hardware-efficient ansatz (rx/rz layers + CZ
+    ladder, 480 parameters at 24 qubits, H = 300 random Pauli strings of
+    weight 2..4): adjoint gradients per second through AdjointProgram, and
+    parameter shift through the plain GPU simulator (simulate_expectation_values_sweep,
+    2 evaluations per parameter) timed on `ps_params` parameters and
+    extrapolated to all of them."""
+    import cirq_gb300
+    from cirq_gb300 import adjoint, workloads
+
+    circuit, symbols, values = workloads.hea_circuit(n, layers, seed=0)
+    ham = workloads.random_pauli_hamiltonian(n, terms, seed=1)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    prog.value_and_grad(values)  # warm-up
+    t = time.perf_counter()
+    for _ in range(reps):
+        e, g = prog.value_and_grad(values)
+    t_adj = (time.perf_counter() - t) / reps
+    sim = cirq_gb300.Simulator()
+    idx = list(range(ps_params))
+    adjoint.parameter_shift_gradient(sim, circuit, ham, symbols, values, indices=idx[:1])  # warm-up
+    t = time.perf_counter()
+    ps = adjoint.parameter_shift_gradient(sim, circuit, ham, symbols, values, indices=idx)
+    t_ps = (time.perf_counter() - t) * len(symbols) / len(idx)
+    return {
+        "workload": f"HEA {n}q x {layers} layers ({len(symbols)} params), H = {terms} Pauli strings",
+        "grads_per_s": 1.0 / t_adj,
+        "s_per_grad": t_adj,
+        "param_shift_s_per_grad": t_ps,
+        "param_shift_sample": f"{len(idx)} of {len(symbols)} parameters timed, extrapolated",
+        "speedup_vs_param_shift": t_ps / t_adj,
+        "max_abs_diff_vs_param_shift": float(np.max(np.abs(g[idx] - ps[idx]))),
+        "energy": e,
+    }
+
+
+def density_bench(n: int = 13, depth: int = 16):
+    """Noisy density matrix: random layers, depolarize(1e-3) after every gate
+    on each of its qubits, amplitude_damp(5e-3) on all qubits per layer;
+    rho = 2^26 complex64 (512 MiB)."""
+    import cirq_gb300
+    from cirq_gb300 import workloads
+
+    c = workloads.noisy_layer_circuit(n, depth, seed=0, p=1e-3, gamma=5e-3)
+    nops = len(list(c.all_operations()))
+    sim = cirq_gb300.DensityMatrixSimulator()
+    r = sim.simulate(c)
+    rho = r.final_density_matrix
+    t = time.perf_counter()
+    r = sim.simulate(c)
+    rho = r.final_density_matrix
+    dt = time.perf_counter() - t
+    compiled = next(iter(sim._cache.values()))
+    return {
+        "workload": f"noisy layers {n}q depth {depth} ({nops} ops incl. channels)",
+        "s_per_simulate": dt,
+        "ops_per_s": nops / dt,
+        "passes": int(compiled.plan.npasses),
+        "trace": float(np.real(np.trace(rho))),
+        "hermiticity_err": float(np.max(np.abs(rho - rho.conj().T))),
+    }
+
+
+def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
+    """QAOA p=4 on seeded random 3-regular graphs, <sum Z_i Z_j> for `points`
+    parameter points split evenly over the widths, one persistent launch."""
+    import cirq
+
+    from cirq_gb300 import batch, workloads
+
+    jobs = []
+    per = points // len(widths)
+    for w in widths:
+        circuit, gammas, betas, obs, edges = workloads.qaoa_circuit(w, p, seed=w)
+        pts = workloads.qaoa_points(p, per, seed=100 + w)
+        res = [cirq.ParamResolver({**dict(zip(gammas, q[:p])), **dict(zip(betas, q[p:]))}) for q in pts]
+        jobs.append(batch.BatchJob(circuit, obs, res))
+    batch.simulate_expectation_values_batch(jobs[:1])  # warm-up
+    t = time.perf_counter()
+    vals = batch.simulate_expectation_values_batch(jobs)
+    dt = time.perf_counter() - t
+    return {
+        "workload": f"QAOA p={p}, {points} points over widths {list(widths)}",
+        "points_per_s": points / dt,
+        "s_total": dt,
+        "mean_expectation": float(np.mean([np.real(v).mean() for v in vals])),
+    }
+
+
+# ---------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,6 +405,7 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the adjoint / density / batch lines")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -397,6 +489,14 @@ def main():
         except MemoryError as e:  # pragma: no cover
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "reference", "sample": f"failed: {e}"}
 
+    extra = {}
+    if not args.no_extra and rank == 0:
+        for name, fn in (("adjoint", adjoint_bench), ("density_matrix", density_bench), ("batch_sweep", batch_bench)):
+            try:
+                extra[name] = fn()
+            except Exception as e:  # reported, not hidden
+                extra[name] = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -442,6 +542,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "fusion_sweep": sweep,
+            **extra,
         }
         print(json.dumps(line))
     if dist is not None:
