@@ -120,8 +120,12 @@ def simulate_expectation_values_batch(
     pool_dev = eng.upload(np.concatenate(pools_l))
     terms = np.concatenate(terms_l) if term_off else np.zeros(0, _lib.PAULI_DTYPE)
     points = np.concatenate(points_l)
+    # CTAs claim points in array order: widest first, so the tail of the
+    # launch is filled with short points (each point keeps its term block)
+    order = np.argsort(-points["nbits"], kind="stable")
+    run_points = np.ascontiguousarray(points[order])
     max_nbits = max(int(points["nbits"].max()), BATCH_TILE_BITS)
-    out = eng.batch_expect(points, passes, ops, pool_dev, terms, max_nbits)[:term_off]
+    out = eng.batch_expect(run_points, passes, ops, pool_dev, terms, max_nbits)[:term_off]
     results = []
     for (first, P, slices, coefs), job in zip(layout, jobs):
         nt = len(coefs)

@@ -859,6 +859,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   if (!mats) return arg_fail("gbq_batch_expect: null matrix pool");
   // validate every point's program on the host and convert each pass's ops
   std::vector<OpDev> dops((size_t)(nops ? nops : 1));
+  int smem_kmax = 0;  // widest shared-memory dense op (0: register phases only)
   std::vector<char> converted((size_t)(npasses ? npasses : 1), 0);
   TileInfo ti;
   for (int p = 0; p < npoints; ++p) {
@@ -882,6 +883,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
         rc = convert_op(ops[ps.op_begin + o], ps.L, pt.nbits, inmask, false, d, lay);
         if (rc) return rc;
         if (!converted[pt.pass_begin + q]) dops[ps.op_begin + o] = d;
+        if ((d.kind == GBQ_OP_DENSE || d.kind == GBQ_OP_PROBE) && d.k > smem_kmax) smem_kmax = d.k;
       }
       converted[pt.pass_begin + q] = 1;
     }
@@ -929,7 +931,7 @@ int gbq_batch_expect(gbq_ctx* c, const gbq_point* points, int npoints, const gbq
   e = cudaMemsetAsync(d_out, 0, (size_t)(nterms ? nterms : 1) * 2 * sizeof(double), c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(out)");
   rc = launch_batch(c, d_points, npoints, d_passes, d_ops, reinterpret_cast<const float2*>(mats),
-                    d_terms, max_nbits, slots, nslots, d_counter, d_out);
+                    d_terms, max_nbits, slots, nslots, d_counter, d_out, smem_kmax);
   if (rc) return rc;
   e = cudaMemcpyAsync(out, d_out, (size_t)nterms * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(out)");

@@ -15,6 +15,7 @@ namespace gbq {
 
 constexpr int kBatchTile = 12;
 
+template <int KMAX>
 __global__ void __launch_bounds__(kThreads, 2)
     k_batch(const gbq_point* __restrict__ points, int npoints, const gbq_pass* __restrict__ passes,
             const OpDev* __restrict__ ops, const float2* __restrict__ mats,
@@ -25,6 +26,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ double red[kThreads / 32];
   __shared__ TileInfo ti;
   __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
+  __shared__ uint64_t ttab[3 * kTileTab];
   __shared__ int s_point;
   constexpr int TS = 1 << LT;
   float2* buf = reinterpret_cast<float2*>(smraw);  // [2][TS]
@@ -66,21 +68,22 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
       }
       __syncthreads();
+      tile_tables_build(ti, ttab);
       const TileSetup ts = tile_setup<LT>(ti);
       __syncthreads();
       // every global write of the previous pass is visible here: the whole
       // pass ran in this CTA and ended with __syncthreads()
-      load_tile_async<LT>(ti, psi, buf, tile_base(ti, 0), ts.lo_t, ts.lp_t);
+      load_tile_async<LT>(ti, psi, buf, tile_base_fast(ttab, 0), ts.lo_t, ts.lp_t);
       cp_async_commit();
       int cur = 0;
       for (int64_t tile = 0; tile < ti.ntiles; ++tile) {
         if (tile + 1 < ti.ntiles)
-          load_tile_async<LT>(ti, psi, buf + (cur ^ 1) * TS, tile_base(ti, tile + 1), ts.lo_t, ts.lp_t);
+          load_tile_async<LT>(ti, psi, buf + (cur ^ 1) * TS, tile_base_fast(ttab, tile + 1), ts.lo_t, ts.lp_t);
         cp_async_commit();
         cp_async_wait<1>();
         __syncthreads();
-        const uint64_t gbase = tile_base(ti, tile);
-        run_ops<LT, 5, false>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
+        const uint64_t gbase = tile_base_fast(ttab, tile);
+        run_ops<LT, KMAX, false>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
         store_tile<LT>(ti, psi, buf + cur * TS, gbase, ts.off_t, ts.ph_t);
         __syncthreads();
         cur ^= 1;
@@ -111,23 +114,37 @@ __global__ void __launch_bounds__(kThreads, 2)
   }
 }
 
-int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
-                 const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
-                 float2* slots, int nslots, int* d_counter, double* d_out) {
+template <int KMAX>
+static int launch_batch_k(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
+                          const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms,
+                          int max_nbits, float2* slots, int nslots, int* d_counter, double* d_out) {
   const int smem = 2 * (1 << kBatchTile) * (int)sizeof(float2);
   static bool attr = false;
   cudaError_t e;
   if (!attr) {
-    e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(k_batch<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_batch)");
     attr = true;
   }
-  k_batch<<<nslots, kThreads, smem, c->stream>>>(d_points, npoints, d_passes, d_ops, mats, d_terms,
-                                                 slots, (int64_t)1 << max_nbits, d_counter, d_out);
+  k_batch<KMAX><<<nslots, kThreads, smem, c->stream>>>(d_points, npoints, d_passes, d_ops, mats,
+                                                       d_terms, slots, (int64_t)1 << max_nbits,
+                                                       d_counter, d_out);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
   c->launches += 1;
   return GBQ_OK;
+}
+
+// kmax: widest shared-memory dense op of all points' passes (0: register
+// phases only, which selects the lean kernel variant).
+int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
+                 const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
+                 float2* slots, int nslots, int* d_counter, double* d_out, int kmax) {
+  if (kmax == 0)
+    return launch_batch_k<0>(c, d_points, npoints, d_passes, d_ops, mats, d_terms, max_nbits, slots,
+                             nslots, d_counter, d_out);
+  return launch_batch_k<5>(c, d_points, npoints, d_passes, d_ops, mats, d_terms, max_nbits, slots,
+                           nslots, d_counter, d_out);
 }
 
 }  // namespace gbq

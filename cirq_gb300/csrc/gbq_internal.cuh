@@ -117,7 +117,7 @@ int launch_pass_l12(Ctx* c, const PassArgs& a, bool dual);
 int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
                  const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
-                 float2* slots, int nslots, int* d_counter, double* d_out);
+                 float2* slots, int nslots, int* d_counter, double* d_out, int kmax);
 
 }  // namespace gbq
 
