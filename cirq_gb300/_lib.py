@@ -161,6 +161,7 @@ SIGNATURES = {
     "gbq_ctx_sync": [_P],
     "gbq_device_info": [_P, _P, _P, _P],
     "gbq_set_graphs": [_P, _I],
+    "gbq_device_name": [_P, _P, _I],
     "gbq_launch_count": [_P, _P],
     "gbq_event_record": [_P, _I],
     "gbq_event_elapsed": [_P, _I, _I, _P],
@@ -174,6 +175,9 @@ SIGNATURES = {
     "gbq_d2h": [_P, _P, _P, _SZ],
     "gbq_sv_set_basis": [_P, _P, _I, _U64],
     "gbq_validate_program": [_I, _P, _I, _P, _I, _I],
+    "gbq_graph_create": [_P, _P, _I, _P, _I, _P, _I, _P, _P],
+    "gbq_graph_launch": [_P, _P],
+    "gbq_graph_destroy": [_P],
     "gbq_run": [_P, _P, _I, _P, _I, _P, _I, _P],
     "gbq_run_dual": [_P, _P, _P, _I, _P, _I, _P, _I, _P, _P],
     "gbq_reduce_slots": [_P, _P, _I, _I64, _P],

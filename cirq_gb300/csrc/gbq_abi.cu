@@ -471,6 +471,17 @@ int gbq_device_info(gbq_ctx* c, int* sm_count, size_t* free_bytes, size_t* total
   return GBQ_OK;
 }
 
+int gbq_device_name(gbq_ctx* c, char* buf, int len) {
+  CHECK_CTX(c);
+  if (!buf || len < 1) return arg_fail("gbq_device_name: bad buffer");
+  cudaDeviceProp p;
+  cudaError_t e = cudaGetDeviceProperties(&p, c->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+  strncpy(buf, p.name, (size_t)len - 1);
+  buf[len - 1] = 0;
+  return GBQ_OK;
+}
+
 int gbq_set_graphs(gbq_ctx* c, int enable) {
   if (!c) return arg_fail("null context");
   c->use_graphs = enable != 0;
@@ -611,6 +622,76 @@ int gbq_validate_program(int nbits, const gbq_pass* passes, int npasses, const g
   }
   delete a;
   return rc;
+}
+
+struct gbq_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+  int64_t launches = 0;  // kernels per replay
+};
+
+int gbq_graph_create(gbq_ctx* c, gbq_c64* state, int nbits, const gbq_pass* passes,
+                     int npasses, const gbq_op* ops, int nops, const gbq_c64* mats,
+                     gbq_graph** out) {
+  CHECK_CTX(c);
+  if (!out) return arg_fail("gbq_graph_create: null output");
+  if (!state || nbits < 1 || nbits > 40) return arg_fail("gbq_graph_create: bad state");
+  if (npasses < 0 || (npasses && (!passes || !ops || !mats))) return arg_fail("gbq_graph_create: null program");
+  // validate (and set kernel attributes) before capturing
+  int rc = gbq_validate_program(nbits, passes, npasses, ops, nops, 0);
+  if (rc) return rc;
+  const bool timing = c->pass_timing;
+  c->pass_timing = false;
+  const int64_t l0 = c->launches;
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    c->pass_timing = timing;
+    return cuda_fail(e, "cudaStreamBeginCapture");
+  }
+  rc = run_passes(c, reinterpret_cast<float2*>(state), nullptr, nbits, passes, npasses, ops, nops,
+                  reinterpret_cast<const float2*>(mats), nullptr);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(c->stream, &g);
+  c->pass_timing = timing;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  gbq_graph* gr = new gbq_graph();
+  gr->graph = g;
+  gr->exec = x;
+  gr->device = c->device;
+  gr->launches = c->launches - l0;
+  c->launches = l0;  // captured, not launched
+  *out = gr;
+  return GBQ_OK;
+}
+
+int gbq_graph_launch(gbq_ctx* c, gbq_graph* g) {
+  CHECK_CTX(c);
+  if (!g || !g->exec) return arg_fail("gbq_graph_launch: null graph");
+  if (g->device != c->device) return arg_fail("gbq_graph_launch: graph belongs to another device");
+  cudaError_t e = cudaGraphLaunch(g->exec, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+  c->launches += g->launches;
+  return GBQ_OK;
+}
+
+int gbq_graph_destroy(gbq_graph* g) {
+  if (!g) return GBQ_OK;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return GBQ_OK;
 }
 
 int gbq_run(gbq_ctx* c, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,

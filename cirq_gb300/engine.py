@@ -143,6 +143,11 @@ class Engine:
         buf.upload(host)
         return buf
 
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        check(self.lib.gbq_device_name(self.ctx, buf, 256), "gbq_device_name")
+        return buf.value.decode(errors="replace")
+
     def sync(self) -> None:
         check(self.lib.gbq_ctx_sync(self.ctx), "gbq_ctx_sync")
 
@@ -171,12 +176,22 @@ class Engine:
 
     # ---- state vectors -------------------------------------------------
     def new_state(
-        self, nbits: int, basis: int = 0, initial: np.ndarray | None = None, nbits_dev: int | None = None
+        self,
+        nbits: int,
+        basis: int = 0,
+        initial: np.ndarray | None = None,
+        nbits_dev: int | None = None,
+        into: DeviceBuffer | None = None,
     ) -> DeviceBuffer:
         """A 2^nbits_dev buffer holding |basis> or `initial` (2^nbits amplitudes)
-        in its first 2^nbits entries and zeros above."""
+        in its first 2^nbits entries and zeros above (written into `into` when given)."""
         nbits_dev = max(nbits, nbits_dev or nbits)
-        buf = self.alloc(8 * (1 << nbits_dev))
+        if into is not None:
+            if into.nbytes < 8 * (1 << nbits_dev):
+                raise ValueError("state buffer too small")
+            buf = into
+        else:
+            buf = self.alloc(8 * (1 << nbits_dev))
         if initial is not None:
             arr = np.ascontiguousarray(np.asarray(initial, dtype=np.complex64).reshape(-1))
             if arr.size != 1 << nbits:
@@ -208,6 +223,18 @@ class Engine:
         )
         # keep the pool alive until the stream has consumed it
         self.sync()
+
+    def graph(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer) -> "Graph":
+        """Captures the program's launches on (state, pool_dev) into a CUDA graph."""
+        g = ctypes.c_void_p()
+        check(
+            self.lib.gbq_graph_create(
+                self.ctx, state.ptr, nbits, plan.passes.ctypes.data, len(plan.passes),
+                plan.ops.ctypes.data, len(plan.ops), pool_dev.ptr, ctypes.byref(g),
+            ),
+            "gbq_graph_create",
+        )
+        return Graph(self, g.value, (state, pool_dev))
 
     def run_dual(self, psi, lam, nbits, plan, pool_dev, partial) -> None:
         if plan.npasses == 0:
@@ -332,6 +359,20 @@ class Engine:
             "gbq_batch_expect",
         )
         return out[0::2] + 1j * out[1::2]
+
+
+class Graph:
+    """A captured program; launch() replays it on the engine's stream.  Holds
+    references to the device buffers whose addresses are baked in."""
+
+    def __init__(self, engine: Engine, handle: int, buffers):
+        self.engine = engine
+        self.handle = handle
+        self._buffers = buffers
+        self._fin = weakref.finalize(self, engine.lib.gbq_graph_destroy, handle)
+
+    def launch(self) -> None:
+        check(self.engine.lib.gbq_graph_launch(self.engine.ctx, self.handle), "gbq_graph_launch")
 
 
 def default_engine(device: int | None = None) -> Engine:

@@ -87,8 +87,13 @@ class _GpuSimulatorBase:
         fusion_max_qubits: int = 4,
         tile_bits: int = 12,
         pass_budget: float = 25.0,
+        use_cuda_graphs: bool = False,
+        autotune: bool = False,
     ):
         _check_dtype(dtype)
+        self._use_graphs = use_cuda_graphs
+        self._autotune = autotune
+        self._runners: dict = {}
         self._dtype = np.complex64
         self.noise = cirq.NoiseModel.from_noise_model_like(noise)
         self._prng = cirq.value.parse_random_state(seed)
@@ -124,7 +129,12 @@ class _GpuSimulatorBase:
         if c is not None:
             self._cache.move_to_end(key)
             return c
-        c = CompiledCircuit(body_ops, qubits, dm=self._dm, planner=self.planner, resolvers=resolvers[:1])
+        planner = self.planner
+        if self._autotune and qubits:
+            from cirq_gb300 import autotune
+
+            planner = autotune.tune(body_ops, qubits, self._dm, resolvers[:1], self.engine)
+        c = CompiledCircuit(body_ops, qubits, dm=self._dm, planner=planner, resolvers=resolvers[:1])
         self._cache[key] = c
         if len(self._cache) > _MAX_CACHE:
             self._cache.popitem(last=False)
@@ -142,13 +152,32 @@ class _GpuSimulatorBase:
         return qubits, resolvers, compiled, meas
 
     def _evolve(self, compiled: CompiledCircuit, pool_row: np.ndarray, initial_state):
-        """Allocates the initial state on the device and runs the program."""
+        """Allocates the initial state on the device and runs the program.
+
+        With use_cuda_graphs, one state and one matrix-pool buffer are kept per
+        compiled circuit and the pass sequence is captured once into a CUDA
+        graph; later points upload new matrices into the same buffer and
+        replay the graph.  The returned state is then that shared buffer: it
+        stays valid until the next simulation of the same circuit."""
         eng = self.engine
-        state = self._initial_device_state(compiled, initial_state)
-        if compiled.plan.npasses:
-            pool_dev = eng.upload(np.ascontiguousarray(pool_row))
-            eng.run(state, compiled.nbits_dev, compiled.plan, pool_dev)
-        return state
+        if not self._use_graphs or not compiled.plan.npasses:
+            state = self._initial_device_state(compiled, initial_state)
+            if compiled.plan.npasses:
+                pool_dev = eng.upload(np.ascontiguousarray(pool_row))
+                eng.run(state, compiled.nbits_dev, compiled.plan, pool_dev)
+            return state
+        runner = self._runners.get(id(compiled))
+        if runner is None or runner[0] is not compiled:
+            state = eng.alloc(8 << compiled.nbits_dev)
+            pool_dev = eng.alloc(8 * max(len(compiled.plan.pool), 2))
+            graph = eng.graph(state, compiled.nbits_dev, compiled.plan, pool_dev)
+            runner = (compiled, state, pool_dev, graph)
+            self._runners[id(compiled)] = runner
+        _, state, pool_dev, graph = runner
+        self._initial_device_state(compiled, initial_state, into=state)
+        pool_dev.upload(np.ascontiguousarray(pool_row, dtype=np.complex64))
+        graph.launch()
+        return _Borrowed(state)
 
     def _measure_terminal(self, state, compiled, meas_ops) -> dict[str, np.ndarray]:
         """One shot of every terminal measurement, then collapse (the reference
@@ -230,6 +259,25 @@ class _GpuSimulatorBase:
         return self._sample_records(state, compiled, meas, repetitions)
 
 
+class _Borrowed:
+    """A non-owning view of a device buffer kept by the simulator (free() is a no-op)."""
+
+    def __init__(self, buf):
+        self._buf = buf
+        self.ptr = buf.ptr
+        self.nbytes = buf.nbytes
+        self.engine = buf.engine
+
+    def free(self) -> None:
+        pass
+
+    def upload(self, host):
+        self._buf.upload(host)
+
+    def download(self, host):
+        return self._buf.download(host)
+
+
 def _confuse(bits, qubits, confusion_map, prng) -> None:
     """Applies measurement confusion matrices per repetition, as
     StepResult._confuse_results does (cirq-core/cirq/sim/simulator.py:822-844)."""
@@ -293,7 +341,7 @@ class Simulator(
     """GPU state-vector simulator with the API of ``cirq.Simulator``
     (``cirq-core/cirq/sim/sparse_simulator.py:31-218``)."""
 
-    def _initial_device_state(self, compiled, initial_state):
+    def _initial_device_state(self, compiled, initial_state, into=None):
         eng = self.engine
         n = compiled.n
         if initial_state is None:
@@ -301,11 +349,11 @@ class Simulator(
         if isinstance(initial_state, (int, np.integer)):
             if not 0 <= int(initial_state) < 2**n:
                 raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
-            return eng.new_state(n, basis=int(initial_state), nbits_dev=compiled.nbits_dev)
+            return eng.new_state(n, basis=int(initial_state), nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("cirq_gb300.Simulator takes raw initial states, not SimulationState")
         vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
-        return eng.new_state(n, initial=vec, nbits_dev=compiled.nbits_dev)
+        return eng.new_state(n, initial=vec, nbits_dev=compiled.nbits_dev, into=into)
 
     def simulate_sweep_iter(
         self,
@@ -408,7 +456,7 @@ class DensityMatrixSimulator(
 
     _dm = True
 
-    def _initial_device_state(self, compiled, initial_state):
+    def _initial_device_state(self, compiled, initial_state, into=None):
         eng = self.engine
         n = compiled.n
         if initial_state is None:
@@ -417,11 +465,11 @@ class DensityMatrixSimulator(
             if not 0 <= int(initial_state) < 2**n:
                 raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
             i = int(initial_state)
-            return eng.new_state(2 * n, basis=(i << n) | i, nbits_dev=compiled.nbits_dev)
+            return eng.new_state(2 * n, basis=(i << n) | i, nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("takes raw initial states, not SimulationState")
         rho = cirq.to_valid_density_matrix(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
-        return eng.new_state(2 * n, initial=rho.reshape(-1), nbits_dev=compiled.nbits_dev)
+        return eng.new_state(2 * n, initial=rho.reshape(-1), nbits_dev=compiled.nbits_dev, into=into)
 
     def simulate_sweep_iter(
         self,

@@ -117,6 +117,8 @@ int gbq_ctx_destroy(gbq_ctx* ctx);
 int gbq_ctx_sync(gbq_ctx* ctx);
 int gbq_device_info(gbq_ctx* ctx, int* sm_count, size_t* free_bytes, size_t* total_bytes);
 int gbq_set_graphs(gbq_ctx* ctx, int enable);
+/* Name of the context's GPU (NUL-terminated, truncated to len - 1 bytes). */
+int gbq_device_name(gbq_ctx* ctx, char* buf, int len);
 /* Number of kernels this context has launched (for launch accounting). */
 int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
 /* Stream-ordered timing: records CUDA event `slot` (0..15) on the context's
@@ -155,6 +157,20 @@ int gbq_sv_set_basis(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t index);
  * 2^GBQ_MIN_TILE_BITS buffer whose extra (high) bits stay |0>. */
 int gbq_run(gbq_ctx* ctx, gbq_c64* state, int nbits, const gbq_pass* passes, int npasses,
             const gbq_op* ops, int nops, const gbq_c64* mats);
+
+/* CUDA-graph capture of a program: gbq_graph_create records the launches
+ * gbq_run would make for (state, program, mats) into a graph (stream capture
+ * on the context's stream; nothing runs); gbq_graph_launch replays it.  The
+ * state and pool pointers are baked in -- their contents may change between
+ * launches (new parameter values, a new initial state), their addresses not.
+ * Replaces one host launch per pass with one graph launch per simulation of
+ * a circuit (the per-point loop of cirq-core/cirq/sim/simulator.py:558-605). */
+typedef struct gbq_graph gbq_graph;
+int gbq_graph_create(gbq_ctx* ctx, gbq_c64* state, int nbits, const gbq_pass* passes,
+                     int npasses, const gbq_op* ops, int nops, const gbq_c64* mats,
+                     gbq_graph** out);
+int gbq_graph_launch(gbq_ctx* ctx, gbq_graph* graph);
+int gbq_graph_destroy(gbq_graph* graph);
 
 /* Checks a program against a state of nbits bits exactly as gbq_run /
  * gbq_run_dual (dual != 0) do before launching, without touching a GPU. */
