@@ -66,6 +66,8 @@ POINT_DTYPE = np.dtype(
 
 OP_DENSE, OP_DIAG, OP_PROBE, OP_PROBE_DIAG = 0, 1, 2, 3
 OP_LAYOUT, OP_RDENSE, OP_RDIAG, OP_RPROBE, OP_RPROBE_DIAG = 4, 5, 6, 7, 8
+OP_MMA = 9
+MMA_TILE_BITS, MAX_MMA_OPS, MAX_MMA_MATS = 11, 8, 6
 
 ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED = -1, -2, -3, -4
 

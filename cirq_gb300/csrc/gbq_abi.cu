@@ -87,6 +87,16 @@ static int set_device(Ctx* c) {
 static int sync(Ctx* c, const char* what) {
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(e, what);
+  if (c->mma_used && c->d_abort) {
+    int flag = 0;
+    e = cudaMemcpy(&flag, c->d_abort, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (flag) {
+      cudaMemset(c->d_abort, 0, sizeof(int));
+      set_error(std::string(what) + ": a tensor-core pass gave up waiting for its MMAs (state invalid)");
+      return GBQ_ERR_CUDA;
+    }
+  }
   return GBQ_OK;
 }
 
@@ -349,21 +359,42 @@ static int timed_pair(Ctx* c, std::pair<cudaEvent_t, cudaEvent_t>& ev) {
   return GBQ_OK;
 }
 
+static bool is_mma_pass(const gbq_pass& p, const gbq_op* ops) {
+  for (int o = 0; o < p.op_count; ++o)
+    if (ops[p.op_begin + o].kind == GBQ_OP_MMA) return true;
+  return false;
+}
+
+// Checks one pass (and fills the kernel arguments of its kind).
+static int convert_pass(const gbq_pass& p, const gbq_op* ops, int nops, int nbits, bool dual, PassArgs& a,
+                        MmaArgs& ma, bool& mma) {
+  memset(&a, 0, sizeof(a));
+  uint64_t inmask = 0;
+  int rc = pass_geometry(p, nops, nbits, a.ti, inmask);
+  if (rc) return rc;
+  mma = is_mma_pass(p, ops);
+  if (mma) {
+    if (dual) return arg_fail("pass: tensor-core passes run on one state only");
+    return build_mma_args(p, ops, nbits, a.ti, inmask, ma);
+  }
+  LayoutState lay;
+  for (int o = 0; o < p.op_count; ++o) {
+    rc = convert_op(ops[p.op_begin + o], p.L, nbits, inmask, dual, a.ops[o], lay);
+    if (rc) return rc;
+  }
+  return GBQ_OK;
+}
+
 static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pass* passes,
                       int npasses, const gbq_op* ops, int nops, const float2* mats,
                       double* partial) {
   const bool dual = lam != nullptr;
   PassArgs a;
+  MmaArgs ma;
   for (int q = 0; q < npasses; ++q) {
-    memset(&a, 0, sizeof(a));
-    uint64_t inmask = 0;
-    int rc = pass_geometry(passes[q], nops, nbits, a.ti, inmask);
+    bool mma = false;
+    int rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, mma);
     if (rc) return rc;
-    LayoutState lay;
-    for (int o = 0; o < passes[q].op_count; ++o) {
-      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual, a.ops[o], lay);
-      if (rc) return rc;
-    }
     a.psi = psi;
     a.lam = lam;
     a.ti.mats = mats;
@@ -374,7 +405,15 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
       if (rc) return rc;
       cudaEventRecord(ev.first, c->stream);
     }
-    rc = launch_pass(c, a, dual);
+    if (mma) {
+      ma.psi = psi;
+      ma.ti.mats = mats;
+      ma.abort = c->d_abort;
+      c->mma_used = true;
+      rc = launch_mma_pass(c, ma);
+    } else {
+      rc = launch_pass(c, a, dual);
+    }
     if (rc) return rc;
     if (c->pass_timing) {
       cudaEventRecord(ev.second, c->stream);
@@ -425,10 +464,13 @@ int gbq_ctx_create(int device, gbq_ctx** out) {
     return cuda_fail(e, "cudaStreamCreate");
   }
   e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_abort, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_abort, 0, sizeof(int));
   if (e != cudaSuccess) {
+    if (c->d_abort) cudaFree(c->d_abort);
     cudaStreamDestroy(c->stream);
     delete c;
-    return cuda_fail(e, "cudaDeviceGetAttribute");
+    return cuda_fail(e, "gbq_ctx_create");
   }
   *out = c;
   return GBQ_OK;
@@ -439,6 +481,7 @@ int gbq_ctx_destroy(gbq_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->scratch) cudaFree(c->scratch);
+  if (c->d_abort) cudaFree(c->d_abort);
   if (c->host_scratch) cudaFreeHost(c->host_scratch);
   for (auto& ev : c->timed) {
     cudaEventDestroy(ev.first);
@@ -612,15 +655,14 @@ int gbq_validate_program(int nbits, const gbq_pass* passes, int npasses, const g
   if (nbits < 1 || nbits > 40) return arg_fail("gbq_validate_program: bad width");
   if (npasses < 0 || (npasses && (!passes || !ops))) return arg_fail("gbq_validate_program: null program");
   PassArgs* a = new PassArgs();
+  MmaArgs* ma = new MmaArgs();
   int rc = GBQ_OK;
   for (int q = 0; q < npasses && rc == GBQ_OK; ++q) {
-    uint64_t inmask = 0;
-    rc = pass_geometry(passes[q], nops, nbits, a->ti, inmask);
-    LayoutState lay;
-    for (int o = 0; rc == GBQ_OK && o < passes[q].op_count; ++o)
-      rc = convert_op(ops[passes[q].op_begin + o], passes[q].L, nbits, inmask, dual != 0, a->ops[o], lay);
+    bool mma = false;
+    rc = convert_pass(passes[q], ops, nops, nbits, dual != 0, *a, *ma, mma);
   }
   delete a;
+  delete ma;
   return rc;
 }
 

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         cp_async_wait<1>();
         __syncthreads();
         const uint64_t gbase = tile_base_fast(ttab, tile);
-        run_ops<LT, KMAX, false>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
+        run_ops<LT, KMAX, false, 4>(ti, sops, buf + cur * TS, nullptr, gbase, tile, red);
         store_tile<LT>(ti, psi, buf + cur * TS, gbase, ts.off_t, ts.ph_t);
         __syncthreads();
         cur ^= 1;

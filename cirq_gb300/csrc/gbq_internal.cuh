@@ -85,6 +85,39 @@ struct PassArgs {
   OpDev ops[GBQ_MAX_OPS_PER_PASS];
 };
 
+// Tensor-core pass (gbq_mma.cu): per MMA op, the amplitude-position columns
+// of its result in the next op's layout (or the final natural layout).
+struct MmaOpDev {
+  int64_t mat;         // pool offset of the first matrix
+  uint16_t tnext[4];   // next-layout position column of target bit p
+  uint16_t rnext[7];   // ... of row bit q (row bits 0..4 are the lane bits)
+  int8_t nsel;
+  int8_t selg[3];      // global bit of selector s
+  int16_t bslot;       // first B-operand slot in shared memory
+  int8_t ndiag;        // diagonal ops applied to this op's result
+  int8_t diag0;
+};
+
+struct MmaDiagDev {
+  int64_t mat;
+  uint16_t trow[7];  // table-index bits contributed by row bit q of the MMA op
+  uint16_t ttgt[4];  // ... by target bit p
+  int8_t k;
+  int8_t dext[8];    // table bit j <- global bit dext[j] (-1: a tile bit)
+  int8_t pad[5];
+};
+
+struct MmaArgs {
+  float2* psi;
+  int* abort;        // set to 1 when an MMA wait gives up
+  TileInfo ti;
+  int32_t nops, ndiag, nmats, pad;
+  uint16_t lcol[GBQ_MMA_TILE_BITS];  // position column of tile bit b in op 0's layout
+  uint16_t pad2;
+  MmaOpDev ops[GBQ_MAX_MMA_OPS];
+  MmaDiagDev diags[GBQ_MAX_OPS_PER_PASS];
+};
+
 // Error plumbing (gbq_abi.cu).
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
@@ -105,6 +138,8 @@ struct Ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> event_pool;
   double timed_ms = 0.0;
   int64_t timed_launches = 0;
+  int* d_abort = nullptr;  // device flag set by a tensor-core pass that gave up a wait
+  bool mma_used = false;
 };
 
 int ensure_scratch(Ctx* c, size_t bytes);
@@ -115,6 +150,9 @@ int launch_pass_l10(Ctx* c, const PassArgs& a, bool dual);
 int launch_pass_l11(Ctx* c, const PassArgs& a, bool dual);
 int launch_pass_l12(Ctx* c, const PassArgs& a, bool dual);
 int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
+int build_mma_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInfo& ti, uint64_t inmask,
+                   MmaArgs& A);
+int launch_mma_pass(Ctx* c, const MmaArgs& a);
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
                  const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
                  float2* slots, int nslots, int* d_counter, double* d_out, int kmax);

@@ -40,6 +40,12 @@ __device__ __forceinline__ uint32_t phys_dev(uint32_t i) {
   return i ^ s;
 }
 
+// Register dense ops of width <= 2 use packed f32x2 FMAs (sm_100 family):
+// acc += m * a as two fma.rn.f32x2, m * (a.x, a.x) and (i m) * (a.y, a.y).
+#ifndef GBQ_FFMA2
+#define GBQ_FFMA2 1
+#endif
+
 __device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
   acc.x = fmaf(a.x, b.x, acc.x);
   acc.x = fmaf(-a.y, b.y, acc.x);
@@ -507,6 +513,56 @@ __device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
   constexpr int REST = (A - 1) & ~MASK;
   const float2* mp = reg_matrix(ti, op, st, gbase, D * D);
   float part = 0.f;
+#if GBQ_FFMA2
+  if constexpr (K <= 2 && !PROBE) {
+    // Packed form: acc += m * a as two f32x2 FMAs, m * (a.x, a.x) and
+    // (i m) * (a.y, a.y).
+    float2 m[D * D], im[D * D];
+#pragma unroll
+    for (int e = 0; e < D * D; e += 2) {
+      const float4 mm = __ldg(reinterpret_cast<const float4*>(mp + e));
+      m[e] = make_float2(mm.x, mm.y);
+      m[e + 1] = make_float2(mm.z, mm.w);
+      im[e] = make_float2(-mm.y, mm.x);
+      im[e + 1] = make_float2(-mm.w, mm.z);
+    }
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_const(g, REST);
+      float2 ax[D], ay[D], bx[DUAL ? D : 1], by[DUAL ? D : 1];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const float2 a = st.v[s0 | dep_const(j, MASK)];
+        ax[j] = make_float2(a.x, a.x);
+        ay[j] = make_float2(a.y, a.y);
+        if constexpr (DUAL) {
+          const float2 b = st.w[s0 | dep_const(j, MASK)];
+          bx[j] = make_float2(b.x, b.x);
+          by[j] = make_float2(b.y, b.y);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          acc = __ffma2_rn(m[r * D + c], ax[c], acc);
+          acc = __ffma2_rn(im[r * D + c], ay[c], acc);
+        }
+        st.v[s0 | dep_const(r, MASK)] = acc;
+        if constexpr (DUAL) {
+          float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            accb = __ffma2_rn(m[r * D + c], bx[c], accb);
+            accb = __ffma2_rn(im[r * D + c], by[c], accb);
+          }
+          st.w[s0 | dep_const(r, MASK)] = accb;
+        }
+      }
+    }
+  } else
+#endif
   if constexpr (K <= 2) {
     float2 m[D * D];
 #pragma unroll
@@ -624,21 +680,21 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
     cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
 }
 
-template <int LT, int KMAX, bool DUAL, bool PROBE, int M = 1>
+template <int LT, int KMAX, bool DUAL, bool PROBE, int RK, int M = 1>
 __device__ __forceinline__ void reg_dense_dispatch(const TileInfo& ti, const OpDev& op,
                                                    RegState<LT, DUAL>& st, uint64_t gbase,
                                                    int64_t tile, double* red) {
   if constexpr (M < (1 << RegState<LT, DUAL>::R)) {
     if (op.rmask == M) {
-      if constexpr (!PROBE || popc_const(M) <= 3)
+      if constexpr ((!PROBE || popc_const(M) <= 3) && popc_const(M) <= RK)
         reg_dense<M, LT, DUAL, PROBE>(ti, op, st, gbase, tile, red);
     } else {
-      reg_dense_dispatch<LT, KMAX, DUAL, PROBE, M + 1>(ti, op, st, gbase, tile, red);
+      reg_dense_dispatch<LT, KMAX, DUAL, PROBE, RK, M + 1>(ti, op, st, gbase, tile, red);
     }
   }
 }
 
-template <int LT, int KMAX, bool DUAL>
+template <int LT, int KMAX, bool DUAL, int RK = 4>
 __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, float2* smA,
                                         float2* smB, uint64_t gbase, int64_t tile, double* red) {
   if constexpr (LT <= 12) {
@@ -655,11 +711,11 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
         phase_enter(st, op, smA, smB);
         in_phase = true;
       } else if (kind == GBQ_OP_RDENSE) {
-        reg_dense_dispatch<LT, KMAX, DUAL, false>(ti, op, st, gbase, tile, red);
+        reg_dense_dispatch<LT, KMAX, DUAL, false, RK>(ti, op, st, gbase, tile, red);
       } else if (kind == GBQ_OP_RDIAG) {
         reg_diag<LT, DUAL, false>(ti, op, st, gbase, tile, red);
       } else if (kind == GBQ_OP_RPROBE) {
-        if constexpr (DUAL) reg_dense_dispatch<LT, KMAX, true, true>(ti, op, st, gbase, tile, red);
+        if constexpr (DUAL) reg_dense_dispatch<LT, KMAX, true, true, RK>(ti, op, st, gbase, tile, red);
       } else if (kind == GBQ_OP_RPROBE_DIAG) {
         if constexpr (DUAL) reg_diag<LT, true, true>(ti, op, st, gbase, tile, red);
       } else {
@@ -687,20 +743,28 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
 // STAGES shared buffers per state: tile i is processed in one while the next
 // STAGES - 1 tiles stream into the others (cp.async groups), so the memory
 // system stays busy while the CTA computes.
-template <int LT, int KMAX, bool DUAL, int STAGES>
-__global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant__ PassArgs a) {
+// RK: widest register dense op compiled in (2 or 4); the RK = 2 lean variant
+// targets 3 CTAs per SM.
+template <int LT, int KMAX, bool DUAL, int STAGES, int RK>
+__global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 : 2)
+    k_tile_pass(const __grid_constant__ PassArgs a) {
   constexpr int kStages = STAGES;
+  // The lean variant reads its ops straight from the kernel parameters
+  // (uniform indices hit the constant cache) so that three CTAs of 2^12
+  // amplitude tiles fit in shared memory.
+  constexpr bool kParamOps = (KMAX == 0 && RK <= 2 && !DUAL);
   extern __shared__ float4 smraw[];
-  __shared__ OpDev sops[GBQ_MAX_OPS_PER_PASS];
+  __shared__ OpDev sops_sh[kParamOps ? 1 : GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t ttab[3 * kTileTab];
   __shared__ double red[kThreads / 32];
   constexpr int TS = 1 << LT;
   constexpr int NS = DUAL ? 2 : 1;
   float2* buf = reinterpret_cast<float2*>(smraw);  // [kStages][NS][TS]
-  {
+  const OpDev* sops = kParamOps ? a.ops : sops_sh;
+  if constexpr (!kParamOps) {
     const int nwords = a.ti.nops * (int)(sizeof(OpDev) / 4);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.ops);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(sops_sh);
     for (int i = threadIdx.x; i < nwords; i += kThreads) dst[i] = src[i];
   }
   tile_tables_build(a.ti, ttab);
@@ -735,7 +799,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
     float2* smA = buf + cur * NS * TS;
     float2* smB = smA + TS;
     const uint64_t gbase = tile_base_fast(ttab, tile);
-    run_ops<LT, KMAX, DUAL>(a.ti, sops, smA, smB, gbase, tile, red);
+    run_ops<LT, KMAX, DUAL, RK>(a.ti, sops, smA, smB, gbase, tile, red);
     store_tile<LT>(a.ti, a.psi, smA, gbase, ts.off_t, ts.ph_t);
     if constexpr (DUAL) store_tile<LT>(a.ti, a.lam, smB, gbase, ts.off_t, ts.ph_t);
     __syncthreads();
@@ -744,27 +808,31 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile_pass(const __grid_constant
   cp_async_wait<0>();
 }
 
-template <int LT, int KMAX, bool DUAL, int STAGES>
+template <int LT, int KMAX, bool DUAL, int STAGES, int RK>
 int launch_tile_pass_stages(Ctx* c, const PassArgs& a) {
   const int smem = STAGES * (DUAL ? 2 : 1) * (1 << LT) * (int)sizeof(float2);
   static int blocks_per_sm = -1;
   cudaError_t e;
   if (blocks_per_sm < 0) {
-    e = cudaFuncSetAttribute(k_tile_pass<LT, KMAX, DUAL, STAGES>,
+    e = cudaFuncSetAttribute(k_tile_pass<LT, KMAX, DUAL, STAGES, RK>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_tile_pass)");
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_pass<LT, KMAX, DUAL, STAGES>,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_pass<LT, KMAX, DUAL, STAGES, RK>,
                                                       kThreads, smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     blocks_per_sm = nb > 0 ? nb : 1;
+    if (const char* cap = getenv("GBQ_CTAS_PER_SM")) {
+      const int want = atoi(cap);
+      if (want > 0 && want < blocks_per_sm) blocks_per_sm = want;
+    }
     if (getenv("GBQ_DEBUG"))
-      fprintf(stderr, "k_tile_pass<L=%d,K=%d,dual=%d,stages=%d>: %d blocks/SM, %d B smem\n", LT, KMAX,
-              (int)DUAL, STAGES, blocks_per_sm, smem);
+      fprintf(stderr, "k_tile_pass<L=%d,K=%d,dual=%d,stages=%d,rk=%d>: %d blocks/SM, %d B smem\n", LT,
+              KMAX, (int)DUAL, STAGES, RK, blocks_per_sm, smem);
   }
   int64_t grid = (int64_t)c->sm_count * blocks_per_sm;
   if (grid > a.ti.ntiles) grid = a.ti.ntiles;
-  k_tile_pass<LT, KMAX, DUAL, STAGES><<<(unsigned)grid, kThreads, smem, c->stream>>>(a);
+  k_tile_pass<LT, KMAX, DUAL, STAGES, RK><<<(unsigned)grid, kThreads, smem, c->stream>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_tile_pass launch");
   c->launches += 1;
@@ -781,10 +849,23 @@ inline int pipeline_stages() {
   return st;
 }
 
+// Widest register dense op of a pass.
+inline int pass_rkmax(const PassArgs& a) {
+  int k = 0;
+  for (int o = 0; o < a.ti.nops; ++o) {
+    const int kind = a.ops[o].kind;
+    if ((kind == GBQ_OP_RDENSE || kind == GBQ_OP_RPROBE) && a.ops[o].k > k) k = a.ops[o].k;
+  }
+  return k;
+}
+
 template <int LT, int KMAX, bool DUAL>
 int launch_tile_pass(Ctx* c, const PassArgs& a) {
-  if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3>(c, a);
-  return launch_tile_pass_stages<LT, KMAX, DUAL, 2>(c, a);
+  if constexpr (KMAX == 0 && !DUAL) {
+    if (pass_rkmax(a) <= 2) return launch_tile_pass_stages<LT, 0, false, 2, 2>(c, a);
+  }
+  if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3, 4>(c, a);
+  return launch_tile_pass_stages<LT, KMAX, DUAL, 2, 4>(c, a);
 }
 
 // Widest shared-memory dense (or dense-probe) op of a pass (0 if none).

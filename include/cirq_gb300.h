@@ -69,6 +69,18 @@ typedef struct gbq_ctx gbq_ctx;
 #define GBQ_OP_RDIAG 6
 #define GBQ_OP_RPROBE 7
 #define GBQ_OP_RPROBE_DIAG 8
+/* Tensor-core op: a 16 x 16 matrix on exactly 4 tile bits (bits[0..3]),
+ * applied with tcgen05 MMAs in a three-term TF32 split (fp32-level
+ * accuracy); selectors, if any, are global bit codes (< 0).  A pass that
+ * holds an MMA op is a tensor-core pass: L = GBQ_MMA_TILE_BITS, m >= 1, its
+ * first op is MMA, every other op is MMA or DIAG (a DIAG applies to the
+ * result of the MMA op before it), at most GBQ_MAX_MMA_OPS MMA ops whose
+ * matrices (2^nsel each) number at most GBQ_MAX_MMA_MATS; single-state runs
+ * only (gbq_run, gbq_graph_create). */
+#define GBQ_OP_MMA 9
+#define GBQ_MMA_TILE_BITS 11
+#define GBQ_MAX_MMA_OPS 8
+#define GBQ_MAX_MMA_MATS 6
 
 #define GBQ_MAX_OPS_PER_PASS 64
 #define GBQ_MAX_TILE_BITS 13

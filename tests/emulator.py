@@ -28,7 +28,8 @@ def run_program(state, nbits, passes, ops, pool):
             kind = int(op["kind"])
             if kind == 4:  # layout: changes where amplitudes live, not their values
                 continue
-            kind = {5: 0, 6: 1}.get(kind, kind)  # register ops compute what plain ops do
+            # register ops and tensor-core (MMA) ops compute what plain ops do
+            kind = {5: 0, 6: 1, 9: 0}.get(kind, kind)
             if kind == 0:  # dense
                 tg = [tile_to_global[int(b)] for b in op["bits"][:k]]
                 nsel = int(op["nsel"])
