@@ -87,13 +87,13 @@ static int set_device(Ctx* c) {
 static int sync(Ctx* c, const char* what) {
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(e, what);
-  if (c->mma_used && c->d_abort) {
+  if (c->abort_armed && c->d_abort) {
     int flag = 0;
     e = cudaMemcpy(&flag, c->d_abort, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, what);
     if (flag) {
       cudaMemset(c->d_abort, 0, sizeof(int));
-      set_error(std::string(what) + ": a tensor-core pass gave up waiting for its MMAs (state invalid)");
+      set_error(std::string(what) + ": a pass gave up a bounded wait (state invalid)");
       return GBQ_ERR_CUDA;
     }
   }
@@ -397,8 +397,10 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
     if (rc) return rc;
     a.psi = psi;
     a.lam = lam;
+    a.abort = c->d_abort;
     a.ti.mats = mats;
     a.ti.partial = partial;
+    c->abort_armed = true;
     std::pair<cudaEvent_t, cudaEvent_t> ev;
     if (c->pass_timing) {
       rc = timed_pair(c, ev);
@@ -409,7 +411,6 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
       ma.psi = psi;
       ma.ti.mats = mats;
       ma.abort = c->d_abort;
-      c->mma_used = true;
       rc = launch_mma_pass(c, ma);
     } else {
       rc = launch_pass(c, a, dual);

@@ -81,6 +81,7 @@ struct TileInfo {
 struct PassArgs {
   float2* psi;
   float2* lam;  // second state (two-state passes only)
+  int* abort;   // set to 1 by a pass that gave up a bounded wait
   TileInfo ti;
   OpDev ops[GBQ_MAX_OPS_PER_PASS];
 };
@@ -138,8 +139,8 @@ struct Ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> event_pool;
   double timed_ms = 0.0;
   int64_t timed_launches = 0;
-  int* d_abort = nullptr;  // device flag set by a tensor-core pass that gave up a wait
-  bool mma_used = false;
+  int* d_abort = nullptr;  // device flag set by a pass that gave up a bounded wait
+  bool abort_armed = false;  // a kernel that can set d_abort has been launched
 };
 
 int ensure_scratch(Ctx* c, size_t bytes);

@@ -694,7 +694,17 @@ __device__ __forceinline__ void reg_dense_dispatch(const TileInfo& ti, const OpD
   }
 }
 
-template <int LT, int KMAX, bool DUAL, int RK = 4>
+// Barrier among the threads that run the ops: the whole CTA, or (NB) the
+// 256 consumer threads of a warp-specialised CTA (named barrier 1).
+template <bool NB>
+__device__ __forceinline__ void ops_barrier() {
+  if constexpr (NB)
+    asm volatile("bar.sync 1, 256;\n" ::: "memory");
+  else
+    __syncthreads();
+}
+
+template <int LT, int KMAX, bool DUAL, int RK = 4, bool NB = false>
 __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, float2* smA,
                                         float2* smB, uint64_t gbase, int64_t tile, double* red) {
   if constexpr (LT <= 12) {
@@ -706,7 +716,7 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
       if (kind == GBQ_OP_LAYOUT) {
         if (in_phase) {
           phase_exit(st, smA, smB);
-          __syncthreads();
+          ops_barrier<NB>();
         }
         phase_enter(st, op, smA, smB);
         in_phase = true;
@@ -721,21 +731,21 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
       } else {
         if (in_phase) {
           phase_exit(st, smA, smB);
-          __syncthreads();
+          ops_barrier<NB>();
           in_phase = false;
         }
         dispatch<LT, KMAX, DUAL>(ti, op, smA, smB, gbase, tile, red);
-        __syncthreads();
+        ops_barrier<NB>();
       }
     }
     if (in_phase) {
       phase_exit(st, smA, smB);
-      __syncthreads();
+      ops_barrier<NB>();
     }
   } else {
     for (int o = 0; o < ti.nops; ++o) {
       dispatch<LT, KMAX, DUAL>(ti, sops[o], smA, smB, gbase, tile, red);
-      __syncthreads();
+      ops_barrier<NB>();
     }
   }
 }
@@ -839,6 +849,178 @@ int launch_tile_pass_stages(Ctx* c, const PassArgs& a) {
   return GBQ_OK;
 }
 
+// ---- warp-specialised pass -----------------------------------------------------
+// Eight consumer warps run the ops; a ninth (producer) warp streams tiles
+// through WS_STAGES shared buffers: it copies tile i into buffer i % S with
+// cp.async (completion signalled on full[b] by cp.async.mbarrier.arrive), and
+// once the consumers have released buffer b (empty[b]) it writes tile i - S
+// back with 16-byte stores before refilling b.  Loads, write-backs and the
+// FMA-bound register phases of other tiles run at the same time, on different
+// pipes.  Every mbarrier wait is bounded; a consumer-wide vote after each wait
+// keeps the named barriers of the consumers consistent if one gives up.
+constexpr int kWsStages = 3;
+constexpr int kWsProducers = 2;  // producer warps per CTA
+constexpr int kWsThreads = kThreads + 32 * kWsProducers;
+constexpr long kWsSpin = 1L << 26;
+
+__device__ __forceinline__ uint32_t ws_su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Bounded wait for the phase with the given parity; gives up (returns
+// false) after kWsSpin polls or when another thread has raised *abort.
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  const uint32_t a = ws_su32(bar);
+  for (long it = 0; it < kWsSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255) == 255 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+// Named-barrier OR over the 256 consumer threads.
+__device__ __forceinline__ bool consumers_any(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, 1, 256, p;\n"
+      "selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
+template <int LT>
+__global__ void __launch_bounds__(kWsThreads, 2) k_tile_ws(const __grid_constant__ PassArgs a) {
+  constexpr int TS = 1 << LT;
+  constexpr int S = kWsStages;
+  constexpr int NH = TS >> 5;  // tile-index values of bits 5..LT-1
+  extern __shared__ float4 smraw[];
+  __shared__ uint64_t ttab[3 * kTileTab];
+  __shared__ uint64_t hoff[NH];   // global offset of tile index (j << 5)
+  __shared__ uint16_t hphys[NH];  // shared index of tile index (j << 5)
+  __shared__ __align__(8) uint64_t full[S], empty[S];
+  __shared__ int abort_flag;
+  __shared__ double red[kThreads / 32];
+  float2* buf = reinterpret_cast<float2*>(smraw);  // [S][TS]
+  const TileInfo& ti = a.ti;
+  const int t = threadIdx.x;
+  for (int e = t; e < 3 * kTileTab; e += kWsThreads) {
+    const int part = e / kTileTab;
+    ttab[e] = tile_base(ti, (int64_t)(e % kTileTab) << (8 * part));
+  }
+  for (int j = t; j < NH; j += kWsThreads) {
+    hoff[j] = lin_off<LT>(ti, (uint32_t)j << 5);
+    hphys[j] = (uint16_t)phys_dev((uint32_t)j << 5);
+  }
+  if (t == 0) {
+    abort_flag = 0;
+    for (int b = 0; b < S; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(ws_su32(&full[b])), "r"(32 * kWsProducers));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;\n" ::"r"(ws_su32(&empty[b])));
+    }
+  }
+  __syncthreads();
+  const int64_t step = gridDim.x;
+  const int64_t count = blockIdx.x < ti.ntiles ? (ti.ntiles - 1 - blockIdx.x) / step + 1 : 0;
+  volatile int* abort = &abort_flag;
+  // warp-uniform role (the shuffle lets the compiler keep the consumer's op
+  // loop on the uniform datapath)
+  const int warp_u = __shfl_sync(0xffffffffu, t >> 5, 0);
+  if (warp_u >= kThreads / 32) {
+    // ---- producer warp
+    const int pt = t - kThreads;  // producer thread
+    const int lane = pt & 31, pw = pt >> 5;
+    const uint64_t lo_l = lin_off<LT>(ti, (uint32_t)lane);             // load: tile index lane + 32 j
+    const uint32_t lp_l = phys_dev((uint32_t)lane);
+    const uint64_t so_l = lin_off<LT>(ti, (uint32_t)(2 * lane) & 31u);  // store: tile index 2 lane + 64 j
+    const uint32_t sp_l = phys_dev((uint32_t)(2 * lane) & 31u);
+    const int shalf = (2 * lane) >> 5;                                // bit 5 of 2 lane
+    for (int64_t i = 0; i < count + S; ++i) {
+      const int b = (int)(i % S);
+      float2* sb = buf + (size_t)b * TS;
+      if (i >= S) {
+        if (!ws_wait(&empty[b], (uint32_t)(((i - S) / S) & 1), abort)) break;
+        const uint64_t gb = tile_base_fast(ttab, blockIdx.x + (i - S) * step);
+        float2* g = a.psi + gb + so_l;
+#pragma unroll 4
+        for (int j = pw; j < NH / 2; j += kWsProducers) {
+          const int h = 2 * j + shalf;
+          const uint32_t p = sp_l ^ hphys[h];
+          const float2 x = sb[p], y = sb[p ^ 1u];
+          __stcs(reinterpret_cast<float4*>(g + hoff[h]), make_float4(x.x, x.y, y.x, y.y));
+        }
+      }
+      if (i < count) {
+        const uint64_t gb = tile_base_fast(ttab, blockIdx.x + i * step);
+        const float2* g = a.psi + gb + lo_l;
+#pragma unroll 8
+        for (int j = pw; j < NH; j += kWsProducers) cp_async8(sb + (lp_l ^ hphys[j]), g + hoff[j]);
+        asm volatile("cp.async.mbarrier.arrive.noinc.shared.b64 [%0];\n" ::"r"(ws_su32(&full[b])) : "memory");
+      }
+    }
+    cp_async_wait<0>();
+  } else {
+    // ---- consumer warps
+    for (int64_t i = 0; i < count; ++i) {
+      const int b = (int)(i % S);
+      const bool ok = ws_wait(&full[b], (uint32_t)((i / S) & 1), abort);
+      if (consumers_any(!ok)) break;
+      float2* sb = buf + (size_t)b * TS;
+      const int64_t tile = blockIdx.x + i * step;
+      const uint64_t gbase = tile_base_fast(ttab, tile);
+      run_ops<LT, 0, false, 2, true>(ti, a.ops, sb, nullptr, gbase, tile, red);
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(ws_su32(&empty[b])) : "memory");
+    }
+  }
+  if (t == 0 || t == kThreads) {  // one consumer and one producer thread report an abort
+    if (*abort && a.abort) atomicExch(a.abort, 1);
+  }
+}
+
+template <int LT>
+int launch_tile_ws(Ctx* c, const PassArgs& a) {
+  constexpr int smem = kWsStages * (1 << LT) * (int)sizeof(float2);
+  static int blocks_per_sm = -1;
+  cudaError_t e;
+  if (blocks_per_sm < 0) {
+    e = cudaFuncSetAttribute(k_tile_ws<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_tile_ws)");
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tile_ws<LT>, kWsThreads, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    blocks_per_sm = nb > 0 ? nb : 1;
+    if (getenv("GBQ_DEBUG"))
+      fprintf(stderr, "k_tile_ws<L=%d>: %d blocks/SM, %d B smem\n", LT, blocks_per_sm, smem);
+  }
+  int64_t grid = (int64_t)c->sm_count * blocks_per_sm;
+  if (grid > a.ti.ntiles) grid = a.ti.ntiles;
+  k_tile_ws<LT><<<(unsigned)grid, kWsThreads, smem, c->stream>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_tile_ws launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
+
+// Warp-specialised passes: single state, register/diag ops of width <= 2
+// only, tile bits 0..4 = global bits 0..4.  GBQ_WS=0 turns them off.
+inline bool ws_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("GBQ_WS");
+    on = (e && atoi(e) == 0) ? 0 : 1;
+  }
+  return on == 1;
+}
+
 // Pipeline depth: 2 by default; GBQ_STAGES=3 selects three buffers.
 inline int pipeline_stages() {
   static int st = -1;
@@ -862,7 +1044,12 @@ inline int pass_rkmax(const PassArgs& a) {
 template <int LT, int KMAX, bool DUAL>
 int launch_tile_pass(Ctx* c, const PassArgs& a) {
   if constexpr (KMAX == 0 && !DUAL) {
-    if (pass_rkmax(a) <= 2) return launch_tile_pass_stages<LT, 0, false, 2, 2>(c, a);
+    if (pass_rkmax(a) <= 2) {
+      if constexpr (LT == 12) {
+        if (ws_enabled() && a.ti.m >= 5) return launch_tile_ws<LT>(c, a);
+      }
+      return launch_tile_pass_stages<LT, 0, false, 2, 2>(c, a);
+    }
   }
   if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3, 4>(c, a);
   return launch_tile_pass_stages<LT, KMAX, DUAL, 2, 4>(c, a);
