@@ -33,6 +33,42 @@ def _cirq():
     return ensure_cirq()
 
 
+@dataclasses.dataclass(frozen=True)
+class Slot:
+    """An operation whose matrix each trajectory chooses (a sampled mixture
+    unitary or a rescaled Kraus operator).  Its matrix comes from the
+    ``picks`` of a :class:`TrajectoryPoint`; it is planned as a dense op."""
+
+    op: Any
+    slot: int
+
+    @property
+    def qubits(self):
+        return self.op.qubits
+
+
+class TrajectoryPoint:
+    """A ParamResolver plus the matrices one trajectory picked for its slots."""
+
+    def __init__(self, base, picks: dict):
+        self.base = base
+        self.picks = picks
+
+    def value_of(self, value, recursive: bool = True):
+        return self.base.value_of(value, recursive)
+
+    @property
+    def param_dict(self):
+        return self.base.param_dict
+
+
+def _generic_unitary(d: int) -> np.ndarray:
+    """A fixed dense unitary (plans a slot as a dense op)."""
+    rs = np.random.RandomState(4321 + d)
+    q, _ = np.linalg.qr(rs.normal(size=(d, d)) + 1j * rs.normal(size=(d, d)))
+    return q
+
+
 @dataclasses.dataclass
 class OpSource:
     """How to produce one BitGate's matrix for a batch of resolvers."""
@@ -41,12 +77,21 @@ class OpSource:
     transform: str  # 'u' (unitary), 'conj' (conjugate unitary), 'superop'
     const: np.ndarray | None  # constant matrix (unparameterised ops)
     eigen: tuple | None  # (components [(h, P)], shift, exponent expr) for EigenGates
+    slot: int | None = None  # trajectory slot: the matrix is the resolver's pick
 
     def matrices(self, resolvers: Sequence[Any]) -> np.ndarray:
         P = len(resolvers)
         if self.const is not None:
             return np.broadcast_to(self.const, (P,) + self.const.shape)
+        if self.slot is not None:
+            d = 2 ** len(self.op.qubits)
+            mats = []
+            for r in resolvers:
+                m = getattr(r, "picks", {}).get(self.slot)
+                mats.append(_generic_unitary(d) if m is None else np.asarray(m, dtype=np.complex128))
+            return np.array(mats)
         cirq = _cirq()
+        resolvers = [getattr(r, "base", r) for r in resolvers]
         if self.eigen is not None:
             comps, shift, expr = self.eigen
             t = np.array([float(r.value_of(expr)) for r in resolvers])
@@ -176,6 +221,19 @@ class CompiledCircuit:
         self.gates: list[BitGate] = []
         self._phase_ops = [op for op in ops if not op.qubits]
         for op in ops:
+            if isinstance(op, Slot):
+                if dm:
+                    raise UnsupportedOperation("trajectory slots are state-vector only")
+                pos = [index[q] for q in op.qubits]
+                if len(pos) > 5:
+                    raise UnsupportedOperation(f"operations on more than 5 qubits are not supported: {op.op!r}")
+                src = OpSource(op, "u", None, None, slot=op.slot)
+                self.sources.append(src)
+                self.gates.append(
+                    BitGate(bits=tuple(n - 1 - p for p in reversed(pos)), matrix=None, diagonal=False,
+                            tag=len(self.sources) - 1)
+                )
+                continue
             if not op.qubits:
                 if dm:
                     continue  # a global phase cancels in rho
@@ -246,7 +304,13 @@ class CompiledCircuit:
         cirq = _cirq()
         rs = np.random.RandomState(1234)
         syms = sorted(
-            {s for src in self.sources if src.const is None for s in cirq.parameter_symbols(src.op)}, key=str
+            {
+                s
+                for src in self.sources
+                if src.const is None and src.slot is None
+                for s in cirq.parameter_symbols(src.op)
+            },
+            key=str,
         )
         generic = [cirq.ParamResolver({s: float(rs.uniform(0.1, 0.9)) for s in syms}) for _ in range(2)]
         keep = []

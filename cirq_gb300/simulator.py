@@ -16,9 +16,9 @@ fallback.  Differences from the reference, by design:
 
 * arithmetic is complex64 only (``dtype=np.complex64``, the reference's
   default); other dtypes raise ``ValueError``;
-* measurements must be terminal (mid-circuit measurement and state-vector
-  noise need per-repetition trajectories) -- other circuits raise
-  ``NotImplementedError``;
+* mid-circuit measurement and state-vector noise run as per-repetition
+  trajectories (``cirq_gb300/trajectories.py``), as the reference's ``_run``
+  does; samples are statistically, not bit-for-bit, equal to the reference's;
 * ``split_untangled_states`` is accepted and ignored: the reference's
   product-state factoring (``cirq-core/cirq/sim/simulation_product_state.py``)
   changes no result, only its CPU cost.
@@ -37,6 +37,7 @@ from cirq_gb300.engine import Engine, default_engine
 from cirq_gb300.ir import pauli_terms
 from cirq_gb300.planner import Planner
 from cirq_gb300.program import CompiledCircuit, split_measurements, structure_key
+from cirq_gb300 import trajectories as _traj
 
 cirq = ensure_cirq()
 
@@ -224,6 +225,78 @@ class _GpuSimulatorBase:
             out[key] = arr
         return out
 
+    def _measure_op(self, state, compiled, op) -> list:
+        """One shot of one measurement with collapse (a mid-circuit measurement,
+        cirq-core/cirq/sim/state_vector.py:235-322 and
+        cirq-core/cirq/sim/density_matrix_utils.py:97-183); returns the
+        recorded bits (invert mask and confusion map applied)."""
+        eng = self.engine
+        n = compiled.n
+        index = {q: i for i, q in enumerate(compiled.qubits)}
+        idx = int(eng.sample(state, n, self._prng.random_sample(1), dm=self._dm)[0])
+        mask = 0
+        for q in op.qubits:
+            mask |= 1 << (n - 1 - index[q])
+        value = idx & mask
+        if self._dm:
+            eng.project(state, compiled.nbits, mask | (mask << n), value | (value << n), 1.0)
+            p = float(eng.probabilities(state, n, dm=True).astype(np.float64).sum())
+            if p > 0:
+                eng.scale(state, compiled.nbits, 1.0 / p)
+        else:
+            eng.project(state, n, mask, value, 1.0)
+            p = eng.norm2(state, n)
+            if p > 0:
+                eng.scale(state, n, 1.0 / math.sqrt(p))
+        gate = op.gate
+        inv = gate.full_invert_mask()
+        bits = np.array([[(idx >> (n - 1 - index[q])) & 1 for q in op.qubits]], dtype=np.int8)
+        for i in range(bits.shape[1]):
+            if inv[i]:
+                bits[0, i] ^= 1
+        if gate.confusion_map:
+            _confuse(bits, op.qubits, gate.confusion_map, self._prng)
+        return [int(b) for b in bits[0]]
+
+    def _traj_needed(self, program) -> bool:
+        """Does this circuit need per-repetition trajectories?"""
+        from cirq_gb300.ir import flatten_ops
+
+        if not program.all_qubits():
+            return False
+        if not self._dm and self.noise is not cirq.NO_NOISE:
+            return True
+        return _traj.needs_trajectories(flatten_ops(program), self._dm)
+
+    def _traj_states(self, program, qubits, resolver, initial_state, reps):
+        """Yields (runner, device state, records) for `reps` trajectories; the
+        state is the runner's buffer, valid until the next trajectory."""
+        ops = _traj.circuit_ops(self, program, qubits, resolver)
+        runner = _traj.TrajectoryRunner(self, ops, qubits, resolver)
+        try:
+            picks, pools = runner.prepare(reps)
+            for r in range(reps):
+                state, records = runner.run(initial_state, picks[r], pools, r)
+                yield runner, _Borrowed(state), records
+        finally:
+            runner.close()
+
+    def _traj_expectations(self, program, pslist, params, qubit_order, initial_state):
+        qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+        index = {q: i for i, q in enumerate(qubits)}
+        for ps in pslist:
+            for q in ps.qubits:
+                if q not in index:
+                    raise ValueError(f"Qubit {q} of the observable is not in the qubit order")
+        terms = [pauli_terms(ps, index, len(qubits)) for ps in pslist]
+        eng = self.engine
+        for r in cirq.to_resolvers(params):
+            _check_all_resolved(program, r)
+            for runner, state, _rec in self._traj_states(program, qubits, r, initial_state, 1):
+                out = [complex(np.sum(eng.expect_paulis(state, runner.n, t, dm=self._dm))) for t in terms]
+                state.free()
+                yield out
+
     def _sample_records(self, state, compiled, meas_ops, repetitions) -> dict[str, np.ndarray]:
         """Terminal-measurement sampling, mirroring StepResult.sample_measurement_ops
         (cirq-core/cirq/sim/simulator.py:733-820) with _allow_repeated=True."""
@@ -251,6 +324,12 @@ class _GpuSimulatorBase:
         param_resolver = param_resolver or cirq.ParamResolver({})
         _check_all_resolved(circuit, param_resolver)
         qubits = tuple(sorted(circuit.all_qubits()))
+        if self._traj_needed(circuit):
+            per_rep = []
+            for _, state, rec in self._traj_states(circuit, qubits, param_resolver, 0, repetitions):
+                state.free()
+                per_rep.append(rec)
+            return _traj.pad_records(per_rep)
         _, resolvers, compiled, meas = self._prepare(circuit, qubits, param_resolver)
         if compiled.n == 0:
             return {op.gate.key: np.zeros((repetitions, 1, 0), dtype=np.int8) for op in meas}
@@ -362,6 +441,18 @@ class Simulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.StateVectorTrialResult]:
+        if self._traj_needed(program):
+            qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+            eng = self.engine
+            for r in cirq.to_resolvers(params):
+                _check_all_resolved(program, r)
+                for runner, state, rec in self._traj_states(program, qubits, r, initial_state, 1):
+                    eng.final_renormalize(state, runner.n)
+                    vec = eng.download_state(state, runner.n)
+                    state.free()
+                    meas = {k: np.array(v[-1], dtype=np.uint8) for k, v in rec.items()}
+                    yield _state_vector_result(r, meas, qubits, vec)
+            return
         qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
         for r in resolvers:
             _check_all_resolved(program, r)
@@ -407,6 +498,11 @@ class Simulator(
                     "Cannot compute expectation value of a non-Hermitian "
                     f"PauliString <{ps}>. Coefficient must be real."
                 )
+        if self._traj_needed(program) or program.has_measurements():
+            # the reference evaluates the final state of simulate(), which
+            # collapses measurements: one trajectory per point
+            yield from self._traj_expectations(program, pslist, params, qubit_order, initial_state)
+            return
         body_prog = cirq.Circuit(op for op in program.all_operations() if not cirq.is_measurement(op))
         qubits, resolvers, compiled, _ = self._prepare(body_prog, qubit_order, params)
         index = {q: i for i, q in enumerate(qubits)}
@@ -478,6 +574,18 @@ class DensityMatrixSimulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.DensityMatrixTrialResult]:
+        if self._traj_needed(program):
+            qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+            eng = self.engine
+            for r in cirq.to_resolvers(params):
+                _check_all_resolved(program, r)
+                for runner, state, rec in self._traj_states(program, qubits, r, initial_state, 1):
+                    n = runner.n
+                    rho = eng.download_state(state, 2 * n).reshape(2**n, 2**n)
+                    state.free()
+                    meas = {k: np.array(v[-1], dtype=np.uint8) for k, v in rec.items()}
+                    yield _density_matrix_result(r, meas, qubits, rho)
+            return
         qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
         for r in resolvers:
             _check_all_resolved(program, r)
@@ -517,6 +625,9 @@ class DensityMatrixSimulator(
         if not isinstance(observables, list):
             observables = [observables]
         pslist = [cirq.PauliSum.wrap(o) for o in observables]
+        if self._traj_needed(program) or program.has_measurements():
+            yield from self._traj_expectations(program, pslist, params, qubit_order, initial_state)
+            return
         body_prog = cirq.Circuit(op for op in program.all_operations() if not cirq.is_measurement(op))
         qubits, resolvers, compiled, _ = self._prepare(body_prog, qubit_order, params)
         index = {q: i for i, q in enumerate(qubits)}

@@ -87,11 +87,11 @@ def test_simulate_with_terminal_measurement_collapses():
         np.testing.assert_allclose(r.final_state_vector, want, atol=1e-6)
 
 
-def test_mid_circuit_measurement_is_rejected_loudly():
+def test_mid_circuit_measurement_runs_per_repetition():
     q0 = cirq.LineQubit(0)
     c = cirq.Circuit(cirq.measure(q0, key="a"), cirq.X(q0), cirq.measure(q0, key="b"))
-    with pytest.raises(NotImplementedError):
-        cirq_gb300.Simulator().run(c, repetitions=3)
+    res = cirq_gb300.Simulator().run(c, repetitions=3)
+    assert res.records["a"].tolist() == [[[0]]] * 3 and res.records["b"].tolist() == [[[1]]] * 3
 
 
 def test_large_state_sampling_chi2_marginal():

@@ -1,0 +1,187 @@
+"""Mid-circuit measurement and state-vector noise as GPU trajectories,
+checked statistically against exact distributions from the oracle."""
+
+import itertools
+
+import numpy as np
+import pytest
+import scipy.stats
+
+import cirq
+import cirq_gb300
+from cirq_gb300.ir import flatten_ops
+from oracle.circuits import simulate_density_matrix
+from oracle.statevector import apply_matrix
+
+pytestmark = pytest.mark.gpu
+
+
+def _pvalue(counts: dict, probs: dict, reps: int) -> float:
+    keys = sorted(set(probs) | set(counts))
+    obs = np.array([counts.get(k, 0) for k in keys], dtype=float)
+    exp = np.array([probs.get(k, 0.0) for k in keys]) * reps
+    assert obs[exp == 0].sum() == 0, "outcome with probability 0 was sampled"
+    keep = exp > 0
+    return scipy.stats.chisquare(obs[keep], exp[keep]).pvalue
+
+
+def _record_distribution(circuit, qubits):
+    """Exact joint distribution of every measurement record, by enumerating
+    the branches of each measurement on the oracle's state vector."""
+    n = len(qubits)
+    index = {q: i for i, q in enumerate(qubits)}
+    ops = flatten_ops(circuit)
+    out: dict = {}
+
+    def rec(i, psi, p, bits):
+        if p < 1e-14:
+            return
+        if i == len(ops):
+            out[tuple(bits)] = out.get(tuple(bits), 0.0) + p
+            return
+        op = ops[i]
+        axes = [index[q] for q in op.qubits]
+        if cirq.is_measurement(op):
+            inv = op.gate.full_invert_mask()
+            for outcome in itertools.product([0, 1], repeat=len(axes)):
+                sl = [slice(None)] * n
+                for a, b in zip(axes, outcome):
+                    sl[a] = b
+                proj = np.zeros_like(psi)
+                proj[tuple(sl)] = psi[tuple(sl)]
+                pr = float(np.sum(np.abs(proj) ** 2))
+                if pr > 1e-14:
+                    rb = [b ^ int(v) for b, v in zip(outcome, inv)]
+                    rec(i + 1, proj / np.sqrt(pr), p * pr, bits + rb)
+        else:
+            rec(i + 1, apply_matrix(psi, axes, cirq.unitary(op)), p, bits)
+
+    psi0 = np.zeros((2,) * n, dtype=np.complex128)
+    psi0[(0,) * n] = 1
+    rec(0, psi0, 1.0, [])
+    return out
+
+
+def _counts(result, keys):
+    recs = [result.records[k] for k in keys]  # (R, instances, bits)
+    counts: dict = {}
+    for r in range(recs[0].shape[0]):
+        key = tuple(int(b) for rr in recs for b in rr[r].reshape(-1))
+        counts[key] = counts.get(key, 0) + 1
+    return counts
+
+
+def test_mid_circuit_measurements_chi2():
+    q = cirq.LineQubit.range(3)
+    c = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.CNOT(q[0], q[1]),
+        cirq.ry(0.7).on(q[2]),
+        cirq.measure(q[0], key="a"),
+        cirq.H(q[1]),
+        cirq.CZ(q[1], q[2]),
+        cirq.measure(q[1], q[2], key="b", invert_mask=(True,)),
+        cirq.rx(1.1).on(q[0]),
+        cirq.measure(q[0], key="c"),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    probs = _record_distribution(c, q)
+    reps = 4000
+    res = cirq_gb300.Simulator(seed=5).run(c, repetitions=reps)
+    assert res.records["b"].shape == (reps, 1, 2)
+    assert _pvalue(_counts(res, ["a", "b", "c"]), probs, reps) > 1e-3
+
+
+def test_repeated_key_and_deterministic_outcomes():
+    q = cirq.LineQubit.range(2)
+    c = cirq.Circuit(
+        cirq.X(q[0]),
+        cirq.measure(q[0], key="m"),
+        cirq.CNOT(q[0], q[1]),
+        cirq.measure(q[1], key="m"),
+        cirq.X(q[0]),
+        cirq.measure(q[0], key="z"),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    res = cirq_gb300.Simulator(seed=1).run(c, repetitions=50)
+    assert res.records["m"].shape == (50, 2, 1)
+    assert np.all(res.records["m"] == 1) and np.all(res.records["z"] == 0)
+
+
+def test_noisy_state_vector_matches_density_matrix_distribution():
+    q = cirq.LineQubit.range(3)
+    body = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.depolarize(0.15).on(q[0]),
+        cirq.CNOT(q[0], q[1]),
+        cirq.bit_flip(0.1).on(q[1]),
+        cirq.ry(0.9).on(q[2]),
+        cirq.amplitude_damp(0.3).on(q[2]),
+        cirq.CZ(q[1], q[2]),
+        cirq.phase_damp(0.4).on(q[1]),
+        cirq.H(q[1]),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    rho = simulate_density_matrix(body, qubit_order=q)
+    p = np.clip(np.real(np.diag(rho)), 0, None)
+    probs = {tuple((i >> (2 - j)) & 1 for j in range(3)): p[i] for i in range(8)}
+    reps = 5000
+    res = cirq_gb300.Simulator(seed=7).run(body + cirq.measure(*q, key="m"), repetitions=reps)
+    assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
+
+
+def test_noise_model_trajectories_match_density_matrix():
+    q = cirq.LineQubit.range(2)
+    body = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(q[0], q[1]), cirq.rx(0.6).on(q[1]))
+    noise = cirq.ConstantQubitNoiseModel(cirq.amplitude_damp(0.2))
+    rho = simulate_density_matrix(body, qubit_order=q, noise=noise)
+    p = np.clip(np.real(np.diag(rho)), 0, None)
+    probs = {((i >> 1) & 1, i & 1): p[i] for i in range(4)}
+    reps = 4000
+    res = cirq_gb300.Simulator(noise=noise, seed=3).run(body + cirq.measure(*q, key="m"), repetitions=reps)
+    assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
+
+
+def test_amplitude_damping_decay_rate():
+    q = cirq.LineQubit(0)
+    c = cirq.Circuit(cirq.X(q), cirq.amplitude_damp(0.3).on(q), cirq.measure(q, key="m"))
+    reps = 4000
+    ones = int(cirq_gb300.Simulator(seed=11).run(c, repetitions=reps).records["m"].sum())
+    assert scipy.stats.binomtest(ones, reps, 0.7).pvalue > 1e-3
+
+
+def test_simulate_returns_one_normalised_trajectory():
+    q = cirq.LineQubit.range(4)
+    c = cirq.Circuit([cirq.H.on_each(*q), cirq.amplitude_damp(0.5).on_each(*q), cirq.CNOT(q[0], q[3])])
+    res = cirq_gb300.Simulator(seed=2).simulate(c, qubit_order=q)
+    assert abs(np.linalg.norm(res.final_state_vector) - 1) < 1e-5
+
+
+def test_density_matrix_mid_circuit_measurement():
+    q = cirq.LineQubit.range(2)
+    c = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.measure(q[0], key="a"),
+        cirq.CNOT(q[0], q[1]),
+        cirq.measure(q[1], key="b"),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    sim = cirq_gb300.DensityMatrixSimulator(seed=4)
+    res = sim.run(c, repetitions=400)
+    a, b = res.records["a"][:, 0, 0], res.records["b"][:, 0, 0]
+    assert np.array_equal(a, b) and 100 < a.sum() < 300
+    out = sim.simulate(c, qubit_order=q)
+    rho = out.final_density_matrix
+    bit = int(out.measurements["a"][0])
+    expect = np.zeros((4, 4))
+    expect[3 * bit, 3 * bit] = 1
+    assert np.allclose(rho, expect, atol=1e-6)
+
+
+def test_expectation_with_terminal_measurement_uses_the_collapsed_state():
+    q = cirq.LineQubit.range(2)
+    c = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(q[0], q[1]), cirq.measure(q[0], key="m"))
+    obs = [cirq.Z(q[1]), cirq.X(q[0])]
+    for sim in (cirq_gb300.Simulator(seed=9), cirq_gb300.DensityMatrixSimulator(seed=9)):
+        vals = sim.simulate_expectation_values(c, obs, permit_terminal_measurements=True)
+        assert abs(abs(vals[0]) - 1) < 1e-5 and abs(vals[1]) < 1e-5

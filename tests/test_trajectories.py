@@ -1,0 +1,77 @@
+"""Trajectory planning (mid-circuit measurement, state-vector noise): host
+logic only, no GPU."""
+
+import numpy as np
+
+import cirq
+from cirq_gb300 import trajectories as tj
+from cirq_gb300.ir import flatten_ops
+from cirq_gb300.planner import Planner
+from cirq_gb300.program import CompiledCircuit, Slot, TrajectoryPoint
+from emulator import run_program
+
+
+def _ops(c):
+    return flatten_ops(c)
+
+
+def test_needs_trajectories():
+    q = cirq.LineQubit.range(2)
+    terminal = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q), cirq.measure(*q, key="m"))
+    mid = cirq.Circuit(cirq.H(q[0]), cirq.measure(q[0], key="a"), cirq.H(q[0]), cirq.measure(q[0], key="b"))
+    noisy = cirq.Circuit(cirq.X(q[0]), cirq.amplitude_damp(0.1)(q[0]), cirq.measure(q[0], key="m"))
+    assert not tj.needs_trajectories(_ops(terminal), dm=False)
+    assert tj.needs_trajectories(_ops(mid), dm=False)
+    assert tj.needs_trajectories(_ops(mid), dm=True)
+    assert tj.needs_trajectories(_ops(noisy), dm=False)
+    assert not tj.needs_trajectories(_ops(noisy), dm=True)
+
+
+def test_build_items_splits_at_events_and_keeps_mixtures_fused():
+    q = cirq.LineQubit.range(3)
+    c = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.depolarize(0.1)(q[0]),  # mixture: a slot inside the segment
+        cirq.CNOT(q[0], q[1]),
+        cirq.measure(q[1], key="a"),
+        cirq.amplitude_damp(0.2)(q[2]),  # general channel: an event
+        cirq.X(q[2]),
+        cirq.measure(q[2], key="b"),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    items, nslot = tj.build_items(_ops(c), dm=False)
+    kinds = [type(it).__name__ for it in items]
+    assert kinds == ["Segment", "Measure", "Channel", "Segment", "Measure"]
+    assert nslot == 2
+    seg = items[0]
+    assert any(isinstance(op, Slot) for op in seg.ops) and len(seg.slots) == 1
+    # density matrices keep every channel in the segments
+    items_dm, nslot_dm = tj.build_items(_ops(c), dm=True)
+    assert [type(it).__name__ for it in items_dm] == ["Segment", "Measure", "Segment", "Measure"]
+    assert nslot_dm == 0
+
+
+def test_slot_pool_follows_the_picks():
+    """A slot is planned as a dense op and takes each point's picked matrix."""
+    q = cirq.LineQubit.range(3)
+    dep = cirq.depolarize(0.3)(q[1])
+    ops = [cirq.H(q[0]), Slot(dep, 0), cirq.CNOT(q[0], q[2])]
+    cc = CompiledCircuit(ops, q, dm=False, planner=Planner(tile_bits=10), resolvers=[cirq.ParamResolver({})])
+    probs, unitaries = zip(*cirq.mixture(dep))
+    n = cc.nbits_dev
+    for i, u in enumerate(unitaries):
+        pool = cc.pool([TrajectoryPoint(cirq.ParamResolver({}), {0: u})])[0]
+        psi0 = np.zeros(2**n, complex)
+        psi0[0] = 1
+        out = run_program(psi0, n, cc.plan.passes, cc.plan.ops, pool.astype(np.complex128))[:8]
+        ref = cirq.final_state_vector(cirq.Circuit(cirq.H(q[0]), cirq.MatrixGate(u)(q[1]), cirq.CNOT(q[0], q[2])),
+                                      qubit_order=q)
+        assert np.allclose(out, ref, atol=1e-6), i
+
+
+def test_pad_records_matches_reference_layout():
+    recs = [{"a": [[1, 0]], "b": [[1]]}, {"a": [[0, 1], [1, 1]]}]
+    out = tj.pad_records(recs)
+    assert out["a"].shape == (2, 2, 2) and out["a"].dtype == np.uint8
+    assert out["a"][0, 0].tolist() == [1, 0] and out["a"][0, 1].tolist() == [0, 0]
+    assert out["b"].shape == (2, 1, 1) and out["b"][1, 0, 0] == 0
