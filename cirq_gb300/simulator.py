@@ -281,6 +281,21 @@ class _GpuSimulatorBase:
         finally:
             runner.close()
 
+    # ---- SimulatesIntermediateState ------------------------------------------
+    def simulate_moment_steps(
+        self,
+        circuit: cirq.AbstractCircuit,
+        param_resolver: cirq.ParamResolverOrSimilarType = None,
+        qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+        initial_state: Any = None,
+    ):
+        """One step result per (noisy) moment, as
+        ``SimulatesIntermediateState.simulate_moment_steps``
+        (cirq-core/cirq/sim/simulator.py:607-640); see cirq_gb300/steps.py."""
+        from cirq_gb300.steps import moment_steps
+
+        return moment_steps(self, circuit, param_resolver, qubit_order, initial_state)
+
     def _traj_expectations(self, program, pslist, params, qubit_order, initial_state):
         qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
         index = {q: i for i, q in enumerate(qubits)}

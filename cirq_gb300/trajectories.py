@@ -221,12 +221,16 @@ class TrajectoryRunner:
         The state buffer belongs to the runner and is reused by the next
         trajectory."""
         sim = self.sim
-        eng = sim.engine
         if self._state is None:
             self._state = sim._initial_device_state(self.empty, initial_state)
         else:
             sim._initial_device_state(self.empty, initial_state, into=self._state)
-        state = self._state
+        return self._state, self.apply(self._state, picks, pools, rep)
+
+    def apply(self, state, picks: dict, pools: list, rep: int) -> dict:
+        """Applies the items to a device state in place; returns the records."""
+        sim = self.sim
+        eng = sim.engine
         records: dict = {}
         for j, it in enumerate(self.items):
             if isinstance(it, Segment):
@@ -239,7 +243,7 @@ class TrajectoryRunner:
                 records.setdefault(cirq.measurement_key_name(it.op), []).append(bits)
             else:
                 self._apply_kraus(state, it, picks)
-        return state, records
+        return records
 
     def _apply_kraus(self, state, it: Channel, picks: dict) -> None:
         eng = self.sim.engine

@@ -185,3 +185,43 @@ def test_expectation_with_terminal_measurement_uses_the_collapsed_state():
     for sim in (cirq_gb300.Simulator(seed=9), cirq_gb300.DensityMatrixSimulator(seed=9)):
         vals = sim.simulate_expectation_values(c, obs, permit_terminal_measurements=True)
         assert abs(abs(vals[0]) - 1) < 1e-5 and abs(vals[1]) < 1e-5
+
+
+def test_moment_steps_match_the_oracle_after_every_moment():
+    from oracle.circuits import simulate_state_vector
+    from cirq_gb300 import workloads
+
+    c = workloads.random_layer_circuit(6, 4, seed=21)
+    q = sorted(c.all_qubits())
+    sim = cirq_gb300.Simulator(seed=1)
+    steps = list(sim.simulate_moment_steps(c, qubit_order=q))
+    assert len(steps) == len(c)
+    for i, _ in enumerate(c):
+        pass
+    for i, step in enumerate(sim.simulate_moment_steps(c, qubit_order=q)):
+        want = simulate_state_vector(c[: i + 1], qubit_order=q)
+        assert np.abs(step.state_vector(copy=True) - want).max() < 1e-5
+        if i == len(c) - 1:
+            samples = step.sample(q[:2], repetitions=2000, seed=3)
+            assert samples.shape == (2000, 2) and samples.dtype == np.uint8
+            p = np.abs(want.reshape(4, -1)) ** 2
+            probs = {(a >> 1 & 1, a & 1): float(p[a].sum()) for a in range(4)}
+            counts: dict = {}
+            for row in samples:
+                counts[tuple(int(x) for x in row)] = counts.get(tuple(int(x) for x in row), 0) + 1
+            assert _pvalue(counts, probs, 2000) > 1e-3
+
+
+def test_moment_steps_with_measurements_and_density_matrix():
+    q = cirq.LineQubit.range(2)
+    c = cirq.Circuit(cirq.X(q[0]), cirq.measure(q[0], key="a"), cirq.CNOT(q[0], q[1]), cirq.measure(q[1], key="b"))
+    steps = list(cirq_gb300.Simulator(seed=1).simulate_moment_steps(c))
+    assert [dict(s.measurements) for s in steps][1]["a"].tolist() == [1]
+    dm_steps = cirq_gb300.DensityMatrixSimulator(seed=1, noise=cirq.amplitude_damp(0.25)).simulate_moment_steps(
+        cirq.Circuit(cirq.X(q[0]), cirq.X(q[1]))
+    )
+    last = None
+    for s in dm_steps:
+        last = s.density_matrix()
+    assert abs(np.trace(last) - 1) < 1e-5
+    assert abs(np.real(last[3, 3]) - 0.75**2) < 1e-5
