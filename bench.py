@@ -11,7 +11,7 @@ Printed JSON line (rank 0):
   e2e        the same metric through cirq_gb300.Simulator.simulate() -- circuit
              in, final state vector out in host memory (H2D of the matrix pool
              and D2H of the 8 GiB state inside the timed region)
-  roofline   dominant kernel k_tile_pass: algorithmic bytes per launch
+  roofline   dominant kernel k_tile_ws: algorithmic bytes per launch
              (16 B x 2^30: one read + one write of the state) / mean launch time
   cpu_baseline  the reference's numpy cirq.Simulator on a bounded gate sample
   fusion_sweep  gate-updates/s for fusion width k = 1..5
@@ -389,6 +389,57 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
     }
 
 
+def mma_bench(n: int = 30, reps: int = 3):
+    """Tensor-core evaluation: one 11-bit-tile pass applying 1, 2 or 4
+    random 4-qubit matrices with tcgen05 MMAs (GBQ_OP_MMA, TF32 three-term
+    split) against the same program on the FP32 CUDA-core path (plain dense
+    ops), ms per pass on a 2^n state resident in HBM."""
+    from cirq_gb300 import _lib
+    from cirq_gb300.engine import Engine
+
+    eng = Engine.get(0)
+    rs = np.random.RandomState(0)
+    state = eng.alloc(8 << n)
+    check = _lib.check
+    out = {"workload": f"{n}q state, one pass, 4-qubit matrices on tile bits (3o + j) mod 11"}
+    try:
+        check(eng.lib.gbq_sv_set_basis(eng.ctx, state.ptr, n, 0))
+        for nm in (1, 2, 4):
+            ops = np.zeros(nm, dtype=_lib.OP_DTYPE)
+            pool = []
+            for o in range(nm):
+                ops[o]["kind"] = _lib.OP_MMA
+                ops[o]["k"] = 4
+                ops[o]["bits"][:4] = [(3 * o + j) % 11 for j in range(4)]
+                ops[o]["mat"] = 256 * o
+                a = rs.normal(size=(16, 16)) + 1j * rs.normal(size=(16, 16))
+                pool.append(np.linalg.qr(a)[0].astype(np.complex64).reshape(-1))
+            passes = np.zeros(1, dtype=_lib.PASS_DTYPE)
+            passes[0]["L"], passes[0]["m"], passes[0]["op_count"] = 11, 5, nm
+            passes[0]["hi"][:6] = list(range(5, 11))
+            pool_dev = eng.upload(np.concatenate(pool))
+            row = {}
+            for label, kind in (("mma_ms", _lib.OP_MMA), ("fp32_ms", _lib.OP_DENSE)):
+                ops["kind"] = kind
+
+                def one():
+                    check(eng.lib.gbq_run(eng.ctx, state.ptr, n, passes.ctypes.data, 1, ops.ctypes.data, nm,
+                                          pool_dev.ptr), "gbq_run")
+
+                one()
+                eng.event(0)
+                for _ in range(reps):
+                    one()
+                eng.event(1)
+                row[label] = eng.elapsed_ms(0, 1) / reps
+            eng.sync()
+            pool_dev.free()
+            out[f"{nm}_ops"] = row
+    finally:
+        state.free()
+    return out
+
+
 # ---------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
@@ -452,7 +503,7 @@ def main():
     alg_bytes = 16 * (1 << compiled.nbits)
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9 if pass_ms else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "tile_pass_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "tile_ws_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
@@ -491,7 +542,8 @@ def main():
 
     extra = {}
     if not args.no_extra and rank == 0:
-        for name, fn in (("adjoint", adjoint_bench), ("density_matrix", density_bench), ("batch_sweep", batch_bench)):
+        for name, fn in (("adjoint", adjoint_bench), ("density_matrix", density_bench), ("batch_sweep", batch_bench),
+                         ("tensor_core_pass", mma_bench)):
             try:
                 extra[name] = fn()
             except Exception as e:  # reported, not hidden
@@ -525,7 +577,7 @@ def main():
             },
             "hbm_frac": (achieved / peak) if achieved else None,
             "roofline": {
-                "kernel": "k_tile_pass",
+                "kernel": "k_tile_ws",
                 "bound": "hbm",
                 "achieved": achieved,
                 "peak": peak,
