@@ -962,8 +962,14 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_ws(const __grid_constant
       if (i < count) {
         const uint64_t gb = tile_base_fast(ttab, blockIdx.x + i * step);
         const float2* g = a.psi + gb + lo_l;
-#pragma unroll 8
-        for (int j = pw; j < NH; j += kWsProducers) cp_async8(sb + (lp_l ^ hphys[j]), g + hoff[j]);
+        // each producer warp refills exactly the 64-amplitude groups
+        // (tile index >> 6 = jj) whose write-back it has just read, so no
+        // warp overwrites data another warp still has to store
+#pragma unroll 4
+        for (int jj = pw; jj < NH / 2; jj += kWsProducers) {
+          cp_async8(sb + (lp_l ^ hphys[2 * jj]), g + hoff[2 * jj]);
+          cp_async8(sb + (lp_l ^ hphys[2 * jj + 1]), g + hoff[2 * jj + 1]);
+        }
         asm volatile("cp.async.mbarrier.arrive.noinc.shared.b64 [%0];\n" ::"r"(ws_su32(&full[b])) : "memory");
       }
     }

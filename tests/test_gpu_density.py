@@ -85,3 +85,16 @@ def test_dm_sampling_chi2():
     if exp[-1] == 0:
         obs, exp = obs[:-1], exp[:-1]
     assert scipy.stats.chisquare(obs, exp).pvalue > 1e-4
+
+
+def test_bench_size_noisy_density_matrix_properties():
+    """The 13-qubit noisy-layers workload (rho = 2^26 amplitudes): trace one,
+    Hermitian, positive diagonal, and the same result on a rerun."""
+    c = workloads.noisy_layer_circuit(13, 16, seed=0, p=1e-3, gamma=5e-3)
+    sim = cirq_gb300.DensityMatrixSimulator()
+    rho = sim.simulate(c).final_density_matrix
+    assert abs(np.trace(rho) - 1) < 1e-5
+    assert np.max(np.abs(rho - rho.conj().T)) < 1e-6
+    assert np.real(np.diag(rho)).min() > -1e-6
+    rho2 = sim.simulate(c).final_density_matrix
+    assert np.array_equal(rho, rho2)

@@ -95,3 +95,31 @@ def test_autotuned_simulator_matches_oracle(tmp_path, monkeypatch):
     want = simulate_state_vector(c)
     assert np.max(np.abs(got - want)) < TOL
     assert (tmp_path / "tune.json").exists()
+
+
+def _final_device_norm_and_state(sim, circuit):
+    """Runs the plan on the device and returns (norm^2 before any host-side
+    renormalisation, final state)."""
+    eng = sim.engine
+    qubits, resolvers, compiled, _ = sim._prepare(circuit, cirq.QubitOrder.DEFAULT, cirq.ParamResolver({}))
+    state = sim._evolve(compiled, compiled.pool([cirq.ParamResolver({})])[0], 0)
+    try:
+        return eng.norm2(state, compiled.n), eng.download_state(state, compiled.n, pinned=False)
+    finally:
+        state.free()
+
+
+def test_full_size_properties_26_qubits():
+    """Bench-like size (the oracle is too slow here): norm preservation over
+    a 26-qubit, depth-40 run with thousands of tiles per launch, bit-identical
+    reruns (the kernels are deterministic), and agreement with a plan of
+    13-bit tiles that runs on a different kernel."""
+    c = workloads.random_layer_circuit(26, 40, seed=0)
+    sim = cirq_gb300.Simulator()
+    n1, v1 = _final_device_norm_and_state(sim, c)
+    assert abs(n1 - 1) < 1e-5
+    n2, v2 = _final_device_norm_and_state(sim, c)
+    assert np.array_equal(v1, v2)
+    n3, v3 = _final_device_norm_and_state(cirq_gb300.Simulator(tile_bits=13), c)
+    assert abs(n3 - 1) < 1e-5
+    assert np.abs(v1 - v3).max() < 1e-5
