@@ -89,7 +89,9 @@ def simulate_expectation_values_batch(
             pool = np.concatenate([pool, np.zeros((P, 1), np.complex64)], axis=1)
             plen += 1
         pools_l.append(pool.reshape(-1))
-        flat_terms = [t for obs in job.terms for t in obs]
+        # terms of one observable with equal X masks sit next to each other,
+        # so the kernel evaluates them with one read of the state
+        flat_terms = [t for obs in job.terms for t in sorted(obs, key=lambda term: term[0])]
         slices = []
         k = 0
         for obs in job.terms:

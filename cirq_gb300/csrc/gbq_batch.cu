@@ -14,6 +14,7 @@
 namespace gbq {
 
 constexpr int kBatchTile = 12;
+constexpr int kTermGroup = 8;    // terms sharing one read of the state
 
 template <int KMAX>
 __global__ void __launch_bounds__(kThreads, 2)
@@ -91,25 +92,43 @@ __global__ void __launch_bounds__(kThreads, 2)
       cp_async_wait<0>();
       __syncthreads();
     }
-    // per term: coef_t <psi|P_t|psi>, P_t = i^ny X^x Z^zy (sign on the input index)
-    for (int t = 0; t < pt.term_count; ++t) {
-      const gbq_pauli tp = terms[pt.term_begin + t];
-      float sre = 0.f, sim = 0.f;
-      for (uint64_t i = threadIdx.x; i < dim; i += kThreads) {
-        const uint64_t j = i ^ tp.x;
-        const float2 a = psi[i], b = psi[j];
-        const float sg = (__popcll(j & tp.zy) & 1) ? -1.f : 1.f;
-        sre += sg * fmaf(a.x, b.x, a.y * b.y);
-        sim += sg * fmaf(a.x, b.y, -a.y * b.x);
+    // per term: coef_t <psi|P_t|psi>, P_t = i^ny X^x Z^zy (sign on the input
+    // index); consecutive terms with the same X mask (up to kTermGroup) share
+    // one read of the state
+    for (int t = 0; t < pt.term_count;) {
+      const gbq_pauli* tb = terms + pt.term_begin + t;
+      const uint64_t x = tb[0].x;
+      int g = 1;
+      while (t + g < pt.term_count && g < kTermGroup && tb[g].x == x) ++g;
+      uint64_t zy[kTermGroup];
+      float sre[kTermGroup], sim[kTermGroup];
+#pragma unroll
+      for (int u = 0; u < kTermGroup; ++u) {
+        zy[u] = u < g ? tb[u].zy : 0ull;
+        sre[u] = sim[u] = 0.f;
       }
-      double cr = tp.coef, ci = 0.0;
-      const int ny = tp.ny & 3;
-      if (ny == 1) { ci = cr; cr = 0.0; }
-      else if (ny == 2) { cr = -cr; }
-      else if (ny == 3) { ci = -cr; cr = 0.0; }
-      const int64_t o = 2 * ((int64_t)pt.term_begin + t);
-      cta_sum_store(cr * sre - ci * sim, out + o, red);
-      cta_sum_store(cr * sim + ci * sre, out + o + 1, red);
+      for (uint64_t i = threadIdx.x; i < dim; i += kThreads) {
+        const uint64_t j = i ^ x;
+        const float2 a = psi[i], b = psi[j];
+        const float pr = fmaf(a.x, b.x, a.y * b.y), pi = fmaf(a.x, b.y, -a.y * b.x);
+#pragma unroll
+        for (int u = 0; u < kTermGroup; ++u) {
+          const float sg = (__popcll(j & zy[u]) & 1) ? -1.f : 1.f;
+          sre[u] = fmaf(sg, pr, sre[u]);
+          sim[u] = fmaf(sg, pi, sim[u]);
+        }
+      }
+      for (int u = 0; u < g; ++u) {
+        double cr = tb[u].coef, ci = 0.0;
+        const int ny = tb[u].ny & 3;
+        if (ny == 1) { ci = cr; cr = 0.0; }
+        else if (ny == 2) { cr = -cr; }
+        else if (ny == 3) { ci = -cr; cr = 0.0; }
+        const int64_t o = 2 * ((int64_t)pt.term_begin + t + u);
+        cta_sum_store(cr * sre[u] - ci * sim[u], out + o, red);
+        cta_sum_store(cr * sim[u] + ci * sre[u], out + o + 1, red);
+      }
+      t += g;
     }
   }
 }
