@@ -195,6 +195,9 @@ SIGNATURES = {
     "gbq_sv_inner": [_P, _P, _P, _I, _P],
     "gbq_batch_expect": [_P, _P, _I, _P, _I, _P, _I, _P, _P, _I, _I, _P],
     "gbq_sv_project": [_P, _P, _I, _U64, _U64, _F],
+    "gbq_points_set_zero": [_P, _P, _I, _I],
+    "gbq_run_points": [_P, _P, _I, _I, _P, _I, _P, _I, _P, _I64],
+    "gbq_points_expect": [_P, _P, _I, _I, _P, _I, _P],
 }
 _RESTYPES = {"gbq_last_error": ctypes.c_char_p}
 

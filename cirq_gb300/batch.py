@@ -1,15 +1,22 @@
-"""Batched expectation-value sweeps: many circuits x many parameter points in one launch.
+"""Batched expectation-value sweeps: many circuits x many parameter points.
 
 ``simulate_expectation_values_batch(jobs)`` evaluates, for every job
 ``(circuit, observables, params)``, the expectation values that
 ``cirq.Simulator.simulate_expectation_values_sweep(circuit, observables, params)``
 returns (``cirq-core/cirq/sim/simulator.py:349-371`` /
 ``cirq-core/cirq/sim/sparse_simulator.py:193-218``), for all jobs and all
-points at once: each circuit is planned once, the matrices of all points are
-produced by vectorised recipe replay, and a single persistent kernel
-(``gbq_batch_expect``) lets every CTA claim points from a shared counter and
-simulate each one alone in its own scratch slot.  Jobs may have different
-widths (the "mixed-width" case); there is no synchronisation between CTAs.
+points at once: each circuit is planned once and the matrices of all points
+are produced by vectorised recipe replay.  Two execution modes:
+
+* default: the states of a job's points lie back to back in HBM and every
+  pass runs over all of them in one launch of the ordinary tile pass
+  (``gbq_run_points``), each tile reading its point's matrices; the Pauli
+  terms of every point are then summed in one launch
+  (``gbq_points_expect``).  A sweep streams through HBM like one large state.
+* ``persistent=True``: all jobs and points in a single persistent launch
+  (``gbq_batch_expect``): every CTA claims points from a shared counter and
+  simulates each one alone in its own scratch slot; jobs may have different
+  widths and no CTA ever waits for another.
 """
 
 from __future__ import annotations
@@ -63,14 +70,92 @@ class BatchJob:
         self.terms = [pauli_terms(o, index, self.n) for o in self.observables]
 
 
+def _job_terms(job):
+    """Unit-coefficient Pauli records of a job (terms of one observable with
+    equal X masks adjacent), their coefficients and per-observable slices."""
+    flat_terms = [t for obs in job.terms for t in sorted(obs, key=lambda term: term[0])]
+    slices = []
+    k = 0
+    for obs in job.terms:
+        slices.append((k, k + len(obs)))
+        k += len(obs)
+    recs = Engine.pauli_records([(x, zy, ny, 1.0) for x, zy, ny, _ in flat_terms])
+    coefs = np.array([c for *_, c in flat_terms], dtype=np.complex128)
+    return recs, coefs, slices
+
+
+def _job_pool(job) -> tuple[np.ndarray, int]:
+    """(P, even pool length) complex64 matrix pools of a job's points."""
+    pool = np.ascontiguousarray(job.compiled.pool(job.resolvers), dtype=np.complex64)
+    P, plen = pool.shape
+    if plen & 1:
+        pool = np.concatenate([pool, np.zeros((P, 1), np.complex64)], axis=1)
+        plen += 1
+    return pool, plen
+
+
+class _PointsRun:
+    """One chunk of a job's points on the device: launched asynchronously,
+    collected later (so the host can build the next job's pools meanwhile)."""
+
+    def __init__(self, eng: Engine, job, pool, plen, start, count, states):
+        c = job.compiled
+        self.eng, self.job, self.start, self.count, self.states = eng, job, start, count, states
+        self.n = c.nbits_dev
+        eng.points_set_zero(states, self.n, count)
+        self.pool_dev = eng.upload(pool[start : start + count].reshape(-1))
+        eng.run_points(states, self.n, count, c.plan, self.pool_dev, plen)
+
+    def collect(self, vals, recs, coefs, slices) -> None:
+        tv = self.eng.points_expect(self.states, self.n, self.count, recs) * coefs[None, :]
+        self.pool_dev.free()
+        for o, (a, b) in enumerate(slices):
+            vals[self.start : self.start + self.count, o] = tv[:, a:b].sum(axis=1)
+
+
+def _points_jobs(eng: Engine, jobs, budget_bytes: int) -> list[np.ndarray]:
+    """Default mode: each job's points evolved together, chunked to fit
+    `budget_bytes`; the host builds job k+1's pools while job k runs."""
+    results = []
+    nxt = _job_pool(jobs[0]) if jobs and jobs[0].resolvers else None
+    for j, job in enumerate(jobs):
+        c = job.compiled
+        n = c.nbits_dev
+        P = len(job.resolvers)
+        recs, coefs, slices = _job_terms(job)
+        vals = np.zeros((P, len(slices)), dtype=np.complex128)
+        results.append(vals)
+        if P == 0:
+            nxt = _job_pool(jobs[j + 1]) if j + 1 < len(jobs) and jobs[j + 1].resolvers else None
+            continue
+        pool, plen = nxt
+        L = int(c.plan.passes["L"].min()) if c.plan.npasses else n
+        chunk = max(1, min(P, budget_bytes // (8 << n), (1 << 24) >> max(n - L, 0)))
+        states = eng.alloc((8 << n) * chunk)
+        try:
+            for start in range(0, P, chunk):
+                run = _PointsRun(eng, job, pool, plen, start, min(chunk, P - start), states)
+                if start + chunk >= P:  # last chunk: overlap the next job's host work
+                    nxt = _job_pool(jobs[j + 1]) if j + 1 < len(jobs) and jobs[j + 1].resolvers else None
+                run.collect(vals, recs, coefs, slices)
+        finally:
+            states.free()
+    return results
+
+
 def simulate_expectation_values_batch(
-    jobs: Sequence[Any], engine: Engine | None = None
+    jobs: Sequence[Any], engine: Engine | None = None, persistent: bool = False
 ) -> list[np.ndarray]:
     """Returns, per job, a complex array (points, observables).
 
-    `jobs` holds BatchJob objects or (circuit, observables, params) tuples."""
+    `jobs` holds BatchJob objects or (circuit, observables, params) tuples;
+    `persistent` selects the single-launch mode (see the module doc)."""
     eng = engine or default_engine()
     jobs = [j if isinstance(j, BatchJob) else BatchJob(*j) for j in jobs]
+    if not persistent:
+        _, free, _ = eng.device_info()
+        budget = max(1 << 28, min(int(free) // 2, 64 << 30))
+        return _points_jobs(eng, jobs, budget)
     passes_l, ops_l, pools_l, terms_l, points_l = [], [], [], [], []
     npass = nop = 0
     mat_off = 0

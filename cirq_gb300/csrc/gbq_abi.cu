@@ -960,6 +960,76 @@ int gbq_sv_apply_paulisum(gbq_ctx* c, const gbq_c64* psi, int nbits, const gbq_p
   return sync(c, "gbq_sv_apply_paulisum");
 }
 
+int gbq_points_set_zero(gbq_ctx* c, gbq_c64* states, int nbits, int npoints) {
+  CHECK_CTX(c);
+  if (!states || nbits < 1 || nbits > 34 || npoints < 1) return arg_fail("gbq_points_set_zero: bad arguments");
+  return points_set_zero(c, reinterpret_cast<float2*>(states), nbits, npoints);
+}
+
+int gbq_run_points(gbq_ctx* c, gbq_c64* states, int nbits, int npoints, const gbq_pass* passes, int npasses,
+                   const gbq_op* ops, int nops, const gbq_c64* mats, int64_t pool_stride) {
+  CHECK_CTX(c);
+  if (!states || nbits < 1 || nbits > 34 || npoints < 1) return arg_fail("gbq_run_points: bad states");
+  if (npasses < 0 || (npasses && (!passes || !ops || !mats))) return arg_fail("gbq_run_points: null program");
+  if (pool_stride < 0 || (pool_stride & 1)) return arg_fail("gbq_run_points: pool_stride must be even and >= 0");
+  int pbits = 0;
+  while ((1 << pbits) < npoints) ++pbits;
+  PassArgs a;
+  MmaArgs ma;
+  for (int q = 0; q < npasses; ++q) {
+    bool mma = false;
+    int rc = convert_pass(passes[q], ops, nops, nbits, false, a, ma, mma);
+    if (rc) return rc;
+    if (mma) return arg_fail("gbq_run_points: tensor-core passes run on one state only");
+    const int L = passes[q].L;
+    if (((int64_t)npoints << (nbits - L)) > ((int64_t)1 << 24))
+      return arg_fail("gbq_run_points: more than 2^24 tiles per pass; split the points");
+    // widen the pass to the index space of all points: the point index is
+    // the top global bits, above the state's own nbits
+    const int nnt = nbits - L;
+    for (int b = 0; b < pbits; ++b) a.ti.nt[nnt + b] = (int8_t)(nbits + b);
+    a.ti.nbits = nbits + pbits;
+    a.ti.ntiles = (int64_t)npoints << nnt;
+    a.ti.pshift = nbits;
+    a.ti.pstride = pool_stride;
+    a.ti.mats = reinterpret_cast<const float2*>(mats);
+    a.ti.partial = nullptr;
+    a.psi = reinterpret_cast<float2*>(states);
+    a.lam = nullptr;
+    a.abort = c->d_abort;
+    c->abort_armed = true;
+    rc = launch_pass(c, a, false);
+    if (rc) return rc;
+  }
+  return GBQ_OK;
+}
+
+int gbq_points_expect(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const gbq_pauli* terms,
+                      int nterms, double* out) {
+  CHECK_CTX(c);
+  if (!states || nbits < 1 || nbits > 34 || npoints < 1 || nterms < 0 || (nterms && (!terms || !out)))
+    return arg_fail("gbq_points_expect: bad arguments");
+  if (nterms == 0) return GBQ_OK;
+  int rc = validate_terms(terms, nterms, nbits);
+  if (rc) return rc;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_terms = al((size_t)nterms * sizeof(gbq_pauli));
+  const size_t b_out = (size_t)npoints * nterms * 2 * sizeof(double);
+  rc = ensure_scratch(c, b_terms + b_out);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(base);
+  double* d_out = reinterpret_cast<double*>(base + b_terms);
+  cudaError_t e = cudaMemcpyAsync(d_terms, terms, (size_t)nterms * sizeof(gbq_pauli), cudaMemcpyHostToDevice,
+                                  c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
+  rc = points_expect(c, reinterpret_cast<const float2*>(states), nbits, npoints, d_terms, nterms, d_out);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(out)");
+  return sync(c, "gbq_points_expect");
+}
+
 int gbq_sv_inner(gbq_ctx* c, const gbq_c64* a, const gbq_c64* b, int nbits, double* out) {
   CHECK_CTX(c);
   if (!a || !b || !out || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_inner: bad arguments");

@@ -47,6 +47,8 @@ __global__ void __launch_bounds__(kThreads, 2)
       if (threadIdx.x == 0) {
         ti.mats = mats + pt.mat_base;
         ti.partial = nullptr;
+        ti.pstride = 0;
+        ti.pshift = 0;
         ti.nbits = pt.nbits;
         ti.L = ps.L;
         ti.m = ps.m;

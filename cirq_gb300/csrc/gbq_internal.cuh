@@ -75,6 +75,12 @@ struct TileInfo {
   int32_t nops;
   uint64_t gw[GBQ_MAX_TILE_BITS];  // global weight (1 << global bit) of each tile bit
   int8_t nt[64];                   // global bits not in the tile, ascending
+  // Batched points (gbq_run_points): the states of several points lie back
+  // to back as one wider index space; point (global index >> pshift) uses
+  // the matrices at mats + point * pstride.  pstride = 0: a single state.
+  int64_t pstride;
+  int32_t pshift;
+  int32_t pad;
 };
 
 // Kernel arguments of one tile pass, passed by value (__grid_constant__).
@@ -154,6 +160,9 @@ int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
 int build_mma_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInfo& ti, uint64_t inmask,
                    MmaArgs& A);
 int launch_mma_pass(Ctx* c, const MmaArgs& a);
+int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
+int points_expect(Ctx* c, const float2* states, int nbits, int npoints, const gbq_pauli* d_terms, int nterms,
+                  double* d_out);
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,
                  const OpDev* d_ops, const float2* mats, const gbq_pauli* d_terms, int max_nbits,
                  float2* slots, int nslots, int* d_counter, double* d_out, int kmax);

@@ -1,0 +1,121 @@
+// Batched points: the states of many parameter points of one compiled circuit
+// lie back to back (point p at states + p * 2^nbits) and are evolved pass by
+// pass together -- one launch of the ordinary tile pass per pass covers every
+// point (gbq_run_points in gbq_abi.cu) -- so a sweep streams through HBM as
+// one large state instead of one CTA per point.  This file holds the two
+// per-point kernels around it: |0...0> initialisation and Pauli-term sums.
+//
+// Replaces the per-resolver loop of SimulatesIntermediateState.simulate_sweep_iter
+// (cirq-core/cirq/sim/simulator.py:558-605) feeding
+// Simulator.simulate_expectation_values_sweep_iter
+// (cirq-core/cirq/sim/sparse_simulator.py:193-218).
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbq_internal.cuh"
+
+namespace gbq {
+
+namespace {
+
+constexpr int kPtThreads = 256;
+constexpr int kPtGroup = 8;  // terms sharing one read of the state
+
+__global__ void k_points_basis(float2* __restrict__ states, int nbits, int npoints) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < npoints) states[(int64_t)p << nbits] = make_float2(1.f, 0.f);
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kPtThreads / 32; ++w) r += red[w];
+  return r;
+}
+
+// Block (chunk c, point p) adds its part of <psi_p|P_t|psi_p> (unit
+// coefficient, P_t = i^ny X^x Z^zy with the sign on the input index) to
+// out[(p * nterms + t) * 2 + {re, im}].  Terms with equal X masks must be
+// adjacent: up to kPtGroup of them share one read of the chunk.
+__global__ void __launch_bounds__(kPtThreads) k_points_expect(const float2* __restrict__ states, int nbits,
+                                                             int chunk_bits, const gbq_pauli* __restrict__ terms,
+                                                             int nterms, double* __restrict__ out) {
+  __shared__ double red[kPtThreads / 32];
+  const int p = blockIdx.y;
+  const float2* psi = states + ((int64_t)p << nbits);
+  const uint64_t lo = (uint64_t)blockIdx.x << chunk_bits, hi = lo + (1ull << chunk_bits);
+  for (int t = 0; t < nterms;) {
+    const uint64_t x = terms[t].x;
+    int g = 1;
+    while (t + g < nterms && g < kPtGroup && terms[t + g].x == x) ++g;
+    uint64_t zy[kPtGroup];
+    float sre[kPtGroup], sim[kPtGroup];
+#pragma unroll
+    for (int u = 0; u < kPtGroup; ++u) {
+      zy[u] = u < g ? terms[t + u].zy : 0ull;
+      sre[u] = sim[u] = 0.f;
+    }
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += kPtThreads) {
+      const uint64_t j = i ^ x;
+      const float2 a = psi[i], b = psi[j];
+      const float pr = fmaf(a.x, b.x, a.y * b.y), pi = fmaf(a.x, b.y, -a.y * b.x);
+#pragma unroll
+      for (int u = 0; u < kPtGroup; ++u) {
+        const float sg = (__popcll(j & zy[u]) & 1) ? -1.f : 1.f;
+        sre[u] = fmaf(sg, pr, sre[u]);
+        sim[u] = fmaf(sg, pi, sim[u]);
+      }
+    }
+    for (int u = 0; u < g; ++u) {
+      const double r = block_sum((double)sre[u], red);
+      const double m = block_sum((double)sim[u], red);
+      if (threadIdx.x == 0) {
+        // i^ny phase of the term
+        double re = r, im = m;
+        const int ny = terms[t + u].ny & 3;
+        if (ny == 1) { re = -m; im = r; }
+        else if (ny == 2) { re = -r; im = -m; }
+        else if (ny == 3) { re = m; im = -r; }
+        double* o = out + ((int64_t)p * nterms + t + u) * 2;
+        atomicAdd(o, re);
+        atomicAdd(o + 1, im);
+      }
+    }
+    t += g;
+  }
+}
+
+}  // namespace
+
+int points_set_zero(Ctx* c, float2* states, int nbits, int npoints) {
+  cudaError_t e = cudaMemsetAsync(states, 0, ((size_t)npoints << nbits) * sizeof(float2), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(points)");
+  k_points_basis<<<(npoints + kPtThreads - 1) / kPtThreads, kPtThreads, 0, c->stream>>>(states, nbits, npoints);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_points_basis launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
+
+int points_expect(Ctx* c, const float2* states, int nbits, int npoints, const gbq_pauli* d_terms, int nterms,
+                  double* d_out) {
+  cudaError_t e = cudaMemsetAsync(d_out, 0, (size_t)npoints * nterms * 2 * sizeof(double), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(points out)");
+  if (nterms == 0) return GBQ_OK;
+  const int chunk_bits = nbits < 16 ? nbits : 16;
+  dim3 grid((unsigned)(1u << (nbits - chunk_bits)), (unsigned)npoints, 1);
+  k_points_expect<<<grid, kPtThreads, 0, c->stream>>>(states, nbits, chunk_bits, d_terms, nterms, d_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_points_expect launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
+
+}  // namespace gbq

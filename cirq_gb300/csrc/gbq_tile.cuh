@@ -93,6 +93,11 @@ __device__ __forceinline__ uint64_t tile_base(const TileInfo& ti, int64_t tile) 
   return g;
 }
 
+// Matrix pool of the point a tile belongs to (batched points) or the pass's pool.
+__device__ __forceinline__ const float2* tile_mats(const TileInfo& ti, uint64_t gbase) {
+  return ti.pstride ? ti.mats + (int64_t)(gbase >> ti.pshift) * ti.pstride : ti.mats;
+}
+
 // Base index of a tile from three 256-entry tables (tile-number bits 0-7,
 // 8-15, 16-23 deposited at the out-of-tile global bits), built once per
 // launch; tile numbers need at most 24 bits (states of <= 37 bits).
@@ -149,7 +154,7 @@ __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, fl
     else if (c < 8 || R > 1) sel_t |= ((gt >> c) & 1u) << s;
     else wsh[s] = c - 8;
   }
-  const float2* mbase = ti.mats + op.mat;
+  const float2* mbase = tile_mats(ti, gbase) + op.mat;
 
   float2 va[W][D];
   float2 vb[DUAL ? W : 1][DUAL ? D : 1];
@@ -281,7 +286,7 @@ __device__ __forceinline__ void op_diag(const TileInfo& ti, const OpDev& op, flo
     if (op.dext[j] >= 0) ext |= (uint32_t)((gbase >> op.dext[j]) & 1u) << j;
   it ^= ext;
   const uint32_t pt = phys_dev((uint32_t)t);
-  const float2* tab = ti.mats + op.mat;
+  const float2* tab = tile_mats(ti, gbase) + op.mat;
   float part = 0.f;
 #pragma unroll
   for (int j = 0; j < A; ++j) {
@@ -497,7 +502,7 @@ __device__ __forceinline__ const float2* reg_matrix(const TileInfo& ti, const Op
     const uint32_t bit = c >= 0 ? (st.tidx >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
     sel |= bit << s;
   }
-  return ti.mats + op.mat + (int64_t)sel * dd;
+  return tile_mats(ti, gbase) + op.mat + (int64_t)sel * dd;
 }
 
 // Dense op (or dense probe) on the register positions in MASK.
@@ -658,7 +663,7 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
   uint32_t rc[R];
 #pragma unroll
   for (int p = 0; p < R; ++p) rc[p] = op.dcol[op.rbits[p]];
-  const float2* tab = ti.mats + op.mat;
+  const float2* tab = tile_mats(ti, gbase) + op.mat;
   float part = 0.f;
 #pragma unroll
   for (int s = 0; s < A; ++s) {

@@ -361,6 +361,44 @@ class Engine:
         return out[0::2] + 1j * out[1::2]
 
 
+    def device_info(self) -> tuple[int, int, int]:
+        """(SM count, free bytes, total bytes) of the engine's GPU."""
+        sm = ctypes.c_int()
+        free = ctypes.c_size_t()
+        total = ctypes.c_size_t()
+        check(self.lib.gbq_device_info(self.ctx, ctypes.byref(sm), ctypes.byref(free), ctypes.byref(total)),
+              "gbq_device_info")
+        return sm.value, free.value, total.value
+
+    # ---- batched points (states of many points back to back) ---------------
+    def points_set_zero(self, states: DeviceBuffer, nbits: int, npoints: int) -> None:
+        check(self.lib.gbq_points_set_zero(self.ctx, states.ptr, nbits, npoints), "gbq_points_set_zero")
+
+    def run_points(self, states: DeviceBuffer, nbits: int, npoints: int, plan, pool_dev: DeviceBuffer,
+                   pool_stride: int) -> None:
+        if plan.npasses == 0:
+            return
+        check(
+            self.lib.gbq_run_points(
+                self.ctx, states.ptr, nbits, npoints, plan.passes.ctypes.data, len(plan.passes),
+                plan.ops.ctypes.data, len(plan.ops), pool_dev.ptr, int(pool_stride),
+            ),
+            "gbq_run_points",
+        )
+
+    def points_expect(self, states: DeviceBuffer, nbits: int, npoints: int, records: np.ndarray) -> np.ndarray:
+        """(npoints, nterms) complex <psi_p|P_t|psi_p> for unit-coefficient records."""
+        out = np.zeros(2 * npoints * max(len(records), 1), dtype=np.float64)
+        if len(records):
+            check(
+                self.lib.gbq_points_expect(self.ctx, states.ptr, nbits, npoints, records.ctypes.data, len(records),
+                                           out.ctypes.data),
+                "gbq_points_expect",
+            )
+        vals = out[0::2] + 1j * out[1::2]
+        return vals[: npoints * len(records)].reshape(npoints, len(records))
+
+
 class Graph:
     """A captured program; launch() replays it on the engine's stream.  Holds
     references to the device buffers whose addresses are baked in."""

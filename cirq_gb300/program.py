@@ -79,7 +79,9 @@ class OpSource:
     eigen: tuple | None  # (components [(h, P)], shift, exponent expr) for EigenGates
     slot: int | None = None  # trajectory slot: the matrix is the resolver's pick
 
-    def matrices(self, resolvers: Sequence[Any]) -> np.ndarray:
+    def matrices(self, resolvers: Sequence[Any], values: dict | None = None) -> np.ndarray:
+        """(P, d, d) matrices; `values` caches expression -> per-resolver
+        values across the sources of one batch (gates sharing a symbol)."""
         P = len(resolvers)
         if self.const is not None:
             return np.broadcast_to(self.const, (P,) + self.const.shape)
@@ -94,7 +96,11 @@ class OpSource:
         resolvers = [getattr(r, "base", r) for r in resolvers]
         if self.eigen is not None:
             comps, shift, expr = self.eigen
-            t = np.array([float(r.value_of(expr)) for r in resolvers])
+            t = None if values is None else values.get(expr)
+            if t is None:
+                t = np.array([float(r.value_of(expr)) for r in resolvers])
+                if values is not None:
+                    values[expr] = t
             out = 0
             for h, proj in comps:
                 out = out + np.exp(1j * np.pi * t * (h + shift))[:, None, None] * proj[None]
@@ -294,7 +300,8 @@ class CompiledCircuit:
         self.gates.append(BitGate(bits=bits, matrix=None, diagonal=False, tag=len(self.sources) - 1))
 
     def gate_batch(self, resolvers) -> dict:
-        return {i: s.matrices(resolvers) for i, s in enumerate(self.sources)}
+        values: dict = {}
+        return {i: s.matrices(resolvers, values) for i, s in enumerate(self.sources)}
 
     def _plan_resolvers(self, resolvers):
         batch = self.gate_batch(resolvers)

@@ -290,6 +290,27 @@ int gbq_batch_expect(gbq_ctx* ctx, const gbq_point* points, int npoints, const g
                      int npasses, const gbq_op* ops, int nops, const gbq_c64* mats,
                      const gbq_pauli* terms, int nterms, int max_nbits, double* out);
 
+/* Batched points of one compiled circuit, evolved together (no reference
+ * counterpart; same role as gbq_batch_expect: replaces the per-resolver loop
+ * of simulate_sweep_iter, cirq-core/cirq/sim/simulator.py:558-605).  The
+ * states of npoints points lie back to back in device memory, point p at
+ * states + p * 2^nbits.
+ * gbq_points_set_zero: every point's state to |0...0>.
+ * gbq_run_points: runs the program on every point; each pass is one launch
+ *   over all points, point p reading its matrices at mats + p * pool_stride
+ *   (op.mat offsets relative to that; pool_stride even).  Single-state pass
+ *   kinds only (no MMA ops), states of nbits <= 34, npoints * 2^(nbits - L)
+ *   <= 2^24 tiles per pass.
+ * gbq_points_expect: out[(p * nterms + t) * 2 + {0, 1}] = (re, im) of
+ *   <psi_p| i^ny X^x Z^zy |psi_p> (unit coefficients) for every point p and
+ *   term t; terms with equal x should be adjacent (they share one read of
+ *   the state).  Host arrays: terms, out. */
+int gbq_points_set_zero(gbq_ctx* ctx, gbq_c64* states, int nbits, int npoints);
+int gbq_run_points(gbq_ctx* ctx, gbq_c64* states, int nbits, int npoints, const gbq_pass* passes,
+                   int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, int64_t pool_stride);
+int gbq_points_expect(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints,
+                      const gbq_pauli* terms, int nterms, double* out);
+
 #ifdef __cplusplus
 }
 #endif
