@@ -378,13 +378,20 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
         res = [cirq.ParamResolver({**dict(zip(gammas, q[:p])), **dict(zip(betas, q[p:]))}) for q in pts]
         jobs.append(batch.BatchJob(circuit, obs, res))
     batch.simulate_expectation_values_batch(jobs[:1])  # warm-up
+    batch.simulate_expectation_values_batch(jobs[:1], persistent=True)
     t = time.perf_counter()
     vals = batch.simulate_expectation_values_batch(jobs)
     dt = time.perf_counter() - t
+    t = time.perf_counter()
+    vals_p = batch.simulate_expectation_values_batch(jobs, persistent=True)
+    dt_p = time.perf_counter() - t
     return {
         "workload": f"QAOA p={p}, {points} points over widths {list(widths)}",
         "points_per_s": points / dt,
         "s_total": dt,
+        "mode": "points of a job evolved together (one tile-pass launch per pass)",
+        "persistent_single_launch_s_total": dt_p,
+        "max_abs_diff_between_modes": float(max(np.abs(a - b).max() for a, b in zip(vals, vals_p))),
         "mean_expectation": float(np.mean([np.real(v).mean() for v in vals])),
     }
 
