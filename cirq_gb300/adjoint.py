@@ -23,6 +23,8 @@ the gate matrix (any other parameterised gate).
 
 from __future__ import annotations
 
+import threading
+
 from typing import Any, Sequence
 
 import numpy as np
@@ -116,48 +118,75 @@ class AdjointProgram:
         return self._engine
 
     # ------------------------------------------------------------------
-    def _reverse_batch(self, resolver) -> dict:
+    def _reverse_batch(self, resolver, gates: dict | None = None) -> dict:
+        """Reverse-program matrices at one point; `gates` are the forward
+        program's evaluated gate matrices at that point, when available."""
         fwd = self.forward
         cache_u: dict = {}
+        values: dict = {}  # expression -> value at this point, shared by all gates
         out = {}
         for j, (kind, i, si) in enumerate(self._rev_src):
             src = fwd.sources[i]
             if i not in cache_u:
-                cache_u[i] = src.matrices([resolver])[0]
+                cache_u[i] = gates[i][0] if gates is not None else src.matrices([resolver], values)[0]
             u = cache_u[i]
             if kind == "dagger":
                 out[j] = u.conj().T[None]
             else:
-                du = src.derivatives([resolver], self.symbols[si])
+                du = src.derivatives([resolver], self.symbols[si], values)
                 out[j] = (du[0] @ u.conj().T)[None]
         return out
 
-    def forward_state(self, values):
-        """Runs the forward program; returns (psi, lam, E, resolver)."""
+    def forward_state(self, values, overlap=None):
+        """Runs the forward program; returns (psi, lam, E, resolver).
+
+        `overlap(resolver, gates)` (optional) runs on the host while the
+        forward passes execute on the GPU; its result is stored in
+        self._overlap_result."""
         eng = self.engine
         r = cirq.ParamResolver(dict(zip(self.symbols, [float(v) for v in values])))
         fwd = self.forward
+        gates = fwd.gate_batch([r])
         psi = eng.new_state(self.n, basis=0, nbits_dev=self.nbits)
+        pool = None
         if fwd.plan.npasses:
-            pool = eng.upload(np.ascontiguousarray(fwd.pool([r])[0]))
-            eng.run(psi, self.nbits, fwd.plan, pool)
+            pool = eng.upload(np.ascontiguousarray(fwd.pool_from_batch(gates, 1)[0]))
+            eng.run(psi, self.nbits, fwd.plan, pool, sync=False)
+        # host work on a helper thread: the calls below wait for the GPU inside
+        # the C library (ctypes releases the GIL), so it runs alongside them
+        worker = None
+        self._overlap_result = None
+        if overlap is not None:
+            def job():
+                self._overlap_result = overlap(r, gates)
+
+            worker = threading.Thread(target=job)
+            worker.start()
         if self.nbits > self.n:
             # padding amplitudes of lam stay zero; apply_paulisum writes the first 2^n
             lam = eng.new_state(self.nbits, basis=0)
         else:
             lam = eng.alloc(8 << self.nbits)
-        eng.apply_paulisum(psi, self.n, self.terms, lam)
-        E = eng.inner(psi, lam, self.n).real
+        try:
+            eng.apply_paulisum(psi, self.n, self.terms, lam)  # synchronises: the forward pool is free
+            if pool is not None:
+                pool.free()
+            E = eng.inner(psi, lam, self.n).real
+        finally:
+            if worker is not None:
+                worker.join()
         return psi, lam, E, r
 
-    def gradient_from(self, psi, lam, resolver) -> np.ndarray:
+    def _reverse_pool(self, resolver, gates=None) -> np.ndarray:
+        return self.reverse.pool_for(self._reverse_batch(resolver, gates), 1)[0]
+
+    def gradient_from(self, psi, lam, resolver, reverse_pool=None) -> np.ndarray:
         """Reverse sweep from (psi, lam) after the forward pass (consumes both)."""
         eng = self.engine
         grad = np.zeros(len(self.symbols))
         if self.nslots == 0:
             return grad
-        batch = self._reverse_batch(resolver)
-        pool = self.reverse.pool_for(batch, 1)[0]
+        pool = reverse_pool if reverse_pool is not None else self._reverse_pool(resolver)
         pool_dev = eng.upload(np.ascontiguousarray(pool))
         partial = eng.alloc(8 * self.nslots * self.reverse_tiles)
         slots = eng.alloc(8 * self.nslots)
@@ -169,8 +198,11 @@ class AdjointProgram:
         return grad
 
     def value_and_grad(self, values) -> tuple[float, np.ndarray]:
-        psi, lam, E, r = self.forward_state(values)
-        g = self.gradient_from(psi, lam, r)
+        # the reverse program's matrices are built on the host while the
+        # forward passes run on the GPU
+        overlap = self._reverse_pool if self.nslots else None
+        psi, lam, E, r = self.forward_state(values, overlap=overlap)
+        g = self.gradient_from(psi, lam, r, reverse_pool=self._overlap_result)
         psi.free()
         lam.free()
         return E, g

@@ -114,6 +114,7 @@ static uint32_t bank_col(int b) { return phys_const(1u << b) & 15u; }
 struct LayoutState {
   int nreg = 0;
   int reg[5] = {0, 0, 0, 0, 0};
+  int nprobe = 0;  // probe ops of the pass so far (their accumulator index)
 };
 
 // Thread-bit order of a layout: 4 bank-independent bits first.
@@ -189,6 +190,7 @@ static int convert_op(const gbq_op& op, int L, int nbits, uint64_t inmask, bool 
   d.k = op.k;
   d.slot = op.slot;
   d.mat = op.mat;
+  if (probe) d.pidx = lay.nprobe++;
   for (int p = 0; p < lay.nreg; ++p) d.rbits[p] = (int8_t)lay.reg[p];
   if (rdense) {
     const int kmax = kind == GBQ_OP_RPROBE ? 3 : 4;

@@ -60,7 +60,7 @@ struct OpDev {
   int8_t rbits[5];    // layout: tile bit of each register position
   int8_t pad2[3];
   int32_t slot;
-  int32_t pad1;
+  int32_t pidx;       // probe: accumulator index within the pass
   int64_t mat;
 };
 

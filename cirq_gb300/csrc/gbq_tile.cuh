@@ -62,6 +62,14 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// Probe accumulation: warp sums of v are added to the CTA's accumulator
+// acc[pidx] in shared memory (no barrier); the pass kernel writes the
+// accumulators once per CTA when its tiles are done.
+__device__ __forceinline__ void probe_add(double v, int pidx, double* acc) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc + pidx, v);
+}
+
 // Block sum of v stored to *out by thread 0 (all threads must call).
 __device__ __forceinline__ void cta_sum_store(double v, double* out, double* red) {
   v = warp_sum(v);
@@ -205,7 +213,7 @@ __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, fl
         }
       }
     }
-    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+    probe_add((double)part, op.pidx, red);
   } else {
     if constexpr (R > 1) __syncthreads();  // other threads still read this group
     if (!active) return;
@@ -306,7 +314,7 @@ __device__ __forceinline__ void op_diag(const TileInfo& ti, const OpDev& op, flo
     }
   }
   if constexpr (PROBE)
-    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+    probe_add((double)part, op.pidx, red);
 }
 
 // KMAX: widest shared-memory dense op the kernel variant contains (0 or 5);
@@ -642,7 +650,7 @@ __device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
     }
   }
   if constexpr (PROBE)
-    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+    probe_add((double)part, op.pidx, red);
   (void)R;
 }
 
@@ -682,7 +690,7 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
     }
   }
   if constexpr (PROBE)
-    cta_sum_store((double)part, ti.partial + (int64_t)op.slot * ti.ntiles + tile, red);
+    probe_add((double)part, op.pidx, red);
 }
 
 template <int LT, int KMAX, bool DUAL, bool PROBE, int RK, int M = 1>
@@ -771,7 +779,7 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops_sh[kParamOps ? 1 : GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t ttab[3 * kTileTab];
-  __shared__ double red[kThreads / 32];
+  __shared__ double red[GBQ_MAX_OPS_PER_PASS];  // probe accumulators (two-state passes)
   constexpr int TS = 1 << LT;
   constexpr int NS = DUAL ? 2 : 1;
   float2* buf = reinterpret_cast<float2*>(smraw);  // [kStages][NS][TS]
@@ -784,6 +792,9 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
   }
   tile_tables_build(a.ti, ttab);
   const TileSetup ts = tile_setup<LT>(a.ti);
+  if constexpr (DUAL) {
+    for (int i = threadIdx.x; i < GBQ_MAX_OPS_PER_PASS; i += kThreads) red[i] = 0.0;
+  }
   __syncthreads();
   const int64_t step = gridDim.x;
   // prologue: the first kStages - 1 tiles
@@ -821,6 +832,22 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
     cur = (cur + 1) % kStages;
   }
   cp_async_wait<0>();
+  if constexpr (DUAL) {
+    // probe totals of this CTA: into the partial of its first tile, zeros
+    // into those of its other tiles (the slot sums over all tiles)
+    __syncthreads();
+    for (int o = 0; o < a.ti.nops; ++o) {
+      const OpDev& op = sops[o];
+      const int kind = op.kind;
+      if (kind != GBQ_OP_PROBE && kind != GBQ_OP_PROBE_DIAG && kind != GBQ_OP_RPROBE &&
+          kind != GBQ_OP_RPROBE_DIAG)
+        continue;
+      double* dst = a.ti.partial + (int64_t)op.slot * a.ti.ntiles;
+      for (int64_t tile = blockIdx.x + (int64_t)threadIdx.x * step; tile < a.ti.ntiles;
+           tile += (int64_t)kThreads * step)
+        dst[tile] = tile == (int64_t)blockIdx.x ? red[op.pidx] : 0.0;
+    }
+  }
 }
 
 template <int LT, int KMAX, bool DUAL, int STAGES, int RK>
@@ -1061,6 +1088,10 @@ int launch_tile_pass(Ctx* c, const PassArgs& a) {
       }
       return launch_tile_pass_stages<LT, 0, false, 2, 2>(c, a);
     }
+  }
+  if constexpr (KMAX == 0 && DUAL) {
+    // two-state (adjoint) passes of width <= 2 register ops: the lean variant
+    if (pass_rkmax(a) <= 2) return launch_tile_pass_stages<LT, 0, true, 2, 2>(c, a);
   }
   if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3, 4>(c, a);
   return launch_tile_pass_stages<LT, KMAX, DUAL, 2, 4>(c, a);

@@ -203,7 +203,10 @@ class Engine:
             check(self.lib.gbq_sv_set_basis(self.ctx, buf.ptr, nbits_dev, int(basis)), "gbq_sv_set_basis")
         return buf
 
-    def run(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer | None = None) -> None:
+    def run(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer | None = None,
+            sync: bool = True) -> None:
+        """Runs a program; with sync=False it returns once the passes are
+        queued and the caller keeps `pool_dev` alive until a later sync."""
         if plan.npasses == 0:
             return
         if pool_dev is None:
@@ -222,7 +225,8 @@ class Engine:
             "gbq_run",
         )
         # keep the pool alive until the stream has consumed it
-        self.sync()
+        if sync:
+            self.sync()
 
     def graph(self, state: DeviceBuffer, nbits: int, plan, pool_dev: DeviceBuffer) -> "Graph":
         """Captures the program's launches on (state, pool_dev) into a CUDA graph."""

@@ -122,20 +122,33 @@ class OpSource:
             return m.reshape(-1, 1, 1) * np.eye(2)[None]
         return m
 
-    def derivatives(self, resolvers: Sequence[Any], symbol) -> np.ndarray | None:
-        """dU/d(symbol) for every resolver (P, d, d), or None if U does not depend on it."""
+    def derivatives(self, resolvers: Sequence[Any], symbol, values: dict | None = None) -> np.ndarray | None:
+        """dU/d(symbol) for every resolver (P, d, d), or None if U does not depend
+        on it.  `values` caches expression -> per-resolver values across calls."""
         cirq = _cirq()
         if self.const is not None:
             return None
         if self.eigen is not None:
             comps, shift, expr = self.eigen
-            import sympy
+            cache = self.__dict__.setdefault("_dexpr", {})
+            dexpr = cache.get(symbol)
+            if dexpr is None:
+                import sympy
 
-            dexpr = sympy.diff(expr, symbol)
+                dexpr = cache[symbol] = sympy.diff(expr, symbol)
             if dexpr == 0:
                 return None
-            t = np.array([float(r.value_of(expr)) for r in resolvers])
-            dt = np.array([float(r.value_of(dexpr)) for r in resolvers])
+
+            def evaluate(e):
+                v = None if values is None else values.get(e)
+                if v is None:
+                    v = np.array([float(r.value_of(e)) for r in resolvers])
+                    if values is not None:
+                        values[e] = v
+                return v
+
+            t = evaluate(expr)
+            dt = evaluate(dexpr)
             out = 0
             for h, proj in comps:
                 f = 1j * np.pi * (h + shift) * np.exp(1j * np.pi * t * (h + shift)) * dt
@@ -345,9 +358,14 @@ class CompiledCircuit:
         """complex64 (P, pool_len) matrix pools for the resolvers."""
         if not self.parameterized:
             return np.broadcast_to(self.plan.pool, (len(resolvers), len(self.plan.pool)))
-        batch = self.gate_batch(resolvers)
+        return self.pool_from_batch(self.gate_batch(resolvers), len(resolvers))
+
+    def pool_from_batch(self, batch: dict, npoints: int) -> np.ndarray:
+        """Matrix pools from already evaluated gate matrices (gate_batch)."""
+        if not self.parameterized:
+            return np.broadcast_to(self.plan.pool, (npoints, len(self.plan.pool)))
         sub = {j: np.asarray(batch[i]) for j, i in enumerate(self.kept)}
-        return self.plan.pool_for(sub, len(resolvers))
+        return self.plan.pool_for(sub, npoints)
 
     def global_phase(self, resolver) -> complex:
         """Product of the global-phase operations (used for 0-qubit circuits)."""
