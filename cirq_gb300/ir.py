@@ -78,74 +78,6 @@ def flatten_ops(circuit) -> list:
     return ops
 
 
-def unitary_gates(ops, index: dict, n: int, *, dm: bool = False) -> tuple[list[BitGate], complex]:
-    """Unitary ops -> BitGates (state vector: n bits; dm=True: 2n bits).
-
-    Returns (gates, global_phase).  Measurements must already be removed.
-    """
-    cirq = _cirq()
-    gates: list[BitGate] = []
-    phase = 1.0 + 0j
-    for op in ops:
-        if not op.qubits:
-            if cirq.has_unitary(op):
-                phase *= complex(cirq.unitary(op).reshape(-1)[0])
-                continue
-            raise UnsupportedOperation(f"operation without qubits and without a unitary: {op!r}")
-        if any(q.dimension != 2 for q in op.qubits):
-            raise UnsupportedOperation(f"only qubits are supported, got {op!r}")
-        if not cirq.has_unitary(op):
-            raise UnsupportedOperation(f"operation without a unitary: {op!r}")
-        u = np.asarray(cirq.unitary(op), dtype=np.complex128)
-        gates.extend(_unitary_to_bitgates(op, u, index, n, dm))
-    return gates, phase
-
-
-def _unitary_to_bitgates(op, u, index, n, dm):
-    pos = [index[q] for q in op.qubits]
-    k = len(pos)
-    if np.allclose(u, np.eye(2**k), atol=0, rtol=0):
-        return []
-    diag = is_diagonal(u)
-    if not dm:
-        bits = tuple(n - 1 - p for p in reversed(pos))
-        return [BitGate(bits, u, diag)]
-    rows = tuple(2 * n - 1 - p for p in reversed(pos))
-    cols = tuple(n - 1 - p for p in reversed(pos))
-    return [BitGate(rows, u, diag), BitGate(cols, np.conjugate(u), diag)]
-
-
-def channel_gates(ops, index: dict, n: int) -> list[BitGate]:
-    """Any ops (unitaries or channels) -> BitGates on the 2n-bit density vector."""
-    cirq = _cirq()
-    gates: list[BitGate] = []
-    for op in ops:
-        if not op.qubits:
-            if cirq.has_unitary(op):  # global phase cancels in rho
-                continue
-            raise UnsupportedOperation(f"operation without qubits: {op!r}")
-        if any(q.dimension != 2 for q in op.qubits):
-            raise UnsupportedOperation(f"only qubits are supported, got {op!r}")
-        if cirq.has_unitary(op):
-            u = np.asarray(cirq.unitary(op), dtype=np.complex128)
-            gates.extend(_unitary_to_bitgates(op, u, index, n, True))
-            continue
-        if not cirq.has_kraus(op):
-            raise UnsupportedOperation(f"operation without Kraus operators: {op!r}")
-        kraus = [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(op)]
-        pos = [index[q] for q in op.qubits]
-        k = len(pos)
-        if 2 * k > 5:
-            raise UnsupportedOperation(
-                f"channels on more than 2 qubits are not supported on the GPU path: {op!r}"
-            )
-        s = sum(np.kron(np.conjugate(kk), kk) for kk in kraus)
-        rows = tuple(2 * n - 1 - p for p in reversed(pos))
-        cols = tuple(n - 1 - p for p in reversed(pos))
-        gates.append(BitGate(rows + cols, s, is_diagonal(s)))
-    return gates
-
-
 def pauli_terms(observable, index: dict, n: int):
     """PauliSum-like -> (gbq_pauli records, coefficients are complex).
 

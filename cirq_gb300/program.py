@@ -20,7 +20,7 @@ per point.
 from __future__ import annotations
 
 import dataclasses
-from typing import Any, Callable, Sequence
+from typing import Any, Sequence
 
 import numpy as np
 

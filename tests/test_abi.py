@@ -2,7 +2,6 @@
 
 import ctypes
 
-import numpy as np
 
 from cirq_gb300 import _lib
 

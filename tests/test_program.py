@@ -10,7 +10,7 @@ from cirq_gb300 import workloads
 from cirq_gb300.planner import Planner
 from cirq_gb300.program import CompiledCircuit, split_measurements
 from emulator import run_program
-from oracle.circuits import simulate_density_matrix, simulate_state_vector
+from oracle.circuits import simulate_state_vector
 
 GOLD = np.load(__file__.replace("test_program.py", "golden/golden.npz"))
 
