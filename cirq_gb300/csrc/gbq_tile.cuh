@@ -693,18 +693,30 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
     probe_add((double)part, op.pidx, red);
 }
 
-template <int LT, int KMAX, bool DUAL, bool PROBE, int RK, int M = 1>
+template <int LT, bool DUAL, bool PROBE, int RK, int M>
+__device__ __forceinline__ void reg_dense_case(const TileInfo& ti, const OpDev& op, RegState<LT, DUAL>& st,
+                                               uint64_t gbase, int64_t tile, double* red) {
+  if constexpr (M < (1 << RegState<LT, DUAL>::R) && (!PROBE || popc_const(M) <= 3) && popc_const(M) <= RK)
+    reg_dense<M, LT, DUAL, PROBE>(ti, op, st, gbase, tile, red);
+}
+
+// One switch over the register-position mask (a jump, not a chain of tests).
+template <int LT, int KMAX, bool DUAL, bool PROBE, int RK>
 __device__ __forceinline__ void reg_dense_dispatch(const TileInfo& ti, const OpDev& op,
                                                    RegState<LT, DUAL>& st, uint64_t gbase,
                                                    int64_t tile, double* red) {
-  if constexpr (M < (1 << RegState<LT, DUAL>::R)) {
-    if (op.rmask == M) {
-      if constexpr ((!PROBE || popc_const(M) <= 3) && popc_const(M) <= RK)
-        reg_dense<M, LT, DUAL, PROBE>(ti, op, st, gbase, tile, red);
-    } else {
-      reg_dense_dispatch<LT, KMAX, DUAL, PROBE, RK, M + 1>(ti, op, st, gbase, tile, red);
-    }
+#define GBQ_RCASE(M) \
+  case M:            \
+    reg_dense_case<LT, DUAL, PROBE, RK, M>(ti, op, st, gbase, tile, red); \
+    break;
+  switch (op.rmask) {
+    GBQ_RCASE(1) GBQ_RCASE(2) GBQ_RCASE(3) GBQ_RCASE(4) GBQ_RCASE(5) GBQ_RCASE(6) GBQ_RCASE(7)
+    GBQ_RCASE(8) GBQ_RCASE(9) GBQ_RCASE(10) GBQ_RCASE(11) GBQ_RCASE(12) GBQ_RCASE(13) GBQ_RCASE(14)
+    GBQ_RCASE(15)
+    default:
+      break;
   }
+#undef GBQ_RCASE
 }
 
 // Barrier among the threads that run the ops: the whole CTA, or (NB) the
