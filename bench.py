@@ -396,6 +396,29 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
     }
 
 
+def width33_bench(depth: int = 40, steps: int = 2):
+    """The 33-qubit form of the headline workload (64 GiB state, same
+    construction): gate-updates/s and the HBM fraction of the tile passes."""
+    from cirq_gb300.engine import Engine
+    from cirq_gb300.planner import Planner
+
+    eng = Engine.get(0)
+    _, free, _ = eng.device_info()
+    if free < (70 << 30):
+        return {"skipped": f"needs 70 GiB free device memory, {free >> 30} GiB free"}
+    circuit, ngates = build_workload(33, depth, 0)
+    compiled = compile_plan(circuit, Planner(tile_bits=12, kmax=4, budget=25.0))
+    ms, pass_ms, passes, _ = device_steps(eng, compiled, steps, 1, pass_timing=True)
+    peak, _ = peaks()
+    return {
+        "workload": f"random-layer circuit 33q depth {depth} ({ngates} gates), seed 0",
+        "gate_updates_per_s": ngates / (ms / 1e3),
+        "ms_per_step": ms,
+        "passes": passes,
+        "hbm_frac": 16 * (1 << 33) / (pass_ms / 1e3) / 1e9 / peak if pass_ms else None,
+    }
+
+
 def mma_bench(n: int = 30, reps: int = 3):
     """Tensor-core evaluation: one 11-bit-tile pass applying 1, 2 or 4
     random 4-qubit matrices with tcgen05 MMAs (GBQ_OP_MMA, TF32 three-term
@@ -550,7 +573,7 @@ def main():
     extra = {}
     if not args.no_extra and rank == 0:
         for name, fn in (("adjoint", adjoint_bench), ("density_matrix", density_bench), ("batch_sweep", batch_bench),
-                         ("tensor_core_pass", mma_bench)):
+                         ("width_33", width33_bench), ("tensor_core_pass", mma_bench)):
             try:
                 extra[name] = fn()
             except Exception as e:  # reported, not hidden
