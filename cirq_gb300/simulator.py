@@ -145,6 +145,10 @@ class _GpuSimulatorBase:
         qubit_order = cirq.QubitOrder.as_qubit_order(qubit_order)
         qubits = tuple(qubit_order.order_for(program.all_qubits()))
         resolvers = list(cirq.to_resolvers(params))
+        # unresolved symbols are the caller's error (ValueError, as the
+        # reference), checked before anything is compiled
+        for r in resolvers or [cirq.ParamResolver({})]:
+            _check_all_resolved(program, r)
         body, meas = split_measurements(program)
         noisy = self._noisy_ops(cirq.Circuit(body), qubits) if body else None
         if noisy is not None:
@@ -469,8 +473,6 @@ class Simulator(
                     yield _state_vector_result(r, meas, qubits, vec)
             return
         qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
-        for r in resolvers:
-            _check_all_resolved(program, r)
         if compiled.n == 0:
             for r in resolvers:
                 vec = np.array([compiled.global_phase(r)], dtype=np.complex64)
@@ -526,8 +528,6 @@ class Simulator(
                 if q not in index:
                     raise ValueError(f"Qubit {q} of the observable is not in the qubit order")
         terms = [pauli_terms(ps, index, compiled.n) for ps in pslist]
-        for r in resolvers:
-            _check_all_resolved(body_prog, r)
         pools = compiled.pool(resolvers)
         eng = self.engine
         for p, r in enumerate(resolvers):
@@ -602,8 +602,6 @@ class DensityMatrixSimulator(
                     yield _density_matrix_result(r, meas, qubits, rho)
             return
         qubits, resolvers, compiled, meas = self._prepare(program, qubit_order, params)
-        for r in resolvers:
-            _check_all_resolved(program, r)
         n = compiled.n
         if n == 0:
             for r in resolvers:
@@ -647,8 +645,6 @@ class DensityMatrixSimulator(
         qubits, resolvers, compiled, _ = self._prepare(body_prog, qubit_order, params)
         index = {q: i for i, q in enumerate(qubits)}
         terms = [pauli_terms(ps, index, compiled.n) for ps in pslist]
-        for r in resolvers:
-            _check_all_resolved(body_prog, r)
         pools = compiled.pool(resolvers)
         eng = self.engine
         for p, r in enumerate(resolvers):

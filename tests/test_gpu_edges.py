@@ -1,0 +1,118 @@
+"""Edge cases of the drop-in API on the GPU: empty and degenerate circuits,
+zero repetitions, unresolved parameters, sweep objects, initial states,
+amplitudes and non-line qubits.  Values are checked against the oracle;
+shapes and dtypes of results against the reference simulator itself."""
+
+import numpy as np
+import pytest
+import sympy
+
+import cirq
+import cirq_gb300
+from cirq_gb300 import workloads
+from oracle.circuits import simulate_density_matrix, simulate_state_vector
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_circuit_and_idle_qubits():
+    r = cirq_gb300.Simulator().simulate(cirq.Circuit())
+    assert r.final_state_vector.shape == (1,) and abs(r.final_state_vector[0] - 1) < 1e-7
+    q = cirq.LineQubit.range(3)
+    r = cirq_gb300.Simulator().simulate(cirq.Circuit(), qubit_order=q, initial_state=6)
+    want = np.zeros(8)
+    want[6] = 1
+    np.testing.assert_allclose(r.final_state_vector, want, atol=1e-7)
+    rho = cirq_gb300.DensityMatrixSimulator().simulate(cirq.Circuit(), qubit_order=q).final_density_matrix
+    assert rho.shape == (8, 8) and abs(rho[0, 0] - 1) < 1e-7
+
+
+def test_global_phase_only_and_single_qubit():
+    c = cirq.Circuit(cirq.global_phase_operation(1j))
+    r = cirq_gb300.Simulator().simulate(c)
+    np.testing.assert_allclose(r.final_state_vector, [1j], atol=1e-7)
+    q = cirq.LineQubit(0)
+    c1 = cirq.Circuit(cirq.rx(0.3).on(q), cirq.global_phase_operation(-1), cirq.rz(1.1).on(q))
+    np.testing.assert_allclose(
+        cirq_gb300.Simulator().simulate(c1).final_state_vector, simulate_state_vector(c1), atol=1e-6
+    )
+
+
+def test_zero_repetitions_shapes_match_reference():
+    q = cirq.LineQubit.range(3)
+    for c in (
+        cirq.Circuit(cirq.H(q[0]), cirq.measure(*q, key="m")),
+        cirq.Circuit(cirq.H(q[0]), cirq.measure(q[0], key="a"), cirq.X(q[1]), cirq.measure(q[1], key="b")),
+    ):
+        ours = cirq_gb300.Simulator().run(c, repetitions=0)
+        ref = cirq.Simulator().run(c, repetitions=0)
+        assert set(ours.records) == set(ref.records)
+        for k in ref.records:
+            assert ours.records[k].shape == ref.records[k].shape
+
+
+def test_run_result_types_match_reference():
+    q = cirq.LineQubit.range(3)
+    c = cirq.Circuit(cirq.H.on_each(*q), cirq.measure(q[0], q[2], key="m"))
+    ours = cirq_gb300.Simulator(seed=1).run(c, repetitions=7)
+    ref = cirq.Simulator(seed=1).run(c, repetitions=7)
+    assert ours.measurements["m"].shape == ref.measurements["m"].shape
+    assert ours.measurements["m"].dtype == ref.measurements["m"].dtype
+
+
+def test_unresolved_symbols_raise_like_the_reference():
+    q = cirq.LineQubit(0)
+    c = cirq.Circuit(cirq.rx(sympy.Symbol("t")).on(q), cirq.measure(q, key="m"))
+    with pytest.raises(ValueError):
+        cirq_gb300.Simulator().run(c)
+    with pytest.raises(ValueError):
+        cirq_gb300.Simulator().simulate(c)
+    with pytest.raises(ValueError):
+        cirq_gb300.DensityMatrixSimulator().simulate(c)
+
+
+def test_complex128_is_rejected():
+    with pytest.raises(ValueError):
+        cirq_gb300.Simulator(dtype=np.complex128)
+
+
+def test_sweep_objects_and_amplitudes():
+    c, syms = workloads.random_layer_circuit(5, 4, seed=9), None
+    t = sympy.Symbol("t")
+    q = sorted(c.all_qubits())
+    cp = c + cirq.Circuit(cirq.rx(t).on(q[0]), cirq.CZ(q[0], q[1]) ** t)
+    sweep = cirq.Linspace(t, 0, 1, 5) * cirq.Points("u", [0.0])
+    results = cirq_gb300.Simulator().simulate_sweep(cp, sweep)
+    assert len(results) == 5
+    for r in results:
+        want = simulate_state_vector(cp, r.params)
+        np.testing.assert_allclose(r.final_state_vector, want, atol=1e-5)
+    amps = cirq_gb300.Simulator().compute_amplitudes(cp, [0, 5, 31], param_resolver={"t": 0.25})
+    want = simulate_state_vector(cp, cirq.ParamResolver({"t": 0.25}))
+    np.testing.assert_allclose(amps, want[[0, 5, 31]], atol=1e-5)
+
+
+def test_state_vector_initial_states_both_simulators():
+    q = cirq.LineQubit.range(4)
+    c = workloads.random_layer_circuit(4, 3, seed=2)
+    rs = np.random.RandomState(3)
+    psi = rs.normal(size=16) + 1j * rs.normal(size=16)
+    psi /= np.linalg.norm(psi)
+    got = cirq_gb300.Simulator().simulate(c, qubit_order=q, initial_state=psi.astype(np.complex64))
+    u = cirq.unitary(cirq.Circuit(c.all_operations()).transform_qubits(lambda x: x))
+    np.testing.assert_allclose(got.final_state_vector, cirq.final_state_vector(c, qubit_order=q, initial_state=psi.astype(np.complex64)), atol=1e-5)
+    rho0 = np.outer(psi, psi.conj())
+    dm = cirq_gb300.DensityMatrixSimulator().simulate(c, qubit_order=q, initial_state=rho0.astype(np.complex64))
+    want = u @ rho0 @ u.conj().T
+    np.testing.assert_allclose(dm.final_density_matrix, want, atol=1e-5)
+
+
+def test_grid_and_named_qubits_keep_the_reference_order():
+    qs = [cirq.GridQubit(1, 0), cirq.GridQubit(0, 1), cirq.NamedQubit("z"), cirq.NamedQubit("a")]
+    c = cirq.Circuit(cirq.H(qs[0]), cirq.CNOT(qs[0], qs[2]), cirq.ry(0.4).on(qs[3]), cirq.CZ(qs[1], qs[3]))
+    ours = cirq_gb300.Simulator().simulate(c)
+    ref = cirq.Simulator().simulate(c)
+    assert ours.qubit_map == ref.qubit_map
+    np.testing.assert_allclose(ours.final_state_vector, ref.final_state_vector, atol=1e-6)
+    rho = cirq_gb300.DensityMatrixSimulator().simulate(c).final_density_matrix
+    np.testing.assert_allclose(rho, simulate_density_matrix(c), atol=1e-6)
