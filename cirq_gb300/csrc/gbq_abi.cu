@@ -1006,6 +1006,27 @@ int gbq_run_points(gbq_ctx* c, gbq_c64* states, int nbits, int npoints, const gb
   return GBQ_OK;
 }
 
+int gbq_points_sample(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const double* u,
+                      uint64_t* out) {
+  CHECK_CTX(c);
+  if (!states || nbits < 1 || nbits > 34 || npoints < 1 || !u || !out)
+    return arg_fail("gbq_points_sample: bad arguments");
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b = al((size_t)npoints * 8);
+  int rc = ensure_scratch(c, 2 * b);
+  if (rc) return rc;
+  char* base = reinterpret_cast<char*>(c->scratch);
+  double* d_u = reinterpret_cast<double*>(base);
+  unsigned long long* d_out = reinterpret_cast<unsigned long long*>(base + b);
+  cudaError_t e = cudaMemcpyAsync(d_u, u, (size_t)npoints * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(u)");
+  rc = points_sample(c, reinterpret_cast<const float2*>(states), nbits, npoints, d_u, d_out);
+  if (rc) return rc;
+  e = cudaMemcpyAsync(out, d_out, (size_t)npoints * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(out)");
+  return sync(c, "gbq_points_sample");
+}
+
 int gbq_points_expect(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const gbq_pauli* terms,
                       int nterms, double* out) {
   CHECK_CTX(c);

@@ -161,6 +161,8 @@ int build_mma_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileIn
                    MmaArgs& A);
 int launch_mma_pass(Ctx* c, const MmaArgs& a);
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
+int points_sample(Ctx* c, const float2* states, int nbits, int npoints, const double* d_u,
+                  unsigned long long* d_out);
 int points_expect(Ctx* c, const float2* states, int nbits, int npoints, const gbq_pauli* d_terms, int nterms,
                   double* d_out);
 int launch_batch(Ctx* c, const gbq_point* d_points, int npoints, const gbq_pass* d_passes,

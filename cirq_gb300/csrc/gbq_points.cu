@@ -92,7 +92,64 @@ __global__ void __launch_bounds__(kPtThreads) k_points_expect(const float2* __re
   }
 }
 
+// One CTA per point: draws out[p] from |psi_p|^2 with the uniform u[p]
+// (inverse CDF in double: per-thread chunk sums, a block scan over the
+// chunks, then the owning thread walks its chunk).
+__global__ void __launch_bounds__(kPtThreads) k_points_sample(const float2* __restrict__ states, int nbits,
+                                                             const double* __restrict__ u,
+                                                             unsigned long long* __restrict__ out) {
+  __shared__ double csum[kPtThreads];
+  __shared__ int owner;
+  const int p = blockIdx.x;
+  const float2* psi = states + ((int64_t)p << nbits);
+  const uint64_t dim = 1ull << nbits;
+  const uint64_t per = (dim + kPtThreads - 1) / kPtThreads;
+  const uint64_t lo = (uint64_t)threadIdx.x * per, hi = lo + per < dim ? lo + per : dim;
+  double s = 0.0;
+  for (uint64_t i = lo; i < hi; ++i) {
+    const float2 a = psi[i];
+    s += (double)a.x * a.x + (double)a.y * a.y;
+  }
+  csum[threadIdx.x] = s;
+  if (threadIdx.x == 0) owner = -1;
+  __syncthreads();
+  // inclusive scan over the chunk sums (Hillis-Steele in shared memory)
+  for (int o = 1; o < kPtThreads; o <<= 1) {
+    const double v = threadIdx.x >= o ? csum[threadIdx.x - o] : 0.0;
+    __syncthreads();
+    csum[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const double total = csum[kPtThreads - 1];
+  const double target = u[p] * total;
+  const double before = threadIdx.x ? csum[threadIdx.x - 1] : 0.0;
+  if (target >= before && (target < csum[threadIdx.x] || threadIdx.x == kPtThreads - 1)) atomicMax(&owner, (int)threadIdx.x);
+  __syncthreads();
+  if ((int)threadIdx.x == owner) {
+    double acc = before;
+    uint64_t pick = hi > lo ? hi - 1 : lo;
+    for (uint64_t i = lo; i < hi; ++i) {
+      const float2 a = psi[i];
+      acc += (double)a.x * a.x + (double)a.y * a.y;
+      if (acc > target) {
+        pick = i;
+        break;
+      }
+    }
+    out[p] = pick;
+  }
+}
+
 }  // namespace
+
+int points_sample(Ctx* c, const float2* states, int nbits, int npoints, const double* d_u,
+                  unsigned long long* d_out) {
+  k_points_sample<<<npoints, kPtThreads, 0, c->stream>>>(states, nbits, d_u, d_out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_points_sample launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
 
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints) {
   cudaError_t e = cudaMemsetAsync(states, 0, ((size_t)npoints << nbits) * sizeof(float2), c->stream);

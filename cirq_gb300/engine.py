@@ -390,6 +390,14 @@ class Engine:
             "gbq_run_points",
         )
 
+    def points_sample(self, states: DeviceBuffer, nbits: int, npoints: int, uniforms: np.ndarray) -> np.ndarray:
+        """One basis index per point, drawn from |psi_p|^2."""
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        out = np.empty(npoints, dtype=np.uint64)
+        check(self.lib.gbq_points_sample(self.ctx, states.ptr, nbits, npoints, u.ctypes.data, out.ctypes.data),
+              "gbq_points_sample")
+        return out
+
     def points_expect(self, states: DeviceBuffer, nbits: int, npoints: int, records: np.ndarray) -> np.ndarray:
         """(npoints, nterms) complex <psi_p|P_t|psi_p> for unit-coefficient records."""
         out = np.zeros(2 * npoints * max(len(records), 1), dtype=np.float64)

@@ -41,7 +41,7 @@ from cirq_gb300 import trajectories as _traj
 
 cirq = ensure_cirq()
 
-_MAX_CACHE = 8
+_MAX_CACHE = 64  # compiled circuits kept per simulator (trajectory segments count too)
 
 
 def _check_dtype(dtype):
@@ -272,10 +272,13 @@ class _GpuSimulatorBase:
             return True
         return _traj.needs_trajectories(flatten_ops(program), self._dm)
 
-    def _traj_states(self, program, qubits, resolver, initial_state, reps):
+    def _traj_states(self, program, qubits, resolver, initial_state, reps, records_only=False):
         """Yields (runner, device state, records) for `reps` trajectories; the
-        state is the runner's buffer, valid until the next trajectory."""
+        state is the runner's buffer, valid until the next trajectory.  With
+        records_only, ops after the last measurement are skipped."""
         ops = _traj.circuit_ops(self, program, qubits, resolver)
+        if records_only:
+            ops = _traj.records_relevant(ops)
         runner = _traj.TrajectoryRunner(self, ops, qubits, resolver)
         try:
             picks, pools = runner.prepare(reps)
@@ -319,11 +322,16 @@ class _GpuSimulatorBase:
     def _sample_records(self, state, compiled, meas_ops, repetitions) -> dict[str, np.ndarray]:
         """Terminal-measurement sampling, mirroring StepResult.sample_measurement_ops
         (cirq-core/cirq/sim/simulator.py:733-820) with _allow_repeated=True."""
-        eng = self.engine
-        n = compiled.n
-        index = {q: i for i, q in enumerate(compiled.qubits)}
         u = self._prng.random_sample(repetitions)
-        samples = eng.sample(state, n, u, dm=self._dm).astype(np.int64)
+        samples = self.engine.sample(state, compiled.n, u, dm=self._dm).astype(np.int64)
+        return self._records_from_samples(samples, compiled, meas_ops)
+
+    def _records_from_samples(self, samples, compiled, meas_ops) -> dict[str, np.ndarray]:
+        """run() records (repetitions, instances, bits) from sampled basis
+        indices: invert masks and confusion maps applied per measurement."""
+        n = compiled.n
+        repetitions = len(samples)
+        index = {q: i for i, q in enumerate(compiled.qubits)}
         results: dict[str, list] = {}
         for op in meas_ops:
             gate = op.gate
@@ -344,8 +352,14 @@ class _GpuSimulatorBase:
         _check_all_resolved(circuit, param_resolver)
         qubits = tuple(sorted(circuit.all_qubits()))
         if self._traj_needed(circuit):
+            if not self._dm:
+                ops = _traj.circuit_ops(self, circuit, qubits, param_resolver)
+                rec = _traj.run_batched(self, ops, qubits, param_resolver, repetitions)
+                if rec is not None:
+                    return rec
             per_rep = []
-            for _, state, rec in self._traj_states(circuit, qubits, param_resolver, 0, repetitions):
+            for _, state, rec in self._traj_states(circuit, qubits, param_resolver, 0, repetitions,
+                                                   records_only=True):
                 state.free()
                 per_rep.append(rec)
             return _traj.pad_records(per_rep)

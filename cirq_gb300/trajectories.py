@@ -123,6 +123,14 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
     return items, nslot
 
 
+def records_relevant(ops):
+    """The ops that can influence run() records: everything after the last
+    measurement (for instance noise a model inserts after the final
+    measurement moment) changes no recorded outcome."""
+    last = max((i for i, op in enumerate(ops) if cirq.is_measurement(op)), default=-1)
+    return list(ops[: last + 1]) if last >= 0 else list(ops)
+
+
 def circuit_ops(sim, program, qubits, resolver):
     """The resolved, noise-inserted operations of a circuit (measurements
     included: noise after a mid-circuit measurement acts on later ops)."""
@@ -131,6 +139,23 @@ def circuit_ops(sim, program, qubits, resolver):
         moments = sim.noise.noisy_moments(resolved, sorted(qubits))
         resolved = cirq.Circuit(cirq.flatten_to_ops_or_moments(moments))
     return flatten_ops(resolved)
+
+
+def slot_program(sim, op_qubits, qubits):
+    """A compiled one-op program whose matrix each trajectory supplies as
+    pick 0 (a Kraus operator or a projector), cached per simulator by the
+    op's qubits: every channel or measurement on the same qubits shares it."""
+    cache = sim.__dict__.setdefault("_slot_programs", {})
+    key = (tuple(op_qubits), tuple(qubits))
+    c = cache.get(key)
+    if c is None:
+        from cirq_gb300.program import CompiledCircuit
+
+        op = cirq.IdentityGate(len(op_qubits)).on(*op_qubits)
+        c = CompiledCircuit([Slot(op, 0)], qubits, dm=False, planner=sim.planner,
+                            resolvers=[cirq.ParamResolver({})])
+        cache[key] = c
+    return c
 
 
 class TrajectoryRunner:
@@ -152,7 +177,7 @@ class TrajectoryRunner:
         self.kraus_seg = {}
         for it in self.items:
             if isinstance(it, Channel):
-                self.kraus_seg[it.slot] = sim._compile([Slot(it.op, it.slot)], self.qubits, base)
+                self.kraus_seg[it.slot] = slot_program(sim, it.op.qubits, self.qubits)
         self._kraus = {it.slot: [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(it.op)]
                        for it in self.items if isinstance(it, Channel)}
         self._pauli = {it.slot: self._pauli_basis(it.op) for it in self.items if isinstance(it, Channel)}
@@ -269,7 +294,7 @@ class TrajectoryRunner:
         w = weights[index]
         picks[it.slot] = ks[index] / math.sqrt(w)
         c = self.kraus_seg[it.slot]
-        pool = c.pool([TrajectoryPoint(self.resolver, picks)])[0]
+        pool = c.pool([TrajectoryPoint(self.resolver, {0: picks[it.slot]})])[0]
         eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("kraus", it.slot), pool))
 
     def prepare(self, reps: int):
@@ -306,3 +331,152 @@ def pad_records(per_rep: list[dict]) -> dict[str, np.ndarray]:
                 xs[i, j, : len(bits)] = bits
         out[k] = xs
     return out
+
+
+def _z_subset_records(runner, qubits_m):
+    """Unit Z-string records for every nonempty subset S of the measured
+    qubits (bit j of S <-> qubits_m[j]) and the subset masks."""
+    m = len(qubits_m)
+    recs, masks = [], []
+    for S in range(1, 1 << m):
+        zy = 0
+        for j, q in enumerate(qubits_m):
+            if (S >> j) & 1:
+                zy |= 1 << (runner.n - 1 - runner.index[q])
+        recs.append((0, zy, 0, 1.0))
+        masks.append(S)
+    return recs, np.array(masks, dtype=np.int64)
+
+
+def run_batched(sim, ops, qubits, resolver, reps: int):
+    """All repetitions of a state-vector circuit with noise and/or
+    mid-circuit measurements evolved together (see the module doc):
+    segments as batched passes with each trajectory's mixture draws,
+    general channels and mid-circuit measurements as batched Pauli
+    expectations -> per-trajectory draws on the host -> one batched
+    one-slot pass (K_i / sqrt(w_i), or the projector / sqrt(p)), terminal
+    measurements as one batched draw.  Returns run() records, or None when a
+    mid-circuit measurement covers more than 5 qubits (the caller then runs
+    trajectories one by one)."""
+    from cirq_gb300.engine import Engine
+
+    if reps < 1:
+        return None
+    ops = records_relevant(ops)
+    items, _ = build_items(ops, dm=False)
+    last_unitary = max((i for i, it in enumerate(items) if not isinstance(it, Measure)), default=-1)
+    for i, it in enumerate(items):
+        if isinstance(it, Measure) and i < last_unitary and len(it.op.qubits) > 5:
+            return None
+    terminal = [it.op for it in items[last_unitary + 1 :]]
+    body = items[: last_unitary + 1]
+    runner = TrajectoryRunner(sim, ops, qubits, resolver)
+    eng = sim.engine
+    prng = sim._prng
+    try:
+        picks, pools = runner.prepare(reps)
+        n = runner.empty.nbits_dev
+        _, free, _ = eng.device_info()
+        budget = max(1 << 28, min(int(free) // 2, 32 << 30))
+        chunk = max(1, min(reps, budget // (8 << n), (1 << 24) >> max(n - 10, 0)))
+        # one-slot programs of the mid-circuit measurements (projector slots)
+        proj = {}
+        for i, it in enumerate(body):
+            if isinstance(it, Measure):
+                proj[i] = slot_program(sim, it.op.qubits, runner.qubits)
+        states = eng.alloc((8 << n) * chunk)
+        records: list = [dict() for _ in range(reps)]
+        samples = np.empty(reps, dtype=np.int64)
+
+        def run_slot(compiled, mats, k, start):
+            """One-slot program with a per-trajectory matrix (mats: (k, d, d))."""
+            pts = [TrajectoryPoint(resolver, {0: m}) for m in mats]
+            pool = np.ascontiguousarray(compiled.pool(pts), dtype=np.complex64)
+            plen = pool.shape[1]
+            if plen & 1:
+                pool = np.concatenate([pool, np.zeros((k, 1), np.complex64)], axis=1)
+                plen += 1
+            pool_dev = eng.upload(pool.reshape(-1))
+            eng.run_points(states, n, k, compiled.plan, pool_dev, plen)
+            eng.sync()
+            pool_dev.free()
+
+        try:
+            for start in range(0, reps, chunk):
+                k = min(chunk, reps - start)
+                eng.points_set_zero(states, n, k)
+                for j, it in enumerate(body):
+                    if isinstance(it, Segment):
+                        c = runner.compiled[j]
+                        if not c.plan.npasses:
+                            continue
+                        pool = pools[j] if pools[j] is not None else np.broadcast_to(c.plan.pool, (reps, len(c.plan.pool)))
+                        pool = np.ascontiguousarray(pool[start : start + k], dtype=np.complex64)
+                        plen = pool.shape[1]
+                        if plen & 1:
+                            pool = np.concatenate([pool, np.zeros((k, 1), np.complex64)], axis=1)
+                            plen += 1
+                        pool_dev = eng.upload(pool.reshape(-1))
+                        eng.run_points(states, n, k, c.plan, pool_dev, plen)
+                        eng.sync()
+                        pool_dev.free()
+                    elif isinstance(it, Channel):
+                        ks = runner._kraus[it.slot]
+                        recs, mats = runner._pauli[it.slot]
+                        vals = np.real(eng.points_expect(states, n, k, Engine.pauli_records(recs)))  # (k, 4^q - 1)
+                        d = 2 ** len(it.op.qubits)
+                        rho = np.eye(d, dtype=np.complex128)[None] + np.einsum("pt,tij->pij", vals, np.array(mats))
+                        rho /= d
+                        kk = np.array([K.conj().T @ K for K in ks])  # (nK, d, d)
+                        w = np.clip(np.real(np.einsum("kij,pji->pk", kk, rho)), 0.0, None)  # (k, nK)
+                        u = prng.random_sample(k)
+                        cum = np.cumsum(w, axis=1)
+                        idx = (cum <= u[:, None]).sum(axis=1)
+                        bad = (idx >= len(ks))
+                        idx = np.where(bad, np.argmax(w, axis=1), idx)
+                        bad |= w[np.arange(k), idx] <= 0
+                        idx = np.where(bad, np.argmax(w, axis=1), idx)
+                        wsel = w[np.arange(k), idx]
+                        mats_k = np.array([ks[a] / np.sqrt(b) for a, b in zip(idx, wsel)])
+                        run_slot(runner.kraus_seg[it.slot], mats_k, k, start)
+                    else:  # mid-circuit measurement
+                        op = it.op
+                        qm = list(op.qubits)
+                        m = len(qm)
+                        drawn = eng.points_sample(states, n, k, prng.random_sample(k)).astype(np.int64)
+                        outcome = np.zeros(k, dtype=np.int64)  # bit j <-> qm[j]
+                        for jq, q in enumerate(qm):
+                            outcome |= ((drawn >> (runner.n - 1 - runner.index[q])) & 1) << jq
+                        recs_z, masks = _z_subset_records(runner, qm)
+                        zv = np.real(eng.points_expect(states, n, k, Engine.pauli_records(recs_z)))  # (k, 2^m - 1)
+                        par = np.array([[bin(o & S).count("1") & 1 for S in masks] for o in range(1 << m)])
+                        sign = 1.0 - 2.0 * par  # (2^m, 2^m - 1)
+                        prob = (1.0 + np.einsum("pt,pt->p", zv, sign[outcome])) / (1 << m)
+                        prob = np.maximum(prob, 1e-30)
+                        # projector / sqrt(p) in the op's matrix order (qubit 0 most significant)
+                        d = 1 << m
+                        mats_k = np.zeros((k, d, d), dtype=np.complex128)
+                        for r in range(k):
+                            row = 0
+                            for jq in range(m):
+                                row |= ((int(outcome[r]) >> jq) & 1) << (m - 1 - jq)
+                            mats_k[r, row, row] = 1.0 / np.sqrt(prob[r])
+                        run_slot(proj[j], mats_k, k, start)
+                        inv = op.gate.full_invert_mask()
+                        for r in range(k):
+                            bits = [((int(outcome[r]) >> jq) & 1) ^ int(inv[jq]) for jq in range(m)]
+                            records[start + r].setdefault(cirq.measurement_key_name(op), []).append(bits)
+                if terminal:
+                    samples[start : start + k] = eng.points_sample(states, n, k, prng.random_sample(k))
+        finally:
+            states.free()
+        out = pad_records(records) if any(records) else {}
+        if terminal:
+            term = sim._records_from_samples(samples, runner.empty, terminal)
+            for key, v in term.items():
+                v8 = v.astype(np.uint8)
+                # a key measured mid-circuit and again at the end: more instances
+                out[key] = np.concatenate([out[key], v8], axis=1) if key in out else v8
+        return out
+    finally:
+        runner.close()

@@ -310,6 +310,12 @@ int gbq_run_points(gbq_ctx* ctx, gbq_c64* states, int nbits, int npoints, const 
                    int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, int64_t pool_stride);
 int gbq_points_expect(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints,
                       const gbq_pauli* terms, int nterms, double* out);
+/* One draw per point from |psi_p|^2: out[p] = the basis index where the
+ * cumulative probability first exceeds u[p] * sum |psi_p|^2 (the state's own
+ * norm; u in [0, 1)).  Batched trajectories: one sample per trajectory,
+ * the inverse-CDF rule of gbq_sample.  Host arrays: u, out. */
+int gbq_points_sample(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints, const double* u,
+                      uint64_t* out);
 
 #ifdef __cplusplus
 }

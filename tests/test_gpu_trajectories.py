@@ -225,3 +225,33 @@ def test_moment_steps_with_measurements_and_density_matrix():
         last = s.density_matrix()
     assert abs(np.trace(last) - 1) < 1e-5
     assert abs(np.real(last[3, 3]) - 0.75**2) < 1e-5
+
+
+def test_mixture_noise_runs_as_batched_trajectories():
+    """Mixture-only noise with terminal measurements: the repetitions are
+    evolved together (far fewer launches than repetitions) and sample the
+    density matrix's distribution."""
+    q = cirq.LineQubit.range(4)
+    body = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.depolarize(0.2).on(q[0]),
+        cirq.CNOT(q[0], q[1]),
+        cirq.bit_flip(0.15).on(q[1]),
+        cirq.ry(0.7).on(q[2]),
+        cirq.phase_flip(0.3).on(q[2]),
+        cirq.CZ(q[1], q[2]),
+        cirq.H(q[2]),
+        cirq.depolarize(0.1).on_each(*q),
+        cirq.CNOT(q[2], q[3]),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    rho = simulate_density_matrix(body, qubit_order=q)
+    p = np.clip(np.real(np.diag(rho)), 0, None)
+    probs = {tuple((i >> (3 - j)) & 1 for j in range(4)): p[i] for i in range(16)}
+    reps = 5000
+    sim = cirq_gb300.Simulator(seed=13)
+    l0 = sim.engine.launches()
+    res = sim.run(body + cirq.measure(*q, key="m"), repetitions=reps)
+    assert sim.engine.launches() - l0 < reps
+    assert res.records["m"].shape == (reps, 1, 4)
+    assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
