@@ -199,6 +199,7 @@ SIGNATURES = {
     "gbq_run_points": [_P, _P, _I, _I, _P, _I, _P, _I, _P, _I64],
     "gbq_points_expect": [_P, _P, _I, _I, _P, _I, _P],
     "gbq_points_sample": [_P, _P, _I, _I, _P, _P],
+    "gbq_points_rdm": [_P, _P, _I, _I, _I, _P, _P],
 }
 _RESTYPES = {"gbq_last_error": ctypes.c_char_p}
 

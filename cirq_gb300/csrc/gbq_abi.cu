@@ -1006,6 +1006,25 @@ int gbq_run_points(gbq_ctx* c, gbq_c64* states, int nbits, int npoints, const gb
   return GBQ_OK;
 }
 
+int gbq_points_rdm(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, int k, const int* bits,
+                   double* out) {
+  CHECK_CTX(c);
+  if (!states || nbits < 2 || nbits > 34 || npoints < 1 || npoints > 65535 || k < 1 || k > 2 || !bits || !out)
+    return arg_fail("gbq_points_rdm: bad arguments");
+  for (int q = 0; q < k; ++q)
+    if (bits[q] < 0 || bits[q] >= nbits) return arg_fail("gbq_points_rdm: bit out of range");
+  if (k == 2 && bits[0] == bits[1]) return arg_fail("gbq_points_rdm: bits must differ");
+  const size_t b = (size_t)npoints * (1u << (2 * k)) * 2 * sizeof(double);
+  int rc = ensure_scratch(c, b);
+  if (rc) return rc;
+  double* d_out = reinterpret_cast<double*>(c->scratch);
+  rc = points_rdm(c, reinterpret_cast<const float2*>(states), nbits, npoints, k, bits, d_out);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(out, d_out, b, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(rdm)");
+  return sync(c, "gbq_points_rdm");
+}
+
 int gbq_points_sample(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const double* u,
                       uint64_t* out) {
   CHECK_CTX(c);
@@ -1030,7 +1049,8 @@ int gbq_points_sample(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints,
 int gbq_points_expect(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const gbq_pauli* terms,
                       int nterms, double* out) {
   CHECK_CTX(c);
-  if (!states || nbits < 1 || nbits > 34 || npoints < 1 || nterms < 0 || (nterms && (!terms || !out)))
+  if (!states || nbits < 1 || nbits > 34 || npoints < 1 || npoints > 65535 || nterms < 0 ||
+      (nterms && (!terms || !out)))
     return arg_fail("gbq_points_expect: bad arguments");
   if (nterms == 0) return GBQ_OK;
   int rc = validate_terms(terms, nterms, nbits);

@@ -140,7 +140,81 @@ __global__ void __launch_bounds__(kPtThreads) k_points_sample(const float2* __re
   }
 }
 
+// Reduced density matrix of k <= 2 qubits for every point: block (chunk,
+// point) sums psi[i(c, j)] conj(psi[i(c, l)]) over its share of the other
+// index bits c and adds it to out[((p * D + j) * D + l) * 2 + {re, im}].
+// Matrix index bit k-1-q <-> global bit g[q] (q = 0 is the first qubit of
+// the channel, as in its Kraus matrices).
+template <int K>
+__global__ void __launch_bounds__(kPtThreads) k_points_rdm(const float2* __restrict__ states, int nbits, int g0,
+                                                          int g1, int chunk_bits, double* __restrict__ out) {
+  constexpr int D = 1 << K;
+  __shared__ double red[kPtThreads / 32];
+  const int p = blockIdx.y;
+  const float2* psi = states + ((int64_t)p << nbits);
+  const int glo = K == 1 ? g0 : (g0 < g1 ? g0 : g1), ghi = K == 1 ? g0 : (g0 < g1 ? g1 : g0);
+  float re[D][D], im[D][D];
+#pragma unroll
+  for (int j = 0; j < D; ++j)
+#pragma unroll
+    for (int l = 0; l < D; ++l) re[j][l] = im[j][l] = 0.f;
+  const uint64_t lo = (uint64_t)blockIdx.x << chunk_bits, hi = lo + (1ull << chunk_bits);
+  for (uint64_t c = lo + threadIdx.x; c < hi; c += kPtThreads) {
+    // insert zero bits at glo, then ghi
+    uint64_t base = ((c >> glo) << (glo + 1)) | (c & ((1ull << glo) - 1));
+    if (K == 2) base = ((base >> ghi) << (ghi + 1)) | (base & ((1ull << ghi) - 1));
+    float2 a[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      uint64_t idx = base;
+      if (K == 1) {
+        if (j & 1) idx |= 1ull << g0;
+      } else {
+        if (j & 2) idx |= 1ull << g0;
+        if (j & 1) idx |= 1ull << g1;
+      }
+      a[j] = psi[idx];
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        re[j][l] = fmaf(a[j].x, a[l].x, fmaf(a[j].y, a[l].y, re[j][l]));
+        im[j][l] = fmaf(a[j].y, a[l].x, fmaf(-a[j].x, a[l].y, im[j][l]));
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < D; ++j)
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      const double r = block_sum((double)re[j][l], red);
+      const double m = block_sum((double)im[j][l], red);
+      if (threadIdx.x == 0) {
+        double* o = out + (((int64_t)p * D + j) * D + l) * 2;
+        atomicAdd(o, r);
+        atomicAdd(o + 1, m);
+      }
+    }
+}
+
 }  // namespace
+
+int points_rdm(Ctx* c, const float2* states, int nbits, int npoints, int k, const int* g, double* d_out) {
+  const int D = 1 << k;
+  cudaError_t e = cudaMemsetAsync(d_out, 0, (size_t)npoints * D * D * 2 * sizeof(double), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rdm out)");
+  const int rest = nbits - k;
+  const int chunk_bits = rest < 16 ? rest : 16;
+  dim3 grid((unsigned)(1u << (rest - chunk_bits)), (unsigned)npoints, 1);
+  if (k == 1)
+    k_points_rdm<1><<<grid, kPtThreads, 0, c->stream>>>(states, nbits, g[0], g[0], chunk_bits, d_out);
+  else
+    k_points_rdm<2><<<grid, kPtThreads, 0, c->stream>>>(states, nbits, g[0], g[1], chunk_bits, d_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_points_rdm launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
 
 int points_sample(Ctx* c, const float2* states, int nbits, int npoints, const double* d_u,
                   unsigned long long* d_out) {

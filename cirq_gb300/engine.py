@@ -390,6 +390,17 @@ class Engine:
             "gbq_run_points",
         )
 
+    def points_rdm(self, states, nbits: int, npoints: int, bits) -> np.ndarray:
+        """(npoints, D, D) complex reduced density matrices of the global
+        index bits `bits` (bits[0] = most significant matrix index bit)."""
+        k = len(bits)
+        b = np.ascontiguousarray(bits, dtype=np.int32)
+        out = np.zeros(npoints * (1 << (2 * k)) * 2, dtype=np.float64)
+        check(self.lib.gbq_points_rdm(self.ctx, states.ptr, nbits, npoints, k, b.ctypes.data, out.ctypes.data),
+              "gbq_points_rdm")
+        d = 1 << k
+        return (out[0::2] + 1j * out[1::2]).reshape(npoints, d, d)
+
     def points_sample(self, states: DeviceBuffer, nbits: int, npoints: int, uniforms: np.ndarray) -> np.ndarray:
         """One basis index per point, drawn from |psi_p|^2."""
         u = np.ascontiguousarray(uniforms, dtype=np.float64)

@@ -21,11 +21,11 @@ plan each, compiled once), measurement events and general-channel events.
 Mixture operations stay inside the fused segments as :class:`Slot`s whose
 matrix is each trajectory's draw, so a noisy circuit keeps its fused passes;
 the draws of all repetitions are made up front and their matrix pools built
-in one vectorised call per segment.  A general channel on k <= 2 qubits
-reads the reduced density matrix of its qubits from the 4^k - 1 Pauli
-expectations of the state (rho_Q = 2^-k sum_P <P> P), computes the weights
-Tr(K_i^dagger K_i rho_Q) on the host, and applies the drawn operator as a
-one-slot segment.  The density-matrix simulator needs trajectories only for
+in one vectorised call per segment.  A general channel on k <= 5 qubits
+reads the reduced density matrix of its qubits (one batched state read for
+k <= 2; the 4^k - 1 Pauli expectations, rho_Q = 2^-k sum_P <P> P, for wider
+channels), computes the weights Tr(K_i^dagger K_i rho_Q) on the host, and
+applies the drawn operator as a one-slot segment.  The density-matrix simulator needs trajectories only for
 mid-circuit measurement (its channels are exact superoperators).
 """
 
@@ -112,8 +112,8 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
             nslot += 1
             continue
         if cirq.has_kraus(op):
-            if len(op.qubits) > 2:
-                raise UnsupportedOperation(f"channels on more than 2 qubits are not supported: {op!r}")
+            if len(op.qubits) > 5:
+                raise UnsupportedOperation(f"channels on more than 5 qubits are not supported: {op!r}")
             flush()
             items.append(Channel(op, nslot))
             nslot += 1
@@ -180,7 +180,6 @@ class TrajectoryRunner:
                 self.kraus_seg[it.slot] = slot_program(sim, it.op.qubits, self.qubits)
         self._kraus = {it.slot: [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(it.op)]
                        for it in self.items if isinstance(it, Channel)}
-        self._pauli = {it.slot: self._pauli_basis(it.op) for it in self.items if isinstance(it, Channel)}
         # device buffers reused by every trajectory: the state and one
         # matrix pool per segment / channel
         self._state = None
@@ -204,20 +203,25 @@ class TrajectoryRunner:
             self._state.free()
             self._state = None
 
-    # ---- host-side draws ---------------------------------------------------
-    def _draw_mixtures(self, reps: int) -> list[dict]:
-        prng = self.sim._prng
-        picks = [dict() for _ in range(reps)]
-        for it in self.items:
-            if not isinstance(it, Segment):
-                continue
-            for sid, op in it.slots:
-                probs, unitaries = zip(*cirq.mixture(op))
-                p = np.asarray(probs, dtype=np.float64)
-                choice = prng.choice(len(unitaries), size=reps, p=p / p.sum())
-                for r in range(reps):
-                    picks[r][sid] = unitaries[choice[r]]
-        return picks
+    def channel_bits(self, op) -> list:
+        """Global index bits of a channel's qubits (first qubit first)."""
+        return [self.n - 1 - self.index[q] for q in op.qubits]
+
+    def channel_rdm(self, states, nbits: int, npoints: int, op) -> np.ndarray:
+        """(npoints, d, d) reduced density matrices of a channel's qubits:
+        one state read per point for 1-2 qubits, the 4^k - 1 Pauli
+        expectations of the wider channels otherwise."""
+        eng = self.sim.engine
+        k = len(op.qubits)
+        if k <= 2:
+            return eng.points_rdm(states, nbits, npoints, self.channel_bits(op))
+        from cirq_gb300.engine import Engine
+
+        recs, mats = self._pauli_basis(op)
+        vals = np.real(eng.points_expect(states, nbits, npoints, Engine.pauli_records(recs)))
+        d = 2**k
+        rho = np.eye(d, dtype=np.complex128)[None] + np.einsum("pt,tij->pij", vals, np.array(mats))
+        return rho / d
 
     def _pauli_basis(self, op):
         """Pauli strings on the channel's qubits: (records, matrices)."""
@@ -239,6 +243,21 @@ class TrajectoryRunner:
             recs.append((x, zy, ny, 1.0))
             mats.append(m)
         return recs, mats
+
+    # ---- host-side draws ---------------------------------------------------
+    def _draw_mixtures(self, reps: int) -> list[dict]:
+        prng = self.sim._prng
+        picks = [dict() for _ in range(reps)]
+        for it in self.items:
+            if not isinstance(it, Segment):
+                continue
+            for sid, op in it.slots:
+                probs, unitaries = zip(*cirq.mixture(op))
+                p = np.asarray(probs, dtype=np.float64)
+                choice = prng.choice(len(unitaries), size=reps, p=p / p.sum())
+                for r in range(reps):
+                    picks[r][sid] = unitaries[choice[r]]
+        return picks
 
     # ---- one trajectory ------------------------------------------------------
     def run(self, initial_state, picks: dict, pools: list, rep: int):
@@ -273,13 +292,7 @@ class TrajectoryRunner:
     def _apply_kraus(self, state, it: Channel, picks: dict) -> None:
         eng = self.sim.engine
         ks = self._kraus[it.slot]
-        recs, mats = self._pauli[it.slot]
-        vals = np.real(eng.expect_paulis(state, self.n, recs))
-        k = len(it.op.qubits)
-        rho = np.eye(2**k, dtype=np.complex128)
-        for v, m in zip(vals, mats):
-            rho = rho + v * m
-        rho /= 2**k
+        rho = self.channel_rdm(state, self.empty.nbits_dev, 1, it.op)[0]
         weights = [max(float(np.real(np.trace(K.conj().T @ K @ rho))), 0.0) for K in ks]
         p = self.sim._prng.random()
         fallback = int(np.argmax(weights))
@@ -378,7 +391,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
         n = runner.empty.nbits_dev
         _, free, _ = eng.device_info()
         budget = max(1 << 28, min(int(free) // 2, 32 << 30))
-        chunk = max(1, min(reps, budget // (8 << n), (1 << 24) >> max(n - 10, 0)))
+        chunk = max(1, min(reps, 65535, budget // (8 << n), (1 << 24) >> max(n - 10, 0)))
         # one-slot programs of the mid-circuit measurements (projector slots)
         proj = {}
         for i, it in enumerate(body):
@@ -422,11 +435,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                         pool_dev.free()
                     elif isinstance(it, Channel):
                         ks = runner._kraus[it.slot]
-                        recs, mats = runner._pauli[it.slot]
-                        vals = np.real(eng.points_expect(states, n, k, Engine.pauli_records(recs)))  # (k, 4^q - 1)
-                        d = 2 ** len(it.op.qubits)
-                        rho = np.eye(d, dtype=np.complex128)[None] + np.einsum("pt,tij->pij", vals, np.array(mats))
-                        rho /= d
+                        rho = runner.channel_rdm(states, n, k, it.op)  # (k, d, d)
                         kk = np.array([K.conj().T @ K for K in ks])  # (nK, d, d)
                         w = np.clip(np.real(np.einsum("kij,pji->pk", kk, rho)), 0.0, None)  # (k, nK)
                         u = prng.random_sample(k)

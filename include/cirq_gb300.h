@@ -304,7 +304,7 @@ int gbq_batch_expect(gbq_ctx* ctx, const gbq_point* points, int npoints, const g
  * gbq_points_expect: out[(p * nterms + t) * 2 + {0, 1}] = (re, im) of
  *   <psi_p| i^ny X^x Z^zy |psi_p> (unit coefficients) for every point p and
  *   term t; terms with equal x should be adjacent (they share one read of
- *   the state).  Host arrays: terms, out. */
+ *   the state); npoints <= 65535.  Host arrays: terms, out. */
 int gbq_points_set_zero(gbq_ctx* ctx, gbq_c64* states, int nbits, int npoints);
 int gbq_run_points(gbq_ctx* ctx, gbq_c64* states, int nbits, int npoints, const gbq_pass* passes,
                    int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, int64_t pool_stride);
@@ -316,6 +316,13 @@ int gbq_points_expect(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoint
  * the inverse-CDF rule of gbq_sample.  Host arrays: u, out. */
 int gbq_points_sample(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints, const double* u,
                       uint64_t* out);
+/* Reduced density matrix of k = 1 or 2 qubits (global index bits bits[0..k-1];
+ * bits[0] is the most significant matrix index bit) for every point:
+ * out[((p * D + j) * D + l) * 2 + {0, 1}] = sum_c psi_p[i(c, j)] conj(psi_p[i(c, l)]),
+ * D = 2^k, npoints <= 65535.  Trajectory Kraus weights Tr(K^dagger K rho) read it (the weights
+ * ||K psi||^2 of cirq-core/cirq/sim/state_vector_simulation_state.py:206-257). */
+int gbq_points_rdm(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints, int k, const int* bits,
+                   double* out);
 
 #ifdef __cplusplus
 }

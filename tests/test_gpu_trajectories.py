@@ -255,3 +255,59 @@ def test_mixture_noise_runs_as_batched_trajectories():
     assert sim.engine.launches() - l0 < reps
     assert res.records["m"].shape == (reps, 1, 4)
     assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
+
+
+@pytest.mark.parametrize("bits", [[3], [0], [10], [7, 2], [2, 7], [10, 0]])
+def test_points_rdm_matches_partial_trace(bits):
+    """Batched reduced density matrices of one or two index bits against a
+    numpy partial trace, for several points at once."""
+    rng = np.random.default_rng(len(bits) * 31 + bits[0])
+    n, npts = 11, 3
+    psi = rng.normal(size=(npts, 1 << n)) + 1j * rng.normal(size=(npts, 1 << n))
+    psi /= np.linalg.norm(psi, axis=1, keepdims=True)
+    eng = cirq_gb300.Simulator().engine
+    states = eng.upload(psi.astype(np.complex64).reshape(-1))
+    got = eng.points_rdm(states, n, npts, bits)
+    k = len(bits)
+    for p in range(npts):
+        # axes of the reshaped state: axis a <-> global bit n - 1 - a
+        t = psi[p].reshape((2,) * n)
+        keep = [n - 1 - b for b in bits]
+        rest = [a for a in range(n) if a not in keep]
+        m = np.transpose(t, keep + rest).reshape(1 << k, -1)
+        want = m @ m.conj().T
+        assert np.max(np.abs(got[p] - want)) < 2e-6
+
+
+def _kraus_channel(ops):
+    return cirq.KrausChannel([np.asarray(k, dtype=np.complex128) for k in ops])
+
+
+@pytest.mark.parametrize("width", [2, 3])
+def test_general_kraus_channels_match_density_matrix(width):
+    """Non-mixture channels on two qubits (batched reduced density matrix)
+    and three qubits (Pauli-basis weights) sample the density matrix's
+    distribution."""
+    g = 0.35
+    ad = [np.array([[1, 0], [0, np.sqrt(1 - g)]]), np.array([[0, np.sqrt(g)], [0, 0]])]
+    ops = ad
+    for _ in range(width - 1):
+        ops = [np.kron(a, b) for a in ops for b in ad]
+    q = cirq.LineQubit.range(4)
+    body = cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.CNOT(q[0], q[1]),
+        cirq.ry(0.4).on(q[3]),
+        _kraus_channel(ops).on(*q[1 : 1 + width]),
+        cirq.CZ(q[1], q[2]),
+        cirq.H(q[2]),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    rho = simulate_density_matrix(body, qubit_order=q)
+    p = np.clip(np.real(np.diag(rho)), 0, None)
+    probs = {tuple((i >> (3 - j)) & 1 for j in range(4)): p[i] for i in range(16)}
+    reps = 3000
+    sim = cirq_gb300.Simulator(seed=5 + width)
+    res = sim.run(body + cirq.measure(*q, key="m"), repetitions=reps)
+    assert res.records["m"].shape == (reps, 1, 4)
+    assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
