@@ -42,6 +42,9 @@ __device__ __forceinline__ uint32_t phys_dev(uint32_t i) {
 
 // Register dense ops of width <= 2 use packed f32x2 FMAs (sm_100 family):
 // acc += m * a as two fma.rn.f32x2, m * (a.x, a.x) and (i m) * (a.y, a.y).
+#ifndef GBQ_SEL_UNROLL
+#define GBQ_SEL_UNROLL 1
+#endif
 #ifndef GBQ_FFMA2
 #define GBQ_FFMA2 1
 #endif
@@ -466,11 +469,8 @@ __device__ __forceinline__ uint32_t slot_phys(const RegState<LT, DUAL>& st, int 
   return p;
 }
 
-template <int LT, bool DUAL>
-__device__ __forceinline__ void phase_enter(RegState<LT, DUAL>& st, const OpDev& op,
-                                            const float2* smA, const float2* smB) {
-  constexpr int R = RegState<LT, DUAL>::R;
-  const int t = threadIdx.x;
+// Shared index and tile index of a thread's slot 0 in a layout.
+__device__ __forceinline__ uint32_t layout_entry(const OpDev& op, int t) {
   uint32_t ph = 0, ti = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j)
@@ -478,8 +478,18 @@ __device__ __forceinline__ void phase_enter(RegState<LT, DUAL>& st, const OpDev&
       ph ^= op.gcol[j];
       ti ^= op.tcol[j];
     }
-  st.phys_t = ph;
-  st.tidx = ti;
+  return ph | (ti << 16);
+}
+
+// lt: this thread's precomputed layout_entry, or ~0u to compute it here.
+template <int LT, bool DUAL>
+__device__ __forceinline__ void phase_enter(RegState<LT, DUAL>& st, const OpDev& op,
+                                            const float2* smA, const float2* smB,
+                                            uint32_t lt = ~0u) {
+  constexpr int R = RegState<LT, DUAL>::R;
+  if (lt == ~0u) lt = layout_entry(op, threadIdx.x);
+  st.phys_t = lt & 0xffffu;
+  st.tidx = lt >> 16;
 #pragma unroll
   for (int p = 0; p < R; ++p) st.pc[p] = op.pcol[p];
 #pragma unroll
@@ -505,11 +515,23 @@ __device__ __forceinline__ const float2* reg_matrix(const TileInfo& ti, const Op
                                                     const RegState<LT, DUAL>& st, uint64_t gbase,
                                                     int dd) {
   uint32_t sel = 0;
+#if GBQ_SEL_UNROLL
+  const int ns = op.nsel;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    if (s < ns) {
+      const int c = op.selg[s];
+      const uint32_t bit = c >= 0 ? (st.tidx >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
+      sel |= bit << s;
+    }
+  }
+#else
   for (int s = 0; s < op.nsel; ++s) {
     const int c = op.selg[s];
     const uint32_t bit = c >= 0 ? (st.tidx >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
     sel |= bit << s;
   }
+#endif
   return tile_mats(ti, gbase) + op.mat + (int64_t)sel * dd;
 }
 
@@ -526,7 +548,55 @@ __device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
   constexpr int REST = (A - 1) & ~MASK;
   const float2* mp = reg_matrix(ti, op, st, gbase, D * D);
   float part = 0.f;
-#if GBQ_FFMA2
+#if GBQ_FFMA2 == 2
+  if constexpr (K <= 2 && !PROBE) {
+    // Packed form with two accumulators per output: p = sum m * (a.x, a.x),
+    // q = sum m * (a.y, a.y); m a = (p.x - q.y, p.y + q.x).  No i m, and two
+    // chains of D f32x2 FMAs instead of one of 2D.
+    float2 m[D * D];
+#pragma unroll
+    for (int e = 0; e < D * D; e += 2) {
+      const float4 mm = __ldg(reinterpret_cast<const float4*>(mp + e));
+      m[e] = make_float2(mm.x, mm.y);
+      m[e + 1] = make_float2(mm.z, mm.w);
+    }
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_const(g, REST);
+      float2 ax[D], ay[D], bx[DUAL ? D : 1], by[DUAL ? D : 1];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const float2 a = st.v[s0 | dep_const(j, MASK)];
+        ax[j] = make_float2(a.x, a.x);
+        ay[j] = make_float2(a.y, a.y);
+        if constexpr (DUAL) {
+          const float2 b = st.w[s0 | dep_const(j, MASK)];
+          bx[j] = make_float2(b.x, b.x);
+          by[j] = make_float2(b.y, b.y);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 p = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          p = __ffma2_rn(m[r * D + c], ax[c], p);
+          q = __ffma2_rn(m[r * D + c], ay[c], q);
+        }
+        st.v[s0 | dep_const(r, MASK)] = make_float2(p.x - q.y, p.y + q.x);
+        if constexpr (DUAL) {
+          float2 pb = make_float2(0.f, 0.f), qb = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            pb = __ffma2_rn(m[r * D + c], bx[c], pb);
+            qb = __ffma2_rn(m[r * D + c], by[c], qb);
+          }
+          st.w[s0 | dep_const(r, MASK)] = make_float2(pb.x - qb.y, pb.y + qb.x);
+        }
+      }
+    }
+  } else
+#elif GBQ_FFMA2
   if constexpr (K <= 2 && !PROBE) {
     // Packed form: acc += m * a as two f32x2 FMAs, m * (a.x, a.x) and
     // (i m) * (a.y, a.y).
@@ -663,8 +733,10 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
   constexpr int R = RegState<LT, DUAL>::R;
   constexpr int A = RegState<LT, DUAL>::A;
   uint32_t base = 0;
-  for (int j = 0; j < op.k; ++j)
-    if (op.dext[j] >= 0) base |= (uint32_t)((gbase >> op.dext[j]) & 1u) << j;
+  const int nk = op.k;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (j < nk && op.dext[j] >= 0) base |= (uint32_t)((gbase >> op.dext[j]) & 1u) << j;
 #pragma unroll
   for (int b = 0; b < LT; ++b)
     if ((st.tidx >> b) & 1u) base ^= op.dcol[b];
@@ -729,12 +801,16 @@ __device__ __forceinline__ void ops_barrier() {
     __syncthreads();
 }
 
+// ltab (optional): ltab[q * kThreads + t] = layout_entry of the q-th layout
+// op of the pass for thread t, for q < nltab.
 template <int LT, int KMAX, bool DUAL, int RK = 4, bool NB = false>
 __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, float2* smA,
-                                        float2* smB, uint64_t gbase, int64_t tile, double* red) {
+                                        float2* smB, uint64_t gbase, int64_t tile, double* red,
+                                        const uint32_t* ltab = nullptr, int nltab = 0) {
   if constexpr (LT <= 12) {
     RegState<LT, DUAL> st;
     bool in_phase = false;
+    int nl = 0;
     for (int o = 0; o < ti.nops; ++o) {
       const OpDev& op = sops[o];
       const int kind = op.kind;
@@ -743,7 +819,8 @@ __device__ __forceinline__ void run_ops(const TileInfo& ti, const OpDev* sops, f
           phase_exit(st, smA, smB);
           ops_barrier<NB>();
         }
-        phase_enter(st, op, smA, smB);
+        phase_enter(st, op, smA, smB, nl < nltab ? ltab[nl * kThreads + threadIdx.x] : ~0u);
+        ++nl;
         in_phase = true;
       } else if (kind == GBQ_OP_RDENSE) {
         reg_dense_dispatch<LT, KMAX, DUAL, false, RK>(ti, op, st, gbase, tile, red);
@@ -906,6 +983,12 @@ constexpr int kWsStages = 3;
 constexpr int kWsProducers = 2;  // producer warps per CTA
 constexpr int kWsThreads = kThreads + 32 * kWsProducers;
 constexpr long kWsSpin = 1L << 26;
+// Layout ops whose per-thread (shared index, tile index) of slot 0 are
+// computed once per CTA (8 KB; two CTAs of 2^12 tiles still fit an SM).
+#ifndef GBQ_WS_LTABS
+#define GBQ_WS_LTABS 8
+#endif
+constexpr int kWsLayoutTabs = GBQ_WS_LTABS;
 
 __device__ __forceinline__ uint32_t ws_su32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -954,9 +1037,16 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_ws(const __grid_constant
   __shared__ __align__(8) uint64_t full[S], empty[S];
   __shared__ int abort_flag;
   __shared__ double red[kThreads / 32];
+  __shared__ uint32_t ltab[(kWsLayoutTabs > 0 ? kWsLayoutTabs : 1) * kThreads];  // consumers' layout entries
   float2* buf = reinterpret_cast<float2*>(smraw);  // [S][TS]
   const TileInfo& ti = a.ti;
   const int t = threadIdx.x;
+  int nltab = 0;
+  for (int o = 0; o < ti.nops && nltab < kWsLayoutTabs; ++o)
+    if (a.ops[o].kind == GBQ_OP_LAYOUT) {
+      if (t < kThreads) ltab[nltab * kThreads + t] = layout_entry(a.ops[o], t);
+      ++nltab;
+    }
   for (int e = t; e < 3 * kTileTab; e += kWsThreads) {
     const int part = e / kTileTab;
     ttab[e] = tile_base(ti, (int64_t)(e % kTileTab) << (8 * part));
@@ -1027,7 +1117,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_ws(const __grid_constant
       float2* sb = buf + (size_t)b * TS;
       const int64_t tile = blockIdx.x + i * step;
       const uint64_t gbase = tile_base_fast(ttab, tile);
-      run_ops<LT, 0, false, 2, true>(ti, a.ops, sb, nullptr, gbase, tile, red);
+      run_ops<LT, 0, false, 2, true>(ti, a.ops, sb, nullptr, gbase, tile, red, ltab, nltab);
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(ws_su32(&empty[b])) : "memory");
     }
   }
