@@ -189,8 +189,10 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
     sim = cirq_gb300.Simulator(**planner_kwargs)
     for _ in range(warmup):
         r = sim.simulate(circuit)
-        _ = r.final_state_vector
-        del r
+        vec = r.final_state_vector
+        # drop the result so that its pinned host buffer returns to the pool
+        # (a user's loop that keeps no result reuses one buffer per call)
+        del r, vec
     times = []
     vec_bytes = 0
     for _ in range(steps):
