@@ -15,7 +15,14 @@ library can be built without it.
 """
 
 __version__ = "0.1.0"
-__all__ = ["Simulator", "DensityMatrixSimulator"]
+__all__ = [
+    "Simulator",
+    "DensityMatrixSimulator",
+    "sample",
+    "sample_sweep",
+    "final_state_vector",
+    "final_density_matrix",
+]
 
 
 def __getattr__(name):
@@ -23,4 +30,8 @@ def __getattr__(name):
         from cirq_gb300 import simulator
 
         return getattr(simulator, name)
+    if name in ("sample", "sample_sweep", "final_state_vector", "final_density_matrix"):
+        from cirq_gb300 import mux
+
+        return getattr(mux, name)
     raise AttributeError(f"module 'cirq_gb300' has no attribute {name!r}")

@@ -1,0 +1,207 @@
+"""Module-level entry points of ``cirq.sim.mux`` on the GPU simulators.
+
+``cirq.sample``, ``cirq.sample_sweep``, ``cirq.final_state_vector`` and
+``cirq.final_density_matrix`` (cirq-core/cirq/sim/mux.py:53-333) build a
+fresh ``cirq.Simulator`` / ``cirq.DensityMatrixSimulator`` per call; the
+functions here keep their signatures, argument checks and error messages and
+run on :class:`cirq_gb300.Simulator` / :class:`cirq_gb300.DensityMatrixSimulator`
+instead.  Choices of simulator:
+
+* ``sample``: a noiseless circuit runs on the state-vector simulator
+  (mid-circuit measurements as trajectories); the reference sends Clifford
+  circuits to its tableau simulator and other measured circuits to the
+  density-matrix simulator.  The sample distribution is the same.
+  A noisy circuit runs on the density-matrix simulator up to
+  ``DM_MAX_QUBITS`` qubits, as in the reference, and as state-vector
+  trajectories above that (where a density matrix does not fit).
+* ``final_density_matrix``: unitary, unmeasured and noiseless -> the
+  state-vector simulator and an outer product on the host (mux.py:285-293);
+  otherwise the density-matrix simulator with measurements dephased
+  (mux.py:294-333).  Dephasing replaces each measured qubit by
+  ``phase_damp(1)``, the channel ``cirq.dephase_measurements`` inserts
+  (cirq-core/cirq/transformers/measurement_transformers.py:244-251),
+  without the measurement key that only records the Kraus index.
+
+Only ``dtype=np.complex64`` is accepted, as by the simulators.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from cirq_gb300._cirq_env import ensure_cirq
+
+cirq = ensure_cirq()
+
+DM_MAX_QUBITS = 14
+
+
+def _sv_sim(dtype, seed, noise=None):
+    from cirq_gb300.simulator import Simulator
+
+    return Simulator(dtype=dtype, seed=seed, noise=noise)
+
+
+def _dm_sim(dtype, seed, noise=None):
+    from cirq_gb300.simulator import DensityMatrixSimulator
+
+    return DensityMatrixSimulator(dtype=dtype, seed=seed, noise=noise)
+
+
+def _to_circuit(program) -> cirq.Circuit:
+    """Circuit, gate or OP_TREE -> Circuit (mux.py:97-106)."""
+    if isinstance(program, cirq.Circuit):
+        return program
+    if isinstance(program, cirq.Gate):
+        return cirq.Circuit(program.on(*cirq.LineQid.for_gate(program)))
+    return cirq.Circuit(program)
+
+
+def sample(
+    program: cirq.Circuit,
+    *,
+    noise: cirq.NOISE_MODEL_LIKE = None,
+    param_resolver: cirq.ParamResolver | None = None,
+    repetitions: int = 1,
+    dtype: type[np.complexfloating] = np.complex64,
+    seed: cirq.RANDOM_STATE_OR_SEED_LIKE = None,
+) -> cirq.Result:
+    """Samples the circuit's measurements (``cirq.sample``, mux.py:53-94)."""
+    noise_model = cirq.NoiseModel.from_noise_model_like(noise)
+    if noise_model == cirq.NO_NOISE:
+        return _sv_sim(dtype, seed).run(program, param_resolver=param_resolver, repetitions=repetitions)
+    if len(program.all_qubits()) <= DM_MAX_QUBITS:
+        sim = _dm_sim(dtype, seed, noise_model)
+    else:
+        sim = _sv_sim(dtype, seed, noise_model)
+    return sim.run(program, param_resolver=param_resolver, repetitions=repetitions)
+
+
+def sample_sweep(
+    program: cirq.Circuit,
+    params: cirq.Sweepable,
+    *,
+    noise: cirq.NOISE_MODEL_LIKE = None,
+    repetitions: int = 1,
+    dtype: type[np.complexfloating] = np.complex64,
+    seed: cirq.RANDOM_STATE_OR_SEED_LIKE = None,
+) -> list[cirq.Result]:
+    """One ``sample`` per resolver with a shared random state (mux.py:180-222)."""
+    prng = cirq.value.parse_random_state(seed)
+    return [
+        sample(program, noise=noise, param_resolver=r, repetitions=repetitions, dtype=dtype, seed=prng)
+        for r in cirq.to_resolvers(params)
+    ]
+
+
+def final_state_vector(
+    program: cirq.CIRCUIT_LIKE,
+    *,
+    initial_state: cirq.STATE_VECTOR_LIKE = 0,
+    param_resolver: cirq.ParamResolverOrSimilarType = None,
+    qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+    ignore_terminal_measurements: bool = False,
+    dtype: type[np.complexfloating] = np.complex64,
+    seed: cirq.RANDOM_STATE_OR_SEED_LIKE = None,
+) -> np.ndarray:
+    """Final state of a unitary program (``cirq.final_state_vector``,
+    mux.py:109-177).
+
+    Raises:
+        ValueError: the circuit contains a measurement (unless
+            ``ignore_terminal_measurements`` and they are terminal) or is not
+            unitary.
+    """
+    circuit_like = _to_circuit(program)
+    if not ignore_terminal_measurements:
+        if any(cirq.is_measurement(op) for op in circuit_like.all_operations()):
+            raise ValueError('Circuit contains a measurement.')
+    else:
+        circuit_like = cirq.drop_terminal_measurements(circuit_like)
+    if not cirq.has_unitary(cirq.resolve_parameters(circuit_like, param_resolver)):
+        raise ValueError(
+            "Program doesn't have a single well defined final state vector "
+            "because it is not unitary. "
+            "Maybe you wanted `cirq.final_density_matrix`?\n"
+            "\n"
+            f"Program: {circuit_like!r}"
+        )
+    result = _sv_sim(dtype, seed).simulate(
+        program=circuit_like,
+        initial_state=initial_state,
+        qubit_order=qubit_order,
+        param_resolver=param_resolver,
+    )
+    return result.state_vector()
+
+
+def _dephase(circuit: cirq.AbstractCircuit) -> cirq.Circuit:
+    """Measurements -> phase_damp(1) on each measured qubit; classically
+    controlled operations must have been deferred first."""
+
+    def dephase(op, _):
+        if isinstance(op.gate, cirq.MeasurementGate):
+            return [cirq.phase_damp(1).on(q) for q in op.qubits]
+        if isinstance(op, cirq.ClassicallyControlledOperation):
+            raise ValueError('Use cirq.defer_measurements first to remove classical controls.')
+        return op
+
+    return cirq.map_operations(circuit, dephase, deep=True).unfreeze()
+
+
+def final_density_matrix(
+    program: cirq.CIRCUIT_LIKE,
+    *,
+    noise: cirq.NOISE_MODEL_LIKE = None,
+    initial_state: cirq.STATE_VECTOR_LIKE = 0,
+    param_resolver: cirq.ParamResolverOrSimilarType = None,
+    qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
+    dtype: type[np.complexfloating] = np.complex64,
+    seed: int | np.random.RandomState | None = None,
+    ignore_measurement_results: bool = True,
+) -> np.ndarray:
+    """Final density matrix (``cirq.final_density_matrix``, mux.py:225-333):
+    measurements dephase unless ``ignore_measurement_results`` is False, in
+    which case they collapse with sampled outcomes."""
+    noise_model = cirq.NoiseModel.from_noise_model_like(noise)
+    circuit_like = _to_circuit(program)
+    can_do_unitary_simulation = cirq.has_unitary(circuit_like)
+    if isinstance(circuit_like, cirq.Circuit) and circuit_like.has_measurements():
+        can_do_unitary_simulation = False
+    if noise_model != cirq.NO_NOISE:
+        can_do_unitary_simulation = False
+
+    if can_do_unitary_simulation:
+        result = _sv_sim(dtype, seed).simulate(
+            program=circuit_like,
+            initial_state=initial_state,
+            qubit_order=qubit_order,
+            param_resolver=param_resolver,
+        )
+        return result.density_matrix_of()
+
+    has_classical_control = circuit_like != cirq.defer_measurements(circuit_like)
+    handling_classical_control = ignore_measurement_results and has_classical_control
+    if handling_classical_control:
+        noise_applied = circuit_like.with_noise(noise) if noise is not None else circuit_like
+        dephased = _dephase(cirq.defer_measurements(noise_applied))
+        prog = dephased
+    elif ignore_measurement_results:
+        prog = _dephase(circuit_like)
+    else:
+        prog = circuit_like
+    result = _dm_sim(dtype, seed, None if handling_classical_control else noise).simulate(
+        prog,
+        initial_state=initial_state,
+        qubit_order=qubit_order,
+        param_resolver=param_resolver,
+    )
+    rho = result.final_density_matrix
+    if handling_classical_control:
+        # the deferral's ancillas come after the circuit's own qubits
+        keep = list(range(cirq.num_qubits(circuit_like)))
+        shape = cirq.qid_shape(dephased)
+        reduced = cirq.partial_trace(np.reshape(rho, shape + shape), keep)
+        width = int(np.prod(cirq.qid_shape(circuit_like)))
+        rho = np.reshape(reduced, (width, width))
+    return rho
