@@ -113,12 +113,14 @@ def moment_steps(sim, circuit, param_resolver, qubit_order, initial_state) -> It
         yield step_cls(sim, state, qubits, {})
         return
     log: dict = {}  # the measurement log so far, as the reference's step results carry it
+    records: dict = {}  # every measurement so far (classical control reads it)
+    measured: dict = {}
     for moment in moments:
         ops = flatten_ops(cirq.Circuit(cirq.flatten_to_ops_or_moments([moment])))
         runner = tj.TrajectoryRunner(sim, ops, qubits, resolver)
         try:
             picks, pools = runner.prepare(1)
-            records = runner.apply(state, picks[0], pools, 0)
+            runner.apply(state, picks[0], pools, 0, records, measured)
         finally:
             runner.close()
         log.update({k: np.array(v[-1], dtype=np.uint8) for k, v in records.items()})

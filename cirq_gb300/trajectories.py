@@ -68,10 +68,39 @@ class Channel:
     slot: int
 
 
+@dataclasses.dataclass
+class Conditional:
+    """A classically controlled unitary: applied in a trajectory when all of
+    its conditions hold on that trajectory's records so far."""
+
+    op: Any  # the ClassicallyControlledOperation (untagged)
+    inner: Any  # the controlled unitary op
+
+
+def is_classically_controlled(op) -> bool:
+    return isinstance(op.untagged, cirq.ClassicallyControlledOperation)
+
+
+def conditions_hold(op, records: dict, measured: dict) -> bool:
+    """Evaluates a ClassicallyControlledOperation's conditions with the
+    reference's own Condition.resolve (cirq-core/cirq/value/condition.py)
+    on the trajectory's records: records[key] = [bits, ...] (as recorded,
+    invert masks applied), measured[key] = [qubits, ...] of each instance.
+    A condition on a key not measured yet raises ValueError, as the
+    reference does."""
+    keyed = {cirq.MeasurementKey.parse_serialized(k): [tuple(int(b) for b in bits) for bits in v]
+             for k, v in records.items()}
+    qubits = {cirq.MeasurementKey.parse_serialized(k): [tuple(q) for q in v] for k, v in measured.items()}
+    store = cirq.ClassicalDataDictionaryStore(_records=keyed, _measured_qubits=qubits)
+    return all(c.resolve(store) for c in op.classical_controls)
+
+
 def needs_trajectories(ops, dm: bool) -> bool:
     """True when a flattened op list cannot be simulated once and sampled."""
     seen_measure = False
     for op in ops:
+        if is_classically_controlled(op):
+            return True
         if cirq.is_measurement(op):
             seen_measure = True
             continue
@@ -97,6 +126,14 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
         cur, cur_slots = [], []
 
     for op in ops:
+        if is_classically_controlled(op):
+            cc = op.untagged
+            inner = cc.without_classical_controls()
+            if cirq.is_measurement(inner) or cirq.is_parameterized(inner) or not cirq.has_unitary(inner):
+                raise UnsupportedOperation(f"classical control of a non-unitary operation: {op!r}")
+            flush()
+            items.append(Conditional(cc, inner))
+            continue
         if cirq.is_measurement(op):
             if not isinstance(getattr(op, "gate", None), cirq.MeasurementGate):
                 raise NotImplementedError(f"unsupported measurement {op!r}")
@@ -171,7 +208,10 @@ class TrajectoryRunner:
         self.items, self.nslot = build_items(ops, self.dm)
         base = [cirq.ParamResolver({})]
         self.compiled = [
-            sim._compile(it.ops, self.qubits, base) if isinstance(it, Segment) else None for it in self.items
+            sim._compile(it.ops, self.qubits, base) if isinstance(it, Segment)
+            else sim._compile([it.inner], self.qubits, base) if isinstance(it, Conditional)
+            else None
+            for it in self.items
         ]
         self.empty = sim._compile([], self.qubits, base)  # geometry of the state buffer
         self.kraus_seg = {}
@@ -271,11 +311,16 @@ class TrajectoryRunner:
             sim._initial_device_state(self.empty, initial_state, into=self._state)
         return self._state, self.apply(self._state, picks, pools, rep)
 
-    def apply(self, state, picks: dict, pools: list, rep: int) -> dict:
-        """Applies the items to a device state in place; returns the records."""
+    def apply(self, state, picks: dict, pools: list, rep: int, records: dict | None = None,
+              measured: dict | None = None) -> dict:
+        """Applies the items to a device state in place; returns the records.
+        `records` / `measured` (key -> bits / qubits of each instance) carry
+        earlier measurements of the same trajectory, for classical control;
+        they are extended in place."""
         sim = self.sim
         eng = sim.engine
-        records: dict = {}
+        records = {} if records is None else records
+        measured = {} if measured is None else measured
         for j, it in enumerate(self.items):
             if isinstance(it, Segment):
                 c = self.compiled[j]
@@ -284,7 +329,13 @@ class TrajectoryRunner:
                     eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), pool))
             elif isinstance(it, Measure):
                 bits = sim._measure_op(state, self.empty, it.op)
-                records.setdefault(cirq.measurement_key_name(it.op), []).append(bits)
+                key = cirq.measurement_key_name(it.op)
+                records.setdefault(key, []).append(bits)
+                measured.setdefault(key, []).append(it.op.qubits)
+            elif isinstance(it, Conditional):
+                c = self.compiled[j]
+                if c.plan.npasses and conditions_hold(it.op, records, measured):
+                    eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), c.plan.pool))
             else:
                 self._apply_kraus(state, it, picks)
         return records
@@ -397,6 +448,10 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
         for i, it in enumerate(body):
             if isinstance(it, Measure):
                 proj[i] = slot_program(sim, it.op.qubits, runner.qubits)
+        # one-slot programs of the classically controlled unitaries
+        for i, it in enumerate(body):
+            if isinstance(it, Conditional):
+                proj[i] = slot_program(sim, it.inner.qubits, runner.qubits)
         states = eng.alloc((8 << n) * chunk)
         records: list = [dict() for _ in range(reps)]
         samples = np.empty(reps, dtype=np.int64)
@@ -418,6 +473,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
             for start in range(0, reps, chunk):
                 k = min(chunk, reps - start)
                 eng.points_set_zero(states, n, k)
+                measured: dict = {}  # key -> qubits of each instance (same for every trajectory)
                 for j, it in enumerate(body):
                     if isinstance(it, Segment):
                         c = runner.compiled[j]
@@ -433,6 +489,12 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                         eng.run_points(states, n, k, c.plan, pool_dev, plen)
                         eng.sync()
                         pool_dev.free()
+                    elif isinstance(it, Conditional):
+                        u = cirq.unitary(it.inner)
+                        eye = np.eye(u.shape[0], dtype=np.complex128)
+                        hold = [conditions_hold(it.op, records[start + r], measured) for r in range(k)]
+                        if any(hold):
+                            run_slot(proj[j], np.array([u if h else eye for h in hold]), k, start)
                     elif isinstance(it, Channel):
                         ks = runner._kraus[it.slot]
                         rho = runner.channel_rdm(states, n, k, it.op)  # (k, d, d)
@@ -472,9 +534,11 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                             mats_k[r, row, row] = 1.0 / np.sqrt(prob[r])
                         run_slot(proj[j], mats_k, k, start)
                         inv = op.gate.full_invert_mask()
+                        key = cirq.measurement_key_name(op)
+                        measured.setdefault(key, []).append(op.qubits)
                         for r in range(k):
                             bits = [((int(outcome[r]) >> jq) & 1) ^ int(inv[jq]) for jq in range(m)]
-                            records[start + r].setdefault(cirq.measurement_key_name(op), []).append(bits)
+                            records[start + r].setdefault(key, []).append(bits)
                 if terminal:
                     samples[start : start + k] = eng.points_sample(states, n, k, prng.random_sample(k))
         finally:

@@ -311,3 +311,54 @@ def test_general_kraus_channels_match_density_matrix(width):
     res = sim.run(body + cirq.measure(*q, key="m"), repetitions=reps)
     assert res.records["m"].shape == (reps, 1, 4)
     assert _pvalue(_counts(res, ["m"]), probs, reps) > 1e-3
+
+
+def _teleport_like():
+    q = cirq.LineQubit.range(3)
+    return q, cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.measure(q[0], key="a"),
+        cirq.X(q[1]).with_classical_controls("a"),
+        cirq.ry(0.9).on(q[2]),
+        cirq.measure(q[2], key="c"),
+        cirq.CNOT(q[1], q[2]).with_classical_controls("c"),
+        cirq.measure(q[1], q[2], key="m"),
+        strategy=cirq.InsertStrategy.NEW,
+    )
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_classical_control_in_run(dm):
+    """Records follow the controls exactly: m[0] = a, m[1] = c xor (c and a)
+    (the controlled CNOT flips q2 when c and q1 = a are both 1)."""
+    q, c = _teleport_like()
+    sim = cirq_gb300.DensityMatrixSimulator(seed=4) if dm else cirq_gb300.Simulator(seed=4)
+    reps = 400 if dm else 3000
+    res = sim.run(c, repetitions=reps)
+    a = res.records["a"][:, 0, 0]
+    cc = res.records["c"][:, 0, 0]
+    m = res.records["m"][:, 0, :]
+    np.testing.assert_array_equal(m[:, 0], a)
+    np.testing.assert_array_equal(m[:, 1], cc ^ (cc & a))
+    assert 0.4 < a.mean() < 0.6
+    assert abs(cc.mean() - np.sin(0.45) ** 2) < (0.08 if dm else 0.04)
+
+
+def test_classical_control_in_simulate_and_moment_steps():
+    q, c = _teleport_like()
+    body = c[:-1]
+    for seed in range(6):
+        r = cirq_gb300.Simulator(seed=seed).simulate(body)
+        a = int(r.measurements["a"][0])
+        cc = int(r.measurements["c"][0])
+        want = np.zeros(8)
+        want[(a << 2) | (a << 1) | (cc ^ (cc & a))] = 1  # q0 collapsed to a
+        got = np.abs(r.final_state_vector) ** 2
+        np.testing.assert_allclose(got, want, atol=1e-5)
+        steps = list(cirq_gb300.Simulator(seed=seed).simulate_moment_steps(body))
+        last = steps[-1]
+        a2 = int(last.measurements["a"][0])
+        c2 = int(last.measurements["c"][0])
+        want2 = np.zeros(8)
+        want2[(a2 << 2) | (a2 << 1) | (c2 ^ (c2 & a2))] = 1
+        np.testing.assert_allclose(np.abs(last.state_vector()) ** 2, want2, atol=1e-5)

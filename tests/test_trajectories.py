@@ -75,3 +75,57 @@ def test_pad_records_matches_reference_layout():
     assert out["a"].shape == (2, 2, 2) and out["a"].dtype == np.uint8
     assert out["a"][0, 0].tolist() == [1, 0] and out["a"][0, 1].tolist() == [0, 0]
     assert out["b"].shape == (2, 1, 1) and out["b"][1, 0, 0] == 0
+
+
+def test_classical_control_becomes_a_conditional_item():
+    q = cirq.LineQubit.range(3)
+    c = cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.measure(q[0], key="a"),
+        cirq.X(q[1]).with_classical_controls("a"),
+        cirq.CNOT(q[1], q[2]),
+    )
+    ops = flatten_ops(c)
+    assert tj.needs_trajectories(ops, dm=False) and tj.needs_trajectories(ops, dm=True)
+    items, _ = tj.build_items(ops, dm=False)
+    kinds = [type(it).__name__ for it in items]
+    assert kinds == ["Segment", "Measure", "Conditional", "Segment"]
+    assert items[2].inner == cirq.X(q[1])
+    # a controlled channel has no unitary to apply per trajectory
+    bad = flatten_ops(cirq.Circuit(cirq.measure(q[0], key="a"),
+                                   cirq.amplitude_damp(0.1).on(q[1]).with_classical_controls("a")))
+    try:
+        tj.build_items(bad, dm=False)
+    except tj.UnsupportedOperation:
+        pass
+    else:
+        raise AssertionError("expected UnsupportedOperation")
+
+
+def test_conditions_resolve_like_the_reference():
+    q = cirq.LineQubit.range(3)
+    op = cirq.X(q[2]).with_classical_controls("a")
+    measured = {"a": [(q[0], q[1])]}
+    assert not tj.conditions_hold(op, {"a": [[0, 0]]}, measured)
+    assert tj.conditions_hold(op, {"a": [[0, 1]]}, measured)
+    # the latest instance of a repeated key decides
+    assert not tj.conditions_hold(op, {"a": [[1, 0], [0, 0]]}, {"a": measured["a"] * 2})
+    # several conditions must all hold; sympy conditions read the integer value
+    op2 = cirq.X(q[2]).with_classical_controls("a", "b")
+    rec = {"a": [[1, 0]], "b": [[0]]}
+    mq = {"a": [(q[0], q[1])], "b": [(q[2],)]}
+    assert not tj.conditions_hold(op2, rec, mq)
+    rec["b"] = [[1]]
+    assert tj.conditions_hold(op2, rec, mq)
+    import sympy
+
+    op3 = cirq.X(q[2]).with_classical_controls(sympy.Eq(sympy.Symbol("a"), 2))
+    assert tj.conditions_hold(op3, {"a": [[1, 0]]}, measured)
+    assert not tj.conditions_hold(op3, {"a": [[1, 1]]}, measured)
+    # a key that was never measured: the reference's ValueError
+    try:
+        tj.conditions_hold(cirq.X(q[2]).with_classical_controls("zz"), {"a": [[1, 0]]}, measured)
+    except ValueError:
+        pass
+    else:
+        raise AssertionError("expected ValueError")
