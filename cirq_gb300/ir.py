@@ -65,14 +65,36 @@ def qubit_positions(qubits: Sequence[Any]) -> dict:
     return {q: i for i, q in enumerate(qubits)}
 
 
+MAX_OP_QUBITS = 5
+
+
+def _wide_unitary(op) -> bool:
+    cirq = _cirq()
+    return (
+        len(op.qubits) > MAX_OP_QUBITS
+        and not cirq.is_measurement(op)
+        and not isinstance(op.untagged, cirq.ClassicallyControlledOperation)
+        and cirq.has_unitary(op)
+    )
+
+
 def flatten_ops(circuit) -> list:
-    """All operations of a resolved circuit in moment order (CircuitOperations unrolled)."""
+    """All operations of a resolved circuit in moment order (CircuitOperations
+    unrolled).  A unitary on more than 5 qubits (a multi-controlled gate, a
+    wide MatrixGate with a decomposition) is replaced by the reference's own
+    exact decomposition (``cirq.decompose``, which keeps global phases) into
+    operations of at most 5 qubits; one without a decomposition is kept and
+    rejected by the compiler."""
     cirq = _cirq()
     ops = []
     for moment in circuit:
         for op in moment:
             if isinstance(op.untagged, cirq.CircuitOperation):
                 ops.extend(flatten_ops(op.untagged.mapped_circuit(deep=True)))
+            elif _wide_unitary(op):
+                ops.extend(
+                    cirq.decompose(op, keep=lambda o: len(o.qubits) <= MAX_OP_QUBITS, on_stuck_raise=None)
+                )
             else:
                 ops.append(op)
     return ops

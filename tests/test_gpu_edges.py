@@ -116,3 +116,18 @@ def test_grid_and_named_qubits_keep_the_reference_order():
     np.testing.assert_allclose(ours.final_state_vector, ref.final_state_vector, atol=1e-6)
     rho = cirq_gb300.DensityMatrixSimulator().simulate(c).final_density_matrix
     np.testing.assert_allclose(rho, simulate_density_matrix(c), atol=1e-6)
+
+
+def test_multi_controlled_gates_beyond_five_qubits():
+    q = cirq.LineQubit.range(8)
+    c = cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.X(q[6]).controlled_by(*q[:6]),
+        cirq.rz(0.3).on(q[7]).controlled_by(*q[1:6]),
+        cirq.CZ(q[0], q[7]),
+    )
+    got = cirq_gb300.Simulator().simulate(c).final_state_vector
+    want = simulate_state_vector(c)
+    assert np.max(np.abs(got - want)) < 2e-6
+    rho = cirq_gb300.DensityMatrixSimulator().simulate(c).final_density_matrix
+    assert np.max(np.abs(rho - np.outer(want, want.conj()))) < 2e-6

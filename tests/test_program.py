@@ -129,3 +129,25 @@ def test_register_layouts_are_complete():
                         assert int(c) not in regs
                 elif o["kind"] in (0, 1, 2, 3):
                     regs = None
+
+
+def test_wide_unitaries_are_decomposed_exactly():
+    """A 7-qubit multi-controlled gate (beyond the 5-qubit op limit) goes
+    through the reference's own decomposition; the plan still matches the
+    oracle's direct application of the 7-qubit unitary."""
+    from cirq_gb300.ir import flatten_ops
+
+    q = cirq.LineQubit.range(8)
+    c = cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.X(q[6]).controlled_by(*q[:6]),
+        cirq.rz(0.3).on(q[7]).controlled_by(*q[1:6]),
+        cirq.CZ(q[0], q[7]),
+    )
+    ops = flatten_ops(c)
+    assert max(len(o.qubits) for o in ops) <= 5
+    compiled = CompiledCircuit(ops, q, dm=False, planner=Planner(tile_bits=10, kmax=4),
+                               resolvers=[cirq.ParamResolver({})])
+    got = _emulate(compiled)[: 2**8]
+    want = simulate_state_vector(c, qubit_order=q)
+    assert np.max(np.abs(got - want)) < 1e-6
