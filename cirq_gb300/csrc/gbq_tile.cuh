@@ -42,9 +42,6 @@ __device__ __forceinline__ uint32_t phys_dev(uint32_t i) {
 
 // Register dense ops of width <= 2 use packed f32x2 FMAs (sm_100 family):
 // acc += m * a as two fma.rn.f32x2, m * (a.x, a.x) and (i m) * (a.y, a.y).
-#ifndef GBQ_SEL_UNROLL
-#define GBQ_SEL_UNROLL 1
-#endif
 #ifndef GBQ_FFMA2
 #define GBQ_FFMA2 1
 #endif
@@ -515,7 +512,6 @@ __device__ __forceinline__ const float2* reg_matrix(const TileInfo& ti, const Op
                                                     const RegState<LT, DUAL>& st, uint64_t gbase,
                                                     int dd) {
   uint32_t sel = 0;
-#if GBQ_SEL_UNROLL
   const int ns = op.nsel;
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
@@ -525,13 +521,6 @@ __device__ __forceinline__ const float2* reg_matrix(const TileInfo& ti, const Op
       sel |= bit << s;
     }
   }
-#else
-  for (int s = 0; s < op.nsel; ++s) {
-    const int c = op.selg[s];
-    const uint32_t bit = c >= 0 ? (st.tidx >> c) & 1u : (uint32_t)((gbase >> (-c - 1)) & 1u);
-    sel |= bit << s;
-  }
-#endif
   return tile_mats(ti, gbase) + op.mat + (int64_t)sel * dd;
 }
 
@@ -548,55 +537,7 @@ __device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
   constexpr int REST = (A - 1) & ~MASK;
   const float2* mp = reg_matrix(ti, op, st, gbase, D * D);
   float part = 0.f;
-#if GBQ_FFMA2 == 2
-  if constexpr (K <= 2 && !PROBE) {
-    // Packed form with two accumulators per output: p = sum m * (a.x, a.x),
-    // q = sum m * (a.y, a.y); m a = (p.x - q.y, p.y + q.x).  No i m, and two
-    // chains of D f32x2 FMAs instead of one of 2D.
-    float2 m[D * D];
-#pragma unroll
-    for (int e = 0; e < D * D; e += 2) {
-      const float4 mm = __ldg(reinterpret_cast<const float4*>(mp + e));
-      m[e] = make_float2(mm.x, mm.y);
-      m[e + 1] = make_float2(mm.z, mm.w);
-    }
-#pragma unroll
-    for (int g = 0; g < NG; ++g) {
-      const int s0 = dep_const(g, REST);
-      float2 ax[D], ay[D], bx[DUAL ? D : 1], by[DUAL ? D : 1];
-#pragma unroll
-      for (int j = 0; j < D; ++j) {
-        const float2 a = st.v[s0 | dep_const(j, MASK)];
-        ax[j] = make_float2(a.x, a.x);
-        ay[j] = make_float2(a.y, a.y);
-        if constexpr (DUAL) {
-          const float2 b = st.w[s0 | dep_const(j, MASK)];
-          bx[j] = make_float2(b.x, b.x);
-          by[j] = make_float2(b.y, b.y);
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        float2 p = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int c = 0; c < D; ++c) {
-          p = __ffma2_rn(m[r * D + c], ax[c], p);
-          q = __ffma2_rn(m[r * D + c], ay[c], q);
-        }
-        st.v[s0 | dep_const(r, MASK)] = make_float2(p.x - q.y, p.y + q.x);
-        if constexpr (DUAL) {
-          float2 pb = make_float2(0.f, 0.f), qb = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            pb = __ffma2_rn(m[r * D + c], bx[c], pb);
-            qb = __ffma2_rn(m[r * D + c], by[c], qb);
-          }
-          st.w[s0 | dep_const(r, MASK)] = make_float2(pb.x - qb.y, pb.y + qb.x);
-        }
-      }
-    }
-  } else
-#elif GBQ_FFMA2
+#if GBQ_FFMA2
   if constexpr (K <= 2 && !PROBE) {
     // Packed form: acc += m * a as two f32x2 FMAs, m * (a.x, a.x) and
     // (i m) * (a.y, a.y).
