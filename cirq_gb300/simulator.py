@@ -138,7 +138,12 @@ class _GpuSimulatorBase:
         c = CompiledCircuit(body_ops, qubits, dm=self._dm, planner=planner, resolvers=resolvers[:1])
         self._cache[key] = c
         if len(self._cache) > _MAX_CACHE:
-            self._cache.popitem(last=False)
+            _, old = self._cache.popitem(last=False)
+            # its CUDA-graph runner (state and pool buffers, graph) goes with it
+            runner = self._runners.pop(id(old), None)
+            if runner is not None and runner[0] is old:
+                runner[1].free()
+                runner[2].free()
         return c
 
     def _prepare(self, program, qubit_order, params):

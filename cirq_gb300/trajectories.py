@@ -178,6 +178,9 @@ def circuit_ops(sim, program, qubits, resolver):
     return flatten_ops(resolved)
 
 
+_MAX_SLOT_PROGRAMS = 256  # one-op programs kept per simulator
+
+
 def slot_program(sim, op_qubits, qubits):
     """A compiled one-op program whose matrix each trajectory supplies as
     pick 0 (a Kraus operator or a projector), cached per simulator by the
@@ -186,6 +189,8 @@ def slot_program(sim, op_qubits, qubits):
     key = (tuple(op_qubits), tuple(qubits))
     c = cache.get(key)
     if c is None:
+        if len(cache) >= _MAX_SLOT_PROGRAMS:
+            cache.clear()
         from cirq_gb300.program import CompiledCircuit
 
         op = cirq.IdentityGate(len(op_qubits)).on(*op_qubits)

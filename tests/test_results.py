@@ -33,3 +33,28 @@ def test_density_matrix_result_hands_over_the_downloaded_matrix():
     # the reference's merged-state accessor still sees the same tensor
     np.testing.assert_allclose(res._get_merged_sim_state().target_tensor.reshape(4, 4), rho)
     assert "final density matrix" in str(res).lower()
+
+
+def test_cache_eviction_releases_graph_runners():
+    """With CUDA graphs, a compiled circuit's runner (its state and pool
+    buffers and graph) is released when the LRU cache evicts the circuit."""
+    import cirq_gb300
+    from cirq_gb300 import simulator as S
+
+    class FakeBuffer:
+        def __init__(self):
+            self.freed = False
+
+        def free(self):
+            self.freed = True
+
+    sim = cirq_gb300.Simulator(use_cuda_graphs=True)
+    q = cirq.LineQubit.range(3)
+    first = sim._compile([cirq.H(q[0])], q, [cirq.ParamResolver({})])
+    bufs = (FakeBuffer(), FakeBuffer())
+    sim._runners[id(first)] = (first, bufs[0], bufs[1], object())
+    for i in range(S._MAX_CACHE):
+        sim._compile([cirq.rx(0.1 * (i + 1)).on(q[i % 3])] * (i + 2), q, [cirq.ParamResolver({})])
+    assert id(first) not in sim._runners
+    assert all(b.freed for b in bufs)
+    assert len(sim._cache) == S._MAX_CACHE
