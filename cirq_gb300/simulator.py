@@ -293,6 +293,31 @@ class _GpuSimulatorBase:
         finally:
             runner.close()
 
+    def _unwrap_initial_state(self, initial_state, qubit_order):
+        """A ``cirq.SimulationStateBase`` initial state -> (its raw tensor,
+        its own qubit order).  As in the reference
+        (``SimulatorBase._create_simulation_state``,
+        cirq-core/cirq/sim/simulator_base.py:322-352, which uses such a state
+        as is), the state's qubits and their order define the simulation;
+        product states are merged first.  Other initial states pass through."""
+        if not isinstance(initial_state, cirq.SimulationStateBase):
+            return initial_state, qubit_order
+        merged = initial_state.create_merged_state()
+        qubits = tuple(merged.qubits)
+        if any(q.dimension != 2 for q in qubits):
+            raise NotImplementedError("only qubit initial states are supported")
+        n = len(qubits)
+        tensor = np.asarray(merged.target_tensor)
+        if isinstance(merged, cirq.DensityMatrixSimulationState):
+            if not self._dm:
+                raise ValueError("a density-matrix initial state needs cirq_gb300.DensityMatrixSimulator")
+            raw = tensor.reshape(2**n, 2**n)
+        elif isinstance(merged, cirq.StateVectorSimulationState):
+            raw = tensor.reshape(-1)
+        else:
+            raise NotImplementedError(f"initial states of type {type(merged).__name__} are not supported")
+        return raw, cirq.QubitOrder.explicit(qubits)
+
     # ---- SimulatesIntermediateState ------------------------------------------
     def simulate_moment_steps(
         self,
@@ -306,6 +331,7 @@ class _GpuSimulatorBase:
         (cirq-core/cirq/sim/simulator.py:607-640); see cirq_gb300/steps.py."""
         from cirq_gb300.steps import moment_steps
 
+        initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         return moment_steps(self, circuit, param_resolver, qubit_order, initial_state)
 
     def _traj_expectations(self, program, pslist, params, qubit_order, initial_state):
@@ -474,7 +500,7 @@ class Simulator(
                 raise ValueError(f"initial_state {initial_state} out of range for {n} qubits")
             return eng.new_state(n, basis=int(initial_state), nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
-            raise NotImplementedError("cirq_gb300.Simulator takes raw initial states, not SimulationState")
+            raise NotImplementedError("unwrap SimulationState initial states first")
         vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
         return eng.new_state(n, initial=vec, nbits_dev=compiled.nbits_dev, into=into)
 
@@ -485,6 +511,7 @@ class Simulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.StateVectorTrialResult]:
+        initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine
@@ -525,6 +552,7 @@ class Simulator(
         """Mirrors Simulator.simulate_expectation_values_sweep_iter
         (cirq-core/cirq/sim/sparse_simulator.py:193-218): expectation values are
         evaluated on the device from the final state, which never leaves HBM."""
+        initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if not permit_terminal_measurements and program.are_any_measurements_terminal():
             raise ValueError(
                 "Provided circuit has terminal measurements, which may "
@@ -603,7 +631,7 @@ class DensityMatrixSimulator(
             i = int(initial_state)
             return eng.new_state(2 * n, basis=(i << n) | i, nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
-            raise NotImplementedError("takes raw initial states, not SimulationState")
+            raise NotImplementedError("unwrap SimulationState initial states first")
         rho = cirq.to_valid_density_matrix(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
         return eng.new_state(2 * n, initial=rho.reshape(-1), nbits_dev=compiled.nbits_dev, into=into)
 
@@ -614,6 +642,7 @@ class DensityMatrixSimulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.DensityMatrixTrialResult]:
+        initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine
@@ -654,6 +683,7 @@ class DensityMatrixSimulator(
         """Mirrors DensityMatrixSimulator.simulate_expectation_values_sweep_iter
         (cirq-core/cirq/sim/density_matrix_simulator.py:204-236): Tr(P rho)
         is evaluated on the device."""
+        initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if not permit_terminal_measurements and program.are_any_measurements_terminal():
             raise ValueError(
                 "Provided circuit has terminal measurements, which may "

@@ -131,3 +131,21 @@ def test_multi_controlled_gates_beyond_five_qubits():
     assert np.max(np.abs(got - want)) < 2e-6
     rho = cirq_gb300.DensityMatrixSimulator().simulate(c).final_density_matrix
     assert np.max(np.abs(rho - np.outer(want, want.conj()))) < 2e-6
+
+
+def test_simulation_state_initial_states():
+    c = workloads.random_layer_circuit(4, 3, seed=8)
+    qs = sorted(c.all_qubits())
+    order = [qs[3], qs[1], qs[0], qs[2]]
+    st = cirq.StateVectorSimulationState(qubits=order, initial_state=9, dtype=np.complex64)
+    r = cirq_gb300.Simulator().simulate(c, initial_state=st)
+    want = simulate_state_vector(c, qubit_order=order, initial_state=9)
+    assert np.max(np.abs(r.final_state_vector - want)) < 2e-6
+    assert r.qubit_map == {qq: i for i, qq in enumerate(order)}
+    # a product state from the reference's own simulator, and the density matrix
+    prod = cirq.Simulator()._create_simulation_state(5, qs)
+    r = cirq_gb300.Simulator().simulate(c, initial_state=prod)
+    assert np.max(np.abs(r.final_state_vector - simulate_state_vector(c, initial_state=5))) < 2e-6
+    dst = cirq.DensityMatrixSimulationState(qubits=qs, initial_state=5, dtype=np.complex64)
+    rho = cirq_gb300.DensityMatrixSimulator().simulate(c, initial_state=dst).final_density_matrix
+    assert np.max(np.abs(rho - simulate_density_matrix(c, initial_state=5))) < 2e-6

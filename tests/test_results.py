@@ -58,3 +58,33 @@ def test_cache_eviction_releases_graph_runners():
     assert id(first) not in sim._runners
     assert all(b.freed for b in bufs)
     assert len(sim._cache) == S._MAX_CACHE
+
+
+def test_simulation_state_initial_states_are_unwrapped():
+    """A cirq SimulationState initial state -> its tensor and its own qubit
+    order (the reference simulates such a state as is)."""
+    import cirq_gb300
+
+    q = cirq.LineQubit.range(3)
+    order = [q[2], q[0], q[1]]
+    sv = cirq.StateVectorSimulationState(qubits=order, initial_state=5, dtype=np.complex64)
+    sim = cirq_gb300.Simulator()
+    raw, qo = sim._unwrap_initial_state(sv, cirq.QubitOrder.DEFAULT)
+    assert raw.shape == (8,) and raw[5] == 1
+    assert tuple(qo.order_for(q)) == tuple(order)
+    # a product state (the reference's default split_untangled_states) is merged
+    prod = cirq.Simulator(split_untangled_states=True)._create_simulation_state(6, q)
+    raw, qo = sim._unwrap_initial_state(prod, cirq.QubitOrder.DEFAULT)
+    assert raw.shape == (8,) and abs(raw[6] - 1) < 1e-7
+    # density-matrix states: accepted by the density-matrix simulator only
+    dm = cirq.DensityMatrixSimulationState(qubits=q, initial_state=2, dtype=np.complex64)
+    raw, _ = cirq_gb300.DensityMatrixSimulator()._unwrap_initial_state(dm, cirq.QubitOrder.DEFAULT)
+    assert raw.shape == (8, 8) and raw[2, 2] == 1
+    try:
+        sim._unwrap_initial_state(dm, cirq.QubitOrder.DEFAULT)
+    except ValueError:
+        pass
+    else:
+        raise AssertionError("expected ValueError")
+    # raw states pass through
+    assert sim._unwrap_initial_state(3, "x") == (3, "x")
