@@ -269,6 +269,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    _cirq()  # the reference install under baseline/_ref
     circuit, ngates = build_workload(args.n, args.depth, args.seed)
     vals = []
     desc = ""
