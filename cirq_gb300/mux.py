@@ -12,15 +12,16 @@ instead.  Choices of simulator:
   circuits to its tableau simulator and other measured circuits to the
   density-matrix simulator.  The sample distribution is the same.
   A noisy circuit runs on the density-matrix simulator up to
-  ``DM_MAX_QUBITS`` qubits, as in the reference, and as state-vector
-  trajectories above that (where a density matrix does not fit).
+  ``DM_MAX_QUBITS`` qubits, as in the reference, and above that (where a
+  density matrix does not fit) as state-vector trajectories of the circuit
+  with its noise placed where the density-matrix simulator places it.
 * ``final_density_matrix``: unitary, unmeasured and noiseless -> the
   state-vector simulator and an outer product on the host (mux.py:285-293);
   otherwise the density-matrix simulator with measurements dephased
-  (mux.py:294-333).  Dephasing replaces each measured qubit by
-  ``phase_damp(1)``, the channel ``cirq.dephase_measurements`` inserts
-  (cirq-core/cirq/transformers/measurement_transformers.py:244-251),
-  without the measurement key that only records the Kraus index.
+  (mux.py:294-333) by the reference's own ``cirq.dephase_measurements``
+  (cirq-core/cirq/transformers/measurement_transformers.py:217-256), whose
+  keyed ``phase_damp(1)`` channels lose their key (it only records the
+  Kraus index).
 
 Only ``dtype=np.complex64`` is accepted, as by the simulators.
 """
@@ -70,11 +71,13 @@ def sample(
     noise_model = cirq.NoiseModel.from_noise_model_like(noise)
     if noise_model == cirq.NO_NOISE:
         return _sv_sim(dtype, seed).run(program, param_resolver=param_resolver, repetitions=repetitions)
+    dm = _dm_sim(dtype, seed, noise_model)
     if len(program.all_qubits()) <= DM_MAX_QUBITS:
-        sim = _dm_sim(dtype, seed, noise_model)
-    else:
-        sim = _sv_sim(dtype, seed, noise_model)
-    return sim.run(program, param_resolver=param_resolver, repetitions=repetitions)
+        return dm.run(program, param_resolver=param_resolver, repetitions=repetitions)
+    # too wide for a density matrix: trajectories of the circuit with the
+    # noise placed as the density-matrix simulator places it for run()
+    placed = dm._reference_noisy_circuit(program, "run")
+    return _sv_sim(dtype, seed).run(placed, param_resolver=param_resolver, repetitions=repetitions)
 
 
 def sample_sweep(
@@ -135,18 +138,38 @@ def final_state_vector(
     return result.state_vector()
 
 
-def _dephase(circuit: cirq.AbstractCircuit) -> cirq.Circuit:
-    """Measurements -> phase_damp(1) on each measured qubit; classically
-    controlled operations must have been deferred first."""
+_DEPHASE_SUPEROP = None
 
-    def dephase(op, _):
-        if isinstance(op.gate, cirq.MeasurementGate):
-            return [cirq.phase_damp(1).on(q) for q in op.qubits]
-        if isinstance(op, cirq.ClassicallyControlledOperation):
-            raise ValueError('Use cirq.defer_measurements first to remove classical controls.')
+
+def _is_dephasing_record(op) -> bool:
+    """A keyed one-qubit KrausChannel equal to phase_damp(1): what
+    cirq.dephase_measurements puts in place of a measured qubit."""
+    global _DEPHASE_SUPEROP
+    if not isinstance(op.gate, cirq.KrausChannel) or len(op.qubits) != 1:
+        return False
+    if _DEPHASE_SUPEROP is None:
+        _DEPHASE_SUPEROP = cirq.kraus_to_superoperator(cirq.kraus(cirq.phase_damp(1)))
+    return np.allclose(cirq.kraus_to_superoperator(cirq.kraus(op)), _DEPHASE_SUPEROP, atol=1e-12)
+
+
+def _unkey(circuit: cirq.AbstractCircuit) -> cirq.Circuit:
+    """Drops the measurement key of every dephasing channel that
+    ``cirq.dephase_measurements`` inserted: the key only records the Kraus
+    index, which the final density matrix ignores.  Op for op, so the moment
+    structure stays the reference's."""
+
+    def unkey(op, _):
+        if cirq.is_measurement(op) and _is_dephasing_record(op):
+            return cirq.phase_damp(1).on(*op.qubits)
         return op
 
-    return cirq.map_operations(circuit, dephase, deep=True).unfreeze()
+    return cirq.map_operations(circuit, unkey, deep=True).unfreeze()
+
+
+def _dephase(circuit: cirq.AbstractCircuit) -> cirq.Circuit:
+    """The reference's own ``cirq.dephase_measurements`` (which raises for
+    classical control) with the keys dropped (``_unkey``)."""
+    return _unkey(cirq.dephase_measurements(circuit))
 
 
 def final_density_matrix(
@@ -182,16 +205,22 @@ def final_density_matrix(
 
     has_classical_control = circuit_like != cirq.defer_measurements(circuit_like)
     handling_classical_control = ignore_measurement_results and has_classical_control
+    sim = _dm_sim(dtype, seed, None if handling_classical_control else noise)
     if handling_classical_control:
         noise_applied = circuit_like.with_noise(noise) if noise is not None else circuit_like
-        dephased = _dephase(cirq.defer_measurements(noise_applied))
+        dephased = cirq.dephase_measurements(cirq.defer_measurements(noise_applied))
         prog = dephased
     elif ignore_measurement_results:
-        prog = _dephase(circuit_like)
+        prog = cirq.dephase_measurements(circuit_like)
     else:
         prog = circuit_like
-    result = _dm_sim(dtype, seed, None if handling_classical_control else noise).simulate(
-        prog,
+    if sim.noise is not cirq.NO_NOISE:
+        # noise goes where the reference's simulator puts it, which depends on
+        # the dephasing channels' keys; the keys are dropped afterwards
+        prog = sim._reference_noisy_circuit(prog, "simulate")
+        sim = sim._noiseless()
+    result = sim.simulate(
+        _unkey(prog),
         initial_state=initial_state,
         qubit_order=qubit_order,
         param_resolver=param_resolver,

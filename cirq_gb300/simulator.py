@@ -102,6 +102,7 @@ class _GpuSimulatorBase:
         self._device = device
         self.planner = Planner(tile_bits=tile_bits, kmax=fusion_max_qubits, budget=pass_budget)
         self._cache: collections.OrderedDict = collections.OrderedDict()
+        self._slot_programs: dict = {}  # one-op trajectory programs (trajectories.slot_program)
         self._engine: Engine | None = None
 
     # ---- plumbing --------------------------------------------------------
@@ -123,6 +124,68 @@ class _GpuSimulatorBase:
             )
         moments = self.noise.noisy_moments(program, sorted(qubits))
         return flatten_ops(cirq.Circuit(cirq.flatten_to_ops_or_moments(moments)))
+
+    def _noiseless(self):
+        """This simulator without its noise model (engine, caches and random
+        state shared), for a program whose noise is already inserted."""
+        import copy
+
+        inner = copy.copy(self)
+        inner.noise = cirq.NO_NOISE
+        return inner
+
+    def _reference_noisy_circuit(self, program, mode: str):
+        """`program` with the noise model inserted where the reference's
+        simulators insert it (cirq-core/cirq/sim/simulator_base.py:216-320).
+
+        The density-matrix simulator puts a noise model that touches no
+        measurement key into a prefix: split_into_matching_protocol_then_general
+        (cirq-core/cirq/sim/simulator.py:952-983) splits the program into the
+        ops that qualify for the prefix and the rest, and each part gets the
+        model's noise on its own qubits.  For simulate() (mode "simulate")
+        prefix ops touch no measurement key and have no parameters; for run()
+        (mode "run") they touch no measurement key, and when the rest is
+        measurements only, those are sampled at the end from the state after
+        the rest's noise, skipping noise on a tuple of qubits already measured
+        (the all_measurements_are_terminal rule of _core_iterator,
+        simulator_base.py:196-213).  The state-vector simulator's noise never
+        qualifies (it has no unitary): noise on the circuit's qubits after
+        every moment."""
+        noise = self.noise
+
+        def noisy(c):
+            if not len(c):
+                return cirq.Circuit()
+            return cirq.Circuit(noise.noisy_moments(c, sorted(c.all_qubits())))
+
+        split = cirq.sim.simulator.split_into_matching_protocol_then_general
+        if not self._dm or cirq.measurement_keys_touched(noise):
+            prefix, suffix = cirq.Circuit(), program
+        elif mode == "simulate":
+            prefix, suffix = split(
+                program, lambda op: not cirq.measurement_keys_touched(op) and not cirq.is_parameterized(op)
+            )
+        else:
+            prefix, suffix = split(program, lambda op: not cirq.measurement_keys_touched(op))
+        if mode == "simulate":
+            return noisy(prefix) + noisy(suffix)
+        suffix_ops = list(suffix.all_operations())
+        if not all(isinstance(op.gate, cirq.MeasurementGate) for op in suffix_ops):
+            return noisy(prefix) + noisy(suffix)
+        measured: set = set()
+        kept = []
+        for moment in noisy(suffix):
+            part = []
+            for op in moment.operations:
+                if op.qubits in measured:
+                    continue
+                if isinstance(op.gate, cirq.MeasurementGate):
+                    measured.add(op.qubits)
+                    continue
+                part.append(op)
+            if part:
+                kept.append(cirq.Moment(part))
+        return noisy(prefix) + cirq.Circuit(kept) + cirq.Circuit(suffix_ops)
 
     def _compile(self, body_ops, qubits, resolvers) -> CompiledCircuit:
         key = structure_key(body_ops, qubits, self._dm, self.planner)
@@ -381,6 +444,8 @@ class _GpuSimulatorBase:
     def _run(self, circuit, param_resolver, repetitions) -> dict[str, np.ndarray]:
         param_resolver = param_resolver or cirq.ParamResolver({})
         _check_all_resolved(circuit, param_resolver)
+        if self.noise is not cirq.NO_NOISE:
+            return self._noiseless()._run(self._reference_noisy_circuit(circuit, "run"), param_resolver, repetitions)
         qubits = tuple(sorted(circuit.all_qubits()))
         if self._traj_needed(circuit):
             if not self._dm:
@@ -512,6 +577,11 @@ class Simulator(
         initial_state: Any = None,
     ) -> Iterator[cirq.StateVectorTrialResult]:
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
+        if self.noise is not cirq.NO_NOISE:
+            yield from self._noiseless().simulate_sweep_iter(
+                self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
+            )
+            return
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine
@@ -568,6 +638,12 @@ class Simulator(
                     "Cannot compute expectation value of a non-Hermitian "
                     f"PauliString <{ps}>. Coefficient must be real."
                 )
+        if self.noise is not cirq.NO_NOISE:
+            yield from self._noiseless().simulate_expectation_values_sweep_iter(
+                self._reference_noisy_circuit(program, "simulate"), pslist, params, qubit_order,
+                initial_state, permit_terminal_measurements=True,
+            )
+            return
         if self._traj_needed(program) or program.has_measurements():
             # the reference evaluates the final state of simulate(), which
             # collapses measurements: one trajectory per point
@@ -643,6 +719,11 @@ class DensityMatrixSimulator(
         initial_state: Any = None,
     ) -> Iterator[cirq.DensityMatrixTrialResult]:
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
+        if self.noise is not cirq.NO_NOISE:
+            yield from self._noiseless().simulate_sweep_iter(
+                self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
+            )
+            return
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine
@@ -693,6 +774,12 @@ class DensityMatrixSimulator(
         if not isinstance(observables, list):
             observables = [observables]
         pslist = [cirq.PauliSum.wrap(o) for o in observables]
+        if self.noise is not cirq.NO_NOISE:
+            yield from self._noiseless().simulate_expectation_values_sweep_iter(
+                self._reference_noisy_circuit(program, "simulate"), pslist, params, qubit_order,
+                initial_state, permit_terminal_measurements=True,
+            )
+            return
         if self._traj_needed(program) or program.has_measurements():
             yield from self._traj_expectations(program, pslist, params, qubit_order, initial_state)
             return

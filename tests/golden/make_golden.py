@@ -157,6 +157,28 @@ def main(ref_path: str) -> None:
     out["known_dm_ad"] = np.array([-0.8, 0.0])  # density_matrix_simulator_test.py:899-900
     out["known_dm_dep"] = np.array([0.0, 0.6])  # :904-905
 
+    # 9. module-level helpers (cirq-core/cirq/sim/mux.py) and wide gates
+    cc = _classical_control_circuit(cirq)
+    out["mux_fdm_classical_control"] = cirq.final_density_matrix(cc, dtype=np.complex128)
+    meas = _measured_circuit(cirq)
+    out["mux_fdm_dephased"] = cirq.final_density_matrix(meas, dtype=np.complex128)
+    out["mux_fdm_dephased_noisy"] = cirq.final_density_matrix(
+        meas, noise=cirq.amplitude_damp(0.1), dtype=np.complex128
+    )
+    qm = sorted(meas.all_qubits())
+    out["mux_fsv_ignore_terminal"] = cirq.final_state_vector(
+        meas, ignore_terminal_measurements=True, qubit_order=qm[::-1], dtype=np.complex128
+    )
+    pc, presolver = _noisy_param_circuit(cirq, sympy)
+    out["dm_noisy_param_split"] = (
+        cirq.DensityMatrixSimulator(dtype=np.complex128, noise=cirq.amplitude_damp(0.2))
+        .simulate(pc, presolver)
+        .final_density_matrix
+    )
+    out["wide_controlled_c128"] = (
+        cirq.Simulator(dtype=np.complex128).simulate(_wide_controlled_circuit(cirq)).final_state_vector
+    )
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     with open(os.path.join(HERE, "golden_meta.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py with cirq {cirq.__version__}\n")
@@ -197,6 +219,58 @@ def _gate_zoo(cirq):
         cirq.global_phase_operation(np.exp(0.3j)),
         cirq.I(q[2]),
         cirq.MatrixGate(cirq.testing.random_unitary(8, random_state=4)).on(q[0], q[2], q[4]),
+    )
+
+
+def _classical_control_circuit(cirq):
+    """Mid-circuit measurements feeding classically controlled gates."""
+    q = cirq.LineQubit.range(3)
+    return cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.ry(0.7).on(q[2]),
+        cirq.measure(q[0], key="a"),
+        cirq.X(q[1]).with_classical_controls("a"),
+        cirq.measure(q[2], key="b"),
+        cirq.CZ(q[0], q[1]).with_classical_controls("b"),
+        cirq.H(q[1]),
+    )
+
+
+def _measured_circuit(cirq):
+    """Unitary layers ending in a measurement of two of four qubits."""
+    q = cirq.LineQubit.range(4)
+    return cirq.Circuit(
+        cirq.H(q[0]),
+        cirq.CNOT(q[0], q[1]),
+        cirq.rx(0.4).on(q[2]),
+        cirq.CZ(q[2], q[3]),
+        cirq.ry(1.1).on(q[3]),
+        cirq.measure(q[1], q[3], key="m"),
+    )
+
+
+def _noisy_param_circuit(cirq, sympy):
+    """Moments mixing unparameterized and parameterized ops: the reference's
+    density-matrix simulator noises its prefix and suffix separately."""
+    q = cirq.LineQubit.range(3)
+    t = sympy.Symbol("t")
+    c = cirq.Circuit(
+        cirq.Moment([cirq.H(q[2]), cirq.rx(t).on(q[0])]),
+        cirq.Moment([cirq.CZ(q[0], q[1])]),
+        cirq.Moment([cirq.ry(0.3).on(q[1]), cirq.X(q[2])]),
+    )
+    return c, cirq.ParamResolver({"t": 0.7})
+
+
+def _wide_controlled_circuit(cirq):
+    """Gates on 6 and 7 qubits (more than one fused block holds)."""
+    q = cirq.LineQubit.range(8)
+    return cirq.Circuit(
+        cirq.H.on_each(*q),
+        cirq.X(q[6]).controlled_by(*q[:6]),
+        cirq.rz(0.3).on(q[7]).controlled_by(*q[1:6]),
+        cirq.CZ(q[0], q[7]),
+        cirq.Y(q[2]).controlled_by(q[0], q[1], q[3], q[4], q[5], q[7], control_values=[1, 0, 1, 1, 0, 1]),
     )
 
 

@@ -12,3 +12,18 @@ def gate_zoo():
     import make_golden
 
     return make_golden._gate_zoo(cirq)
+
+
+def fixture_circuit(name: str):
+    """One of the other fixture circuits of make_golden (by builder name)."""
+    import cirq
+    import make_golden
+
+    return getattr(make_golden, name)(cirq)
+
+
+def golden_module():
+    """The fixture generator module itself (its circuit builders)."""
+    import make_golden
+
+    return make_golden

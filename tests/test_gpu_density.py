@@ -98,3 +98,32 @@ def test_bench_size_noisy_density_matrix_properties():
     assert np.real(np.diag(rho)).min() > -1e-6
     rho2 = sim.simulate(c).final_density_matrix
     assert np.array_equal(rho, rho2)
+
+
+def test_noise_placement_matches_the_reference():
+    """Noise model on a parameterized circuit (prefix / suffix noised apart,
+    as the reference's density-matrix simulator does) against the reference's
+    own result, and run() with a terminal two-qubit measurement (noise after
+    the measurement moment acts before sampling) against the exact
+    distribution of the same placement."""
+    import sympy
+    import scipy.stats
+
+    import make_zoo
+
+    pc, r = make_zoo.golden_module()._noisy_param_circuit(cirq, sympy)
+    rho = cirq_gb300.DensityMatrixSimulator(noise=cirq.amplitude_damp(0.2)).simulate(pc, r).final_density_matrix
+    np.testing.assert_allclose(rho, GOLD["dm_noisy_param_split"], atol=TOL)
+
+    q = cirq.LineQubit.range(2)
+    cm = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q), cirq.ry(0.4).on(q[1]), cirq.measure(*q, key="m"))
+    sim = cirq_gb300.DensityMatrixSimulator(noise=cirq.amplitude_damp(0.3), seed=6)
+    placed = sim._reference_noisy_circuit(cm, "run")
+    body = cirq.Circuit(op for op in placed.all_operations() if not cirq.is_measurement(op))
+    from oracle.circuits import simulate_density_matrix as oracle_dm
+
+    p = np.real(np.diag(oracle_dm(body, qubit_order=q)))
+    reps = 20000
+    bits = sim.run(cm, repetitions=reps).measurements["m"]
+    counts = np.bincount(bits[:, 0].astype(int) * 2 + bits[:, 1], minlength=4)
+    assert scipy.stats.chisquare(counts, p / p.sum() * reps).pvalue > 1e-3

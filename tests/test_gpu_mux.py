@@ -93,7 +93,11 @@ def test_sample_distribution(noisy):
     c = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(q[0], q[1]), cirq.ry(1.1).on(q[2]), cirq.measure(*q, key="m"))
     noise = cirq.amplitude_damp(0.2) if noisy else None
     res = cirq_gb300.sample(c, noise=noise, repetitions=4000, seed=11)
-    rho = simulate_density_matrix(c[:-1], noise=noise)
+    # cirq.sample runs the density-matrix simulator: with noise, the noise
+    # after the terminal three-qubit measurement acts before sampling
+    placed = cirq_gb300.DensityMatrixSimulator(noise=noise)._reference_noisy_circuit(c, "run") if noisy else c
+    body = cirq.Circuit(op for op in placed.all_operations() if not cirq.is_measurement(op))
+    rho = simulate_density_matrix(body, qubit_order=q)
     probs = np.clip(np.real(np.diag(rho)), 0, None)
     assert res.measurements["m"].shape == (4000, 3)
     assert _chi2_p(res.measurements["m"], probs / probs.sum()) > 1e-3
@@ -107,3 +111,27 @@ def test_sample_sweep_one_result_per_point():
     assert len(res) == 3
     means = [float(r.measurements["m"].mean()) for r in res]
     assert means[0] == 0.0 and means[2] == 1.0 and 0.35 < means[1] < 0.65
+
+
+GOLD = np.load(__file__.replace("test_gpu_mux.py", "golden/golden.npz"))
+
+
+def test_module_helpers_vs_reference_fixtures():
+    """cirq.final_density_matrix / final_state_vector results computed by the
+    reference itself (tests/golden/make_golden.py)."""
+    import make_zoo
+
+    cc = make_zoo.fixture_circuit("_classical_control_circuit")
+    got = cirq_gb300.final_density_matrix(cc)
+    assert np.max(np.abs(got - GOLD["mux_fdm_classical_control"])) < 2e-6
+    meas = make_zoo.fixture_circuit("_measured_circuit")
+    got = cirq_gb300.final_density_matrix(meas)
+    assert np.max(np.abs(got - GOLD["mux_fdm_dephased"])) < 2e-6
+    got = cirq_gb300.final_density_matrix(meas, noise=cirq.amplitude_damp(0.1))
+    assert np.max(np.abs(got - GOLD["mux_fdm_dephased_noisy"])) < 2e-6
+    q = sorted(meas.all_qubits())
+    got = cirq_gb300.final_state_vector(meas, ignore_terminal_measurements=True, qubit_order=q[::-1])
+    assert np.max(np.abs(got - GOLD["mux_fsv_ignore_terminal"])) < 2e-6
+    wide = make_zoo.fixture_circuit("_wide_controlled_circuit")
+    got = cirq_gb300.Simulator().simulate(wide).final_state_vector
+    assert np.max(np.abs(got - GOLD["wide_controlled_c128"])) < 2e-6

@@ -47,6 +47,8 @@ def test_dephase_matches_the_reference_transformer_channel_by_channel():
     c = cirq.Circuit(cirq.H(q[0]), cirq.measure(q[0], q[2], key="m"), cirq.CNOT(q[0], q[1]))
     ours = mux._dephase(c)
     ref = cirq.dephase_measurements(c)
+    # same moments (a noise model inserts noise per moment)
+    assert [sorted(map(str, m.qubits)) for m in ours] == [sorted(map(str, m.qubits)) for m in ref]
     ours_ops = list(ours.all_operations())
     ref_ops = list(ref.all_operations())
     assert [o.qubits for o in ours_ops] == [o.qubits for o in ref_ops]

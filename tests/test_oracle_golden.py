@@ -89,3 +89,71 @@ def test_renormalization_rule_matches_reference_c64():
     for n, d, s in [(10, 20, 1), (12, 8, 2)]:
         v64 = GOLD[f"layers_n{n}_d{d}_s{s}_c64"]
         np.testing.assert_allclose(np.linalg.norm(renormalize_like_cirq(v64)), 1.0, atol=1e-6)
+
+
+def test_final_density_matrix_fixtures():
+    """cirq.final_density_matrix / final_state_vector fixtures: the oracle's
+    arithmetic on circuits prepared by the package's host-side transforms
+    (dephasing with the reference's transformer, noise placed where the
+    reference's density-matrix simulator places it, keys dropped)."""
+    import make_zoo
+    from cirq_gb300 import DensityMatrixSimulator
+    from cirq_gb300.mux import _dephase, _unkey
+
+    meas = make_zoo.fixture_circuit("_measured_circuit")
+    np.testing.assert_allclose(oc.simulate_density_matrix(_dephase(meas)), GOLD["mux_fdm_dephased"], atol=1e-12)
+    sim = DensityMatrixSimulator(noise=cirq.amplitude_damp(0.1))
+    noisy = sim._reference_noisy_circuit(cirq.dephase_measurements(meas), "simulate")
+    np.testing.assert_allclose(oc.simulate_density_matrix(_unkey(noisy)), GOLD["mux_fdm_dephased_noisy"], atol=1e-12)
+    q = sorted(meas.all_qubits())
+    np.testing.assert_allclose(
+        oc.simulate_state_vector(meas, qubit_order=q[::-1]), GOLD["mux_fsv_ignore_terminal"], atol=1e-12
+    )
+    # classical control: deferred to ancillas, dephased, ancillas traced out
+    cc = make_zoo.fixture_circuit("_classical_control_circuit")
+    deferred = _dephase(cirq.defer_measurements(cc))
+    rho = oc.simulate_density_matrix(deferred)
+    n = len(cc.all_qubits())
+    m = len(deferred.all_qubits())
+    reduced = cirq.partial_trace(rho.reshape((2,) * (2 * m)), list(range(n))).reshape(2**n, 2**n)
+    np.testing.assert_allclose(reduced, GOLD["mux_fdm_classical_control"], atol=1e-12)
+
+
+def test_wide_controlled_gates():
+    import make_zoo
+
+    c = make_zoo.fixture_circuit("_wide_controlled_circuit")
+    np.testing.assert_allclose(oc.simulate_state_vector(c), GOLD["wide_controlled_c128"], atol=1e-12)
+
+
+def test_noise_placement_of_the_density_matrix_simulator():
+    """Noise placed by the package's host-side rule (prefix / suffix split of
+    the reference's density-matrix simulator) + the oracle's arithmetic
+    reproduce the reference: simulate() of a parameterized noisy circuit
+    (golden), and run()'s sample distribution with a terminal two-qubit
+    measurement (the reference's own samples, chi-squared)."""
+    import sympy
+    import scipy.stats
+
+    import make_zoo
+    from cirq_gb300 import DensityMatrixSimulator
+
+    make_golden = make_zoo.golden_module()
+
+    pc, r = make_golden._noisy_param_circuit(cirq, sympy)
+    sim = DensityMatrixSimulator(noise=cirq.amplitude_damp(0.2))
+    got = oc.simulate_density_matrix(sim._reference_noisy_circuit(pc, "simulate"), r)
+    np.testing.assert_allclose(got, GOLD["dm_noisy_param_split"], atol=1e-12)
+
+    q = cirq.LineQubit.range(2)
+    cm = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q), cirq.ry(0.4).on(q[1]), cirq.measure(*q, key="m"))
+    noise = cirq.amplitude_damp(0.3)
+    ours = DensityMatrixSimulator(noise=noise)._reference_noisy_circuit(cm, "run")
+    body = cirq.Circuit(op for op in ours.all_operations() if not cirq.is_measurement(op))
+    p = np.real(np.diag(oc.simulate_density_matrix(body, qubit_order=q)))
+    reps = 40000
+    res = cirq.DensityMatrixSimulator(noise=noise, seed=5).run(cm, repetitions=reps)
+    bits = res.measurements["m"]
+    counts = np.bincount(bits[:, 0] * 2 + bits[:, 1], minlength=4)
+    assert scipy.stats.chisquare(counts, p / p.sum() * reps).pvalue > 1e-3
+

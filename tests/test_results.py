@@ -88,3 +88,51 @@ def test_simulation_state_initial_states_are_unwrapped():
         raise AssertionError("expected ValueError")
     # raw states pass through
     assert sim._unwrap_initial_state(3, "x") == (3, "x")
+
+
+def _noise_ops(c):
+    return [op for op in c.all_operations() if cirq.VirtualTag() in op.tags]
+
+
+def test_noise_placement_follows_the_reference_run_rule():
+    """DensityMatrixSimulator.run: noise on the prefix's qubits after each
+    prefix moment, then the terminal measurements' moment, whose noise is
+    kept unless it acts on a qubit tuple already measured."""
+    import cirq_gb300
+
+    q = cirq.LineQubit.range(2)
+    body = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(q[0], q[1]))
+    sim = cirq_gb300.DensityMatrixSimulator(noise=cirq.depolarize(0.1))
+    # one two-qubit measurement: the noise after it acts on (q0,) and (q1,)
+    c = sim._reference_noisy_circuit(body + cirq.measure(*q, key="m"), "run")
+    assert len(_noise_ops(c)) == 3 * 2
+    assert isinstance(list(c.all_operations())[-1].gate, cirq.MeasurementGate)
+    # one measurement per qubit: the noise after them is skipped
+    c = sim._reference_noisy_circuit(body + cirq.Moment([cirq.measure(q[0]), cirq.measure(q[1])]), "run")
+    assert len(_noise_ops(c)) == 2 * 2
+    # state vector: no prefix; noise after every moment on the circuit's qubits
+    sv = cirq_gb300.Simulator(noise=cirq.depolarize(0.1))
+    c = sv._reference_noisy_circuit(body + cirq.measure(*q, key="m"), "simulate")
+    assert len(_noise_ops(c)) == 3 * 2
+
+
+def test_noise_placement_follows_the_reference_simulate_split():
+    """simulate(): parameterized ops and what follows them on their qubits
+    form the suffix; each part is noised on its own qubits, so a moment
+    split between the parts gets two noise layers."""
+    import sympy
+
+    import cirq_gb300
+
+    q = cirq.LineQubit.range(3)
+    t = sympy.Symbol("t")
+    c = cirq.Circuit(
+        cirq.Moment([cirq.H(q[2]), cirq.rx(t).on(q[0])]),
+        cirq.Moment([cirq.CZ(q[0], q[1])]),
+    )
+    sim = cirq_gb300.DensityMatrixSimulator(noise=cirq.depolarize(0.1))
+    noisy = sim._reference_noisy_circuit(c, "simulate")
+    # prefix [H(q2)] on {q2}: 1 noise op; suffix [rx(q0)], [CZ(q0,q1)] on {q0, q1}: 2 x 2
+    assert len(_noise_ops(noisy)) == 1 + 4
+    on_q2 = [op for op in _noise_ops(noisy) if op.qubits == (q[2],)]
+    assert len(on_q2) == 1
