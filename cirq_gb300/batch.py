@@ -57,8 +57,10 @@ class BatchJob:
         planner = planner or Planner(tile_bits=BATCH_TILE_BITS, kmax=4, budget=40.0)
         if planner.tile_bits != BATCH_TILE_BITS:
             raise ValueError("batched sweeps use 12-bit tiles")
-        self.compiled = CompiledCircuit(body, self.qubits, dm=False, planner=planner,
-                                        resolvers=self.resolvers[:1] or [cirq.ParamResolver({})])
+        # the structure comes from the first point, or from a generic one when
+        # the sweep is empty (every symbol at 0.37, as for adjoint programs)
+        rep = self.resolvers[:1] or [cirq.ParamResolver({s: 0.37 for s in cirq.parameter_symbols(circuit)})]
+        self.compiled = CompiledCircuit(body, self.qubits, dm=False, planner=planner, resolvers=rep)
         # the batch kernel needs at least one full 12-bit tile
         if self.compiled.nbits_dev < BATCH_TILE_BITS:
             self.compiled.nbits_dev = BATCH_TILE_BITS
@@ -163,6 +165,9 @@ def simulate_expectation_values_batch(
     layout = []  # per job: (first point index, npoints, term slices per observable)
     total_points = 0
     for job in jobs:
+        if not job.resolvers:  # an empty sweep: no points, no passes
+            layout.append((total_points, 0, [(0, 0)] * len(job.observables), np.zeros(0, np.complex128)))
+            continue
         plan = job.compiled.plan
         p = plan.passes.copy()
         p["op_begin"] += nop

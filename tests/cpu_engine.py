@@ -86,3 +86,57 @@ class EmuEngine:
 
     def sync(self) -> None:
         pass
+
+    # ---- batched points (cirq_gb300.batch) ----------------------------------
+    def device_info(self):
+        return 152, 8 << 30, 16 << 30
+
+    @staticmethod
+    def _pauli_values(psi, nbits, recs) -> np.ndarray:
+        """<psi| i^ny X^x Z^zy |psi> * coef for each gbq_pauli record."""
+        n = 2**nbits
+        src = psi[:n]
+        j = np.arange(n, dtype=np.int64)
+        out = np.zeros(len(recs), dtype=np.complex128)
+        for t, r in enumerate(recs):
+            x, zy, ny, coef = int(r["x"]), int(r["zy"]), int(r["ny"]), float(r["coef"])
+            sign = 1.0 - 2.0 * (np.bitwise_count((j ^ x) & zy) & 1)
+            out[t] = coef * (1j**ny) * np.vdot(src, sign * src[j ^ x])
+        return out
+
+    def points_set_zero(self, states, nbits, npoints) -> None:
+        arr = np.zeros(npoints << nbits, dtype=np.complex128)
+        arr[:: 1 << nbits] = 1
+        states.arr = arr
+
+    def run_points(self, states, nbits, npoints, plan, pool_dev, pool_stride) -> None:
+        size = 1 << nbits
+        for p in range(npoints):
+            pool = pool_dev.arr[p * pool_stride : (p + 1) * pool_stride]
+            states.arr[p * size : (p + 1) * size] = run_program(
+                states.arr[p * size : (p + 1) * size], nbits, plan.passes, plan.ops, pool
+            )
+        self.launches += plan.npasses
+
+    def points_expect(self, states, nbits, npoints, recs) -> np.ndarray:
+        size = 1 << nbits
+        unit = recs.copy()
+        unit["coef"] = 1.0
+        return np.array([self._pauli_values(states.arr[p * size : (p + 1) * size], nbits, unit)
+                         for p in range(npoints)]).reshape(npoints, len(recs))
+
+    def batch_expect(self, points, passes, ops, pool_dev, terms, max_nbits) -> np.ndarray:
+        """Every point runs its pass range on its own state with the pool at
+        its mat_base, then evaluates its term block (gbq_batch_expect)."""
+        out = np.zeros(max(len(terms), 1), dtype=np.complex128)
+        for pt in points:
+            nbits = int(pt["nbits"])
+            psi = np.zeros(1 << nbits, dtype=np.complex128)
+            psi[0] = 1
+            pb, pc = int(pt["pass_begin"]), int(pt["pass_count"])
+            if pc:
+                psi = run_program(psi, nbits, passes[pb : pb + pc], ops, pool_dev.arr[int(pt["mat_base"]):])
+            tb, tc = int(pt["term_begin"]), int(pt["term_count"])
+            out[tb : tb + tc] = self._pauli_values(psi, nbits, terms[tb : tb + tc])
+        self.launches += 1
+        return out
