@@ -13,11 +13,18 @@ import numpy as np
 from emulator import run_dual_program, run_program
 
 
+def _buf(x):
+    """The emulated buffer behind a buffer or a simulator's non-owning view."""
+    return getattr(x, "_buf", x)
+
+
 class EmuBuffer:
     def __init__(self, nbytes: int, arr=None):
         self.nbytes = int(nbytes)
         self.arr = arr  # complex128 state, float64 partials, or the uploaded array
         self.freed = False
+        self.ptr = id(self)
+        self.engine = None
 
     def free(self) -> None:
         self.freed = True
@@ -32,7 +39,10 @@ class EmuBuffer:
 
 class EmuEngine:
     def __init__(self):
-        self.launches = 0
+        self._launches = 0
+
+    def launches(self) -> int:
+        return self._launches
 
     def alloc(self, nbytes: int) -> EmuBuffer:
         return EmuBuffer(nbytes)
@@ -54,35 +64,35 @@ class EmuEngine:
 
     def run(self, state, nbits, plan, pool_dev=None, sync=True) -> None:
         if plan.npasses:
-            state.arr = run_program(state.arr, nbits, plan.passes, plan.ops, pool_dev.arr)
-            self.launches += plan.npasses
+            _buf(state).arr = run_program(_buf(state).arr, nbits, plan.passes, plan.ops, _buf(pool_dev).arr)
+            self._launches += plan.npasses
 
     def run_dual(self, psi, lam, nbits, plan, pool_dev, partial) -> None:
         if plan.npasses == 0:
             return
-        psi.arr, lam.arr, slots = run_dual_program(psi.arr, lam.arr, nbits, plan.passes, plan.ops, pool_dev.arr)
-        self.launches += plan.npasses
-        partial.arr = slots  # slot -> total (the tiles' sum)
+        _buf(psi).arr, _buf(lam).arr, slots = run_dual_program(_buf(psi).arr, _buf(lam).arr, nbits, plan.passes, plan.ops, _buf(pool_dev).arr)
+        self._launches += plan.npasses
+        _buf(partial).arr = slots  # slot -> total (the tiles' sum)
 
     def reduce_slots(self, partial, nslots, ntiles, out) -> None:
-        out.arr = np.array([partial.arr.get(s, 0.0) for s in range(nslots)], dtype=np.float64)
+        _buf(out).arr = np.array([_buf(partial).arr.get(s, 0.0) for s in range(nslots)], dtype=np.float64)
 
     def apply_paulisum(self, psi, nbits, terms, out) -> None:
         n = 2**nbits
-        src = psi.arr[:n]
+        src = _buf(psi).arr[:n]
         j = np.arange(n, dtype=np.int64)
         acc = np.zeros(n, dtype=np.complex128)
         for x, zy, ny, coef in terms:
             sign = 1.0 - 2.0 * (np.bitwise_count((j ^ x) & zy) & 1)  # Z^zy first, then X^x
             acc += coef * (1j**ny) * sign * src[j ^ x]
-        dst = np.zeros_like(psi.arr) if out.arr is None or len(out.arr) != len(psi.arr) else out.arr
+        dst = np.zeros_like(_buf(psi).arr) if _buf(out).arr is None or len(_buf(out).arr) != len(_buf(psi).arr) else _buf(out).arr
         dst[:] = 0
         dst[:n] = acc
-        out.arr = dst
+        _buf(out).arr = dst
 
     def inner(self, a, b, nbits) -> complex:
         n = 2**nbits
-        return complex(np.vdot(a.arr[:n], b.arr[:n]))
+        return complex(np.vdot(_buf(a).arr[:n], _buf(b).arr[:n]))
 
     def sync(self) -> None:
         pass
@@ -107,22 +117,22 @@ class EmuEngine:
     def points_set_zero(self, states, nbits, npoints) -> None:
         arr = np.zeros(npoints << nbits, dtype=np.complex128)
         arr[:: 1 << nbits] = 1
-        states.arr = arr
+        _buf(states).arr = arr
 
     def run_points(self, states, nbits, npoints, plan, pool_dev, pool_stride) -> None:
         size = 1 << nbits
         for p in range(npoints):
-            pool = pool_dev.arr[p * pool_stride : (p + 1) * pool_stride]
-            states.arr[p * size : (p + 1) * size] = run_program(
-                states.arr[p * size : (p + 1) * size], nbits, plan.passes, plan.ops, pool
+            pool = _buf(pool_dev).arr[p * pool_stride : (p + 1) * pool_stride]
+            _buf(states).arr[p * size : (p + 1) * size] = run_program(
+                _buf(states).arr[p * size : (p + 1) * size], nbits, plan.passes, plan.ops, pool
             )
-        self.launches += plan.npasses
+        self._launches += plan.npasses
 
     def points_expect(self, states, nbits, npoints, recs) -> np.ndarray:
         size = 1 << nbits
         unit = recs.copy()
         unit["coef"] = 1.0
-        return np.array([self._pauli_values(states.arr[p * size : (p + 1) * size], nbits, unit)
+        return np.array([self._pauli_values(_buf(states).arr[p * size : (p + 1) * size], nbits, unit)
                          for p in range(npoints)]).reshape(npoints, len(recs))
 
     def batch_expect(self, points, passes, ops, pool_dev, terms, max_nbits) -> np.ndarray:
@@ -135,8 +145,99 @@ class EmuEngine:
             psi[0] = 1
             pb, pc = int(pt["pass_begin"]), int(pt["pass_count"])
             if pc:
-                psi = run_program(psi, nbits, passes[pb : pb + pc], ops, pool_dev.arr[int(pt["mat_base"]):])
+                psi = run_program(psi, nbits, passes[pb : pb + pc], ops, _buf(pool_dev).arr[int(pt["mat_base"]):])
             tb, tc = int(pt["term_begin"]), int(pt["term_count"])
             out[tb : tb + tc] = self._pauli_values(psi, nbits, terms[tb : tb + tc])
-        self.launches += 1
+        self._launches += 1
+        return out
+
+    # ---- simulators (cirq_gb300.simulator / trajectories / steps) ------------
+    def download_state(self, state, nbits, pinned=True) -> np.ndarray:
+        return np.asarray(_buf(state).arr[: 1 << nbits]).astype(np.complex64)
+
+    def final_renormalize(self, state, nbits) -> bool:
+        """gbq_sv_final_renormalize: the rule of state_vector_simulator.py:131-146
+        at complex64."""
+        v = _buf(state).arr[: 1 << nbits].astype(np.complex64)
+        norm = np.linalg.norm(v)
+        if abs(norm - 1) > np.sqrt(np.finfo(np.float32).eps):
+            return False
+        vn = (v / norm).astype(np.complex64)
+        if abs(np.vdot(vn, vn) - 1) - abs(np.vdot(v, v) - 1) < 0:
+            _buf(state).arr[: 1 << nbits] = vn
+            return True
+        return False
+
+    def norm2(self, state, nbits) -> float:
+        return float(np.sum(np.abs(_buf(state).arr[: 1 << nbits]) ** 2))
+
+    def scale(self, state, nbits, factor) -> None:
+        _buf(state).arr[: 1 << nbits] *= np.float32(factor)
+
+    def project(self, state, nbits, mask, value, scale) -> None:
+        j = np.arange(1 << nbits, dtype=np.int64)
+        keep = (j & int(mask)) == int(value)
+        a = _buf(state).arr[: 1 << nbits]
+        _buf(state).arr[: 1 << nbits] = np.where(keep, a * np.float32(scale), 0)
+
+    def _probs(self, state, nbits, dm) -> np.ndarray:
+        if dm:
+            d = 1 << nbits
+            return np.real(np.diagonal(_buf(state).arr[: d * d].reshape(d, d)))
+        return np.abs(_buf(state).arr[: 1 << nbits]) ** 2
+
+    def probabilities(self, state, nbits, dm=False) -> np.ndarray:
+        return self._probs(state, nbits, dm).astype(np.float32)
+
+    def sample(self, state, nbits, uniforms, dm=False) -> np.ndarray:
+        from oracle.statevector import sample_from_probs
+
+        self._launches += 1
+        return sample_from_probs(self._probs(state, nbits, dm), uniforms).astype(np.uint64)
+
+    def expect_paulis(self, state, nbits, terms, dm=False) -> np.ndarray:
+        if not terms:
+            return np.zeros(0, dtype=np.complex128)
+        coefs = np.array([c for *_, c in terms], dtype=np.complex128)
+        if not dm:
+            recs = np.zeros(len(terms), dtype=[("x", "u8"), ("zy", "u8"), ("ny", "i4"), ("coef", "f8")])
+            for i, (x, zy, ny, _) in enumerate(terms):
+                recs[i] = (x, zy, ny, 1.0)
+            return self._pauli_values(_buf(state).arr, nbits, recs) * coefs
+        d = 1 << nbits
+        rho = _buf(state).arr[: d * d].reshape(d, d)
+        m = np.arange(d, dtype=np.int64)
+        out = np.zeros(len(terms), dtype=np.complex128)
+        for t, (x, zy, ny, _) in enumerate(terms):
+            sign = 1.0 - 2.0 * (np.bitwise_count(m & zy) & 1)
+            out[t] = (1j**ny) * np.sum(sign * rho[m, m ^ x])  # Tr(P rho), P|m> = i^ny (-1)^{m.zy} |m^x>
+        return out * coefs
+
+    def points_sample(self, states, nbits, npoints, uniforms) -> np.ndarray:
+        from oracle.statevector import sample_from_probs
+
+        size = 1 << nbits
+        u = np.asarray(uniforms, dtype=np.float64)
+        return np.array([sample_from_probs(np.abs(_buf(states).arr[p * size : (p + 1) * size]) ** 2, u[p : p + 1])[0]
+                         for p in range(npoints)], dtype=np.uint64)
+
+    def points_rdm(self, states, nbits, npoints, bits) -> np.ndarray:
+        size = 1 << nbits
+        k = len(bits)
+        d = 1 << k
+        j = np.arange(size, dtype=np.int64)
+        sub = np.zeros(size, dtype=np.int64)
+        rest = j.copy()
+        for q, b in enumerate(bits):  # bits[0] is the most significant matrix index bit
+            sub |= ((j >> b) & 1) << (k - 1 - q)
+            rest &= ~(1 << b)
+        out = np.zeros((npoints, d, d), dtype=np.complex128)
+        for p in range(npoints):
+            psi = _buf(states).arr[p * size : (p + 1) * size]
+            for a in range(d):
+                for c in range(d):
+                    ia = np.nonzero(sub == a)[0]
+                    ic = np.nonzero(sub == c)[0]
+                    # pair entries with equal remaining bits
+                    out[p, a, c] = np.sum(psi[ia[np.argsort(rest[ia])]] * np.conj(psi[ic[np.argsort(rest[ic])]]))
         return out

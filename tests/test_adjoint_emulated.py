@@ -26,7 +26,7 @@ def test_hea_vs_reference_gradients():
     E, g = prog.value_and_grad(values)
     assert abs(E - float(GOLD["hea_n5_l2_energy"])) < TOL
     np.testing.assert_allclose(g, GOLD["hea_n5_l2_grad_ps"], atol=1e-5)
-    assert eng.launches > 0
+    assert eng.launches() > 0
 
 
 def _param_circuit(seed, n):
