@@ -1,0 +1,82 @@
+"""Random circuits through the public API on the CPU emulation of the engine,
+compared with the reference simulators themselves (complex128), run here on
+the same inputs: noiseless parameterized state vectors under random qubit
+orders and initial states, and noisy parameterized density matrices with
+explicit channels and noise models (whose placement follows the reference's
+simulators).  CPU only."""
+
+import numpy as np
+import pytest
+import sympy
+
+import cirq
+import cirq_gb300
+from cirq_gb300 import simulator as sim_mod
+from cpu_engine import EmuEngine
+
+SYMS = sympy.symbols("a b")
+
+
+@pytest.fixture
+def emu(monkeypatch):
+    eng = EmuEngine()
+    monkeypatch.setattr(sim_mod, "default_engine", lambda device=None: eng)
+    return eng
+
+
+def _random_circuit(rng, q, channels: bool):
+    n = len(q)
+    moments = []
+    for _ in range(int(rng.integers(3, 9))):
+        ops, used = [], set()
+        for _ in range(int(rng.integers(1, n + 1))):
+            kind = int(rng.integers(0, 9 if channels else 6))
+            k = 2 if kind in (3, 4) else 1
+            free = [x for x in q if x not in used]
+            if len(free) < k:
+                break
+            qs = [free[i] for i in rng.choice(len(free), size=k, replace=False)]
+            used.update(qs)
+            s = SYMS[int(rng.integers(0, 2))] if rng.random() < 0.4 else float(rng.uniform(-1, 1))
+            op = [
+                lambda: cirq.rx(s).on(*qs),
+                lambda: (cirq.Z ** s).on(*qs),
+                lambda: cirq.PhasedXZGate(x_exponent=0.3, z_exponent=-0.2, axis_phase_exponent=0.7).on(*qs),
+                lambda: (cirq.CZ ** s).on(*qs),
+                lambda: cirq.ZZPowGate(exponent=s).on(*qs),
+                lambda: cirq.H(*qs),
+                lambda: cirq.amplitude_damp(0.15).on(*qs),
+                lambda: cirq.depolarize(0.1).on(*qs),
+                lambda: cirq.phase_damp(0.3).on(*qs),
+            ][kind]()
+            ops.append(op)
+        if ops:
+            moments.append(cirq.Moment(ops))
+    return cirq.Circuit(moments)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_state_vectors_match_the_reference(emu, seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 7))
+    q = cirq.LineQubit.range(n)
+    c = _random_circuit(rng, q, channels=False)
+    r = cirq.ParamResolver({s: float(rng.uniform(-2, 2)) for s in SYMS})
+    order = [q[i] for i in rng.permutation(n)]
+    init = int(rng.integers(0, 2**n))
+    want = cirq.Simulator(dtype=np.complex128).simulate(c, r, qubit_order=order, initial_state=init)
+    got = cirq_gb300.Simulator().simulate(c, r, qubit_order=order, initial_state=init)
+    np.testing.assert_allclose(got.final_state_vector, want.final_state_vector, atol=1e-5)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_noisy_density_matrices_match_the_reference(emu, seed):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(2, 5))
+    q = cirq.LineQubit.range(n)
+    c = _random_circuit(rng, q, channels=True)
+    r = cirq.ParamResolver({s: float(rng.uniform(-2, 2)) for s in SYMS})
+    noise = [None, cirq.depolarize(0.05), cirq.amplitude_damp(0.1)][seed % 3]
+    want = cirq.DensityMatrixSimulator(dtype=np.complex128, noise=noise).simulate(c, r).final_density_matrix
+    got = cirq_gb300.DensityMatrixSimulator(noise=noise).simulate(c, r).final_density_matrix
+    np.testing.assert_allclose(got, want, atol=1e-5)
