@@ -80,3 +80,47 @@ def test_noisy_density_matrices_match_the_reference(emu, seed):
     want = cirq.DensityMatrixSimulator(dtype=np.complex128, noise=noise).simulate(c, r).final_density_matrix
     got = cirq_gb300.DensityMatrixSimulator(noise=noise).simulate(c, r).final_density_matrix
     np.testing.assert_allclose(got, want, atol=1e-5)
+
+
+def _two_sample_p(a: np.ndarray, b: np.ndarray) -> float:
+    """Chi-squared homogeneity test of two samples of outcome indices."""
+    import scipy.stats
+
+    keys = np.union1d(a, b)
+    table = np.array([[np.sum(a == k) for k in keys], [np.sum(b == k) for k in keys]])
+    table = table[:, table.sum(axis=0) > 0]
+    if table.shape[1] < 2:
+        return 1.0
+    return scipy.stats.chi2_contingency(table)[1]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_run_distributions_match_the_reference(emu, seed):
+    """run() of random measured circuits (terminal and mid-circuit
+    measurements, noise models on either simulator) sampled by the reference
+    and by the package: the two samples agree (chi-squared homogeneity)."""
+    rng = np.random.default_rng(500 + seed)
+    n = int(rng.integers(2, 4))
+    q = cirq.LineQubit.range(n)
+    body = _random_circuit(rng, q, channels=seed % 2 == 1)
+    r = cirq.ParamResolver({s: float(rng.uniform(-2, 2)) for s in SYMS})
+    mid = seed % 3 == 0
+    c = cirq.Circuit(body[: len(body) // 2])
+    if mid:
+        c.append(cirq.measure(q[0], key="mid"))
+    c += body[len(body) // 2 :]
+    c.append(cirq.measure(*q, key="m"))
+    noise = [None, cirq.depolarize(0.08), cirq.amplitude_damp(0.2)][seed % 3]
+    dm = seed % 4 < 2
+    reps = 1500
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    want = ref_cls(noise=noise, seed=seed).run(c, r, repetitions=reps)
+    got = ours_cls(noise=noise, seed=seed + 1).run(c, r, repetitions=reps)
+    weights = 1 << np.arange(n - 1, -1, -1)
+    a = want.records["m"][:, -1, :].astype(int) @ weights
+    b = got.records["m"][:, -1, :].astype(int) @ weights
+    if mid:
+        a = a * 2 + want.records["mid"][:, 0, 0]
+        b = b * 2 + got.records["mid"][:, 0, 0]
+    assert _two_sample_p(a, b) > 1e-3, (seed, dm, str(noise))
