@@ -124,3 +124,45 @@ def test_run_distributions_match_the_reference(emu, seed):
         a = a * 2 + want.records["mid"][:, 0, 0]
         b = b * 2 + got.records["mid"][:, 0, 0]
     assert _two_sample_p(a, b) > 1e-3, (seed, dm, str(noise))
+
+
+def _random_pauli_sum(rng, q):
+    terms = []
+    for _ in range(int(rng.integers(1, 5))):
+        k = int(rng.integers(1, len(q) + 1))
+        qs = [q[i] for i in rng.choice(len(q), size=k, replace=False)]
+        ps = cirq.PauliString({x: [cirq.X, cirq.Y, cirq.Z][int(rng.integers(0, 3))] for x in qs})
+        terms.append(float(rng.normal()) * ps)
+    return sum(terms[1:], terms[0])
+
+
+@pytest.mark.parametrize("seed", range(30))
+def test_expectations_amplitudes_and_sweeps_match_the_reference(emu, seed):
+    rng = np.random.default_rng(900 + seed)
+    n = int(rng.integers(2, 5))
+    q = cirq.LineQubit.range(n)
+    dm = seed % 2 == 1
+    c = _random_circuit(rng, q, channels=dm)
+    obs = [_random_pauli_sum(rng, q) for _ in range(2)]
+    sweep = cirq.Zip(cirq.Linspace("a", -1.0, 1.0, 3), cirq.Linspace("b", 0.5, 2.0, 3))
+    if dm:
+        noise = [None, cirq.depolarize(0.05)][seed % 4 // 2]
+        ref = cirq.DensityMatrixSimulator(dtype=np.complex128, noise=noise)
+        ours = cirq_gb300.DensityMatrixSimulator(noise=noise)
+    else:
+        ref, ours = cirq.Simulator(dtype=np.complex128), cirq_gb300.Simulator()
+    want = ref.simulate_expectation_values_sweep(c, obs, sweep)
+    got = ours.simulate_expectation_values_sweep(c, obs, sweep)
+    np.testing.assert_allclose(np.array(got), np.array(want), atol=1e-5)
+    wres = ref.simulate_sweep(c, sweep)
+    gres = ours.simulate_sweep(c, sweep)
+    for w, g in zip(wres, gres):
+        if dm:
+            np.testing.assert_allclose(g.final_density_matrix, w.final_density_matrix, atol=1e-5)
+        else:
+            np.testing.assert_allclose(g.final_state_vector, w.final_state_vector, atol=1e-5)
+    if not dm:
+        bits = [int(b) for b in rng.integers(0, 2**n, size=4)]
+        r = cirq.ParamResolver({"a": 0.3, "b": -0.4})
+        np.testing.assert_allclose(ours.compute_amplitudes(c, bits, r), ref.compute_amplitudes(c, bits, r),
+                                   atol=1e-5)
