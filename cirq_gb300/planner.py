@@ -184,6 +184,19 @@ class PassPlan:
     ops: list  # _Dense / _Diag
 
 
+def _snap(m) -> np.ndarray:
+    """Matrix entries as stored in the complex64 pool: real and imaginary
+    parts below 1e-12 become exact zeros, so that a gate at an integer or
+    half-integer exponent (X**1 from its eigen-decomposition, whose phases
+    carry ~1e-16 residues) is the exact permutation / phase matrix the
+    reference's specialised code applies.  complex64 cannot resolve such
+    parts next to O(1) entries in any case."""
+    m = np.asarray(m, dtype=np.complex128)
+    re = np.where(np.abs(m.real) < 1e-12, 0.0, m.real)
+    im = np.where(np.abs(m.imag) < 1e-12, 0.0, m.imag)
+    return re + 1j * im
+
+
 @dataclasses.dataclass
 class Plan:
     """A planned program: passes, ops and the matrix pool (complex64)."""
@@ -224,22 +237,22 @@ class Plan:
                     M = _Replayer.dense_step(M, step, gates)
                 if perm is not None:
                     M = M[:, :, perm[:, None], perm[None, :]]
-                out[:, off : off + ns * d * d] = M.reshape(npoints, -1)
+                out[:, off : off + ns * d * d] = _snap(M.reshape(npoints, -1))
             elif kind in ("probe", "probe_diag"):
                 (b,) = shape
                 G = np.asarray(gates[recipe[0][1]])
                 if kind == "probe_diag":
-                    out[:, off : off + 2**b] = np.diagonal(G, axis1=1, axis2=2)
+                    out[:, off : off + 2**b] = _snap(np.diagonal(G, axis1=1, axis2=2))
                 else:
                     if perm is not None:
                         G = G[:, perm[:, None], perm[None, :]]
-                    out[:, off : off + 4**b] = G.reshape(npoints, -1)
+                    out[:, off : off + 4**b] = _snap(G.reshape(npoints, -1))
             else:
                 (b,) = shape
                 D = np.ones((npoints, 1), dtype=np.complex128)
                 for step in recipe:
                     D = _Replayer.diag_step(D, step, gates)
-                out[:, off : off + 2**b] = D
+                out[:, off : off + 2**b] = _snap(D)
         return out
 
 
@@ -680,7 +693,7 @@ class Planner:
                     data = op.d[0]
                     layout.append(("diag", op.recipe, off, (len(op.bits),), None))
                 r["mat"] = off
-                chunks.append(np.asarray(data).astype(np.complex64))
+                chunks.append(_snap(data).astype(np.complex64))
                 off += len(data)
                 if off & 1:
                     chunks.append(np.zeros(1, np.complex64))

@@ -202,11 +202,18 @@ def split_measurements(circuit):
     ops = flatten_ops(circuit)
     if not any(cirq.is_measurement(op) for op in ops):
         return ops, []
-    if not circuit.are_all_measurements_terminal():
-        raise NotImplementedError(
-            "cirq_gb300 simulates measurements only at the end of the circuit "
-            "(mid-circuit measurement needs per-repetition trajectories)"
-        )
+    # terminal: no operation other than a measurement acts on a measured
+    # qubit afterwards (measurements commute with one another, so repeated or
+    # overlapping final measurements all read one sampled basis state)
+    measured: set = set()
+    for op in ops:
+        if cirq.is_measurement(op):
+            measured.update(op.qubits)
+        elif measured.intersection(op.qubits):
+            raise NotImplementedError(
+                "cirq_gb300 simulates measurements only at the end of the circuit "
+                "(mid-circuit measurement needs per-repetition trajectories)"
+            )
     body = [op for op in ops if not cirq.is_measurement(op)]
     meas = [op for op in ops if cirq.is_measurement(op)]
     for op in meas:

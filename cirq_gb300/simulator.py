@@ -676,9 +676,15 @@ class Simulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
     ) -> Iterator[Sequence[complex]]:
         """Amplitudes of the final state (cirq-core/cirq/sim/state_vector_simulator.py:74-98)."""
+        if isinstance(bitstrings, np.ndarray) and len(bitstrings.shape) > 1:
+            raise ValueError(
+                "The list of bitstrings must be input as a 1-dimensional array of ints. "
+                f"Got an array with shape {bitstrings.shape}."
+            )
+        if isinstance(bitstrings, tuple):
+            bitstrings = list(bitstrings)
         for result in self.simulate_sweep_iter(program, params, qubit_order):
-            vec = result.final_state_vector
-            yield [vec[int(b)] for b in bitstrings]
+            yield result.final_state_vector[bitstrings].tolist()
 
 
 class DensityMatrixSimulator(

@@ -103,7 +103,24 @@ def moment_steps(sim, circuit, param_resolver, qubit_order, initial_state) -> It
     qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(circuit.all_qubits()))
     step_cls = GpuDensityMatrixStep if sim._dm else GpuStateVectorStep
     if not qubits:
-        raise NotImplementedError("simulate_moment_steps needs at least one qubit")
+        # no amplitudes to evolve: the reference's own step results around a
+        # 0-qubit state (the global phase so far), one per moment, or one
+        # for an empty circuit (simulator_base.py:192-194)
+        phase = 1.0 + 0j
+        steps_needed = max(len(resolved), 1)
+        for i in range(steps_needed):
+            if i < len(resolved):
+                for op in resolved[i].operations:
+                    phase *= complex(np.asarray(cirq.unitary(op)).reshape(-1)[0])
+            if sim._dm:
+                st = cirq.DensityMatrixSimulationState(qubits=(), initial_state=np.full((1, 1), abs(phase) ** 2),
+                                                       dtype=np.complex64)
+                yield cirq.DensityMatrixStepResult(sim_state=st, dtype=np.complex64)
+            else:
+                st = cirq.StateVectorSimulationState(qubits=(), initial_state=np.array([phase], dtype=np.complex64),
+                                                     dtype=np.complex64)
+                yield cirq.SparseSimulatorStep(sim_state=st, dtype=np.complex64)
+        return
     moments = list(sim.noise.noisy_moments(resolved, sorted(resolved.all_qubits())))
     initial = 0 if initial_state is None else initial_state
     empty = sim._compile([], qubits, [cirq.ParamResolver({})])

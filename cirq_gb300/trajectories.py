@@ -155,7 +155,12 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
             items.append(Channel(op, nslot))
             nslot += 1
             continue
-        raise UnsupportedOperation(f"operation {op!r} has neither a unitary, a mixture nor Kraus operators")
+        # the reference's error for an operation it cannot act on
+        # (cirq-core/cirq/sim/state_vector_simulation_state.py:395-399)
+        raise TypeError(
+            "Can't simulate operations that don't implement SupportsUnitary, "
+            f"SupportsConsistentApplyUnitary, SupportsMixture or is a measurement: {op!r}"
+        )
     flush()
     return items, nslot
 

@@ -168,3 +168,22 @@ def test_moment_steps(emu):
         np.testing.assert_allclose(st.state_vector(), want, atol=1e-5)
         count += 1
     assert count == len(c)
+
+
+def test_overlapping_final_measurements(emu):
+    """Measurements of the same qubits at the end commute: all read one
+    sampled basis state (the reference's test_overlapping_measurements_at_end)."""
+    a, b = cirq.LineQubit.range(2)
+    c = cirq.Circuit(
+        cirq.H(a),
+        cirq.CNOT(a, b),
+        cirq.measure(a, key="a"),
+        cirq.measure(a, key="not a", invert_mask=(True,)),
+        cirq.measure(b, key="b"),
+        cirq.measure(a, b, key="ab"),
+    )
+    for sim in (cirq_gb300.Simulator(seed=1), cirq_gb300.DensityMatrixSimulator(seed=2)):
+        m = sim.run(c, repetitions=200).measurements
+        np.testing.assert_array_equal(m["a"][:, 0], m["not a"][:, 0] ^ 1)
+        np.testing.assert_array_equal(m["a"][:, 0] * 2 + m["b"][:, 0], m["ab"][:, 0] * 2 + m["ab"][:, 1])
+        assert 20 <= int(m["b"].sum()) <= 180
