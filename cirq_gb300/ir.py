@@ -95,9 +95,34 @@ def flatten_ops(circuit) -> list:
                 ops.extend(
                     cirq.decompose(op, keep=lambda o: len(o.qubits) <= MAX_OP_QUBITS, on_stuck_raise=None)
                 )
+            elif _needs_decomposition(op):
+                # no unitary, mixture or Kraus operators of its own: the
+                # reference acts on its decomposition (act_on's fallback)
+                sub = cirq.decompose_once(op, default=None)
+                if sub is None:
+                    ops.append(op)
+                else:
+                    ops.extend(flatten_ops(cirq.Circuit(sub)))
             else:
                 ops.append(op)
     return ops
+
+
+def _needs_decomposition(op) -> bool:
+    cirq = _cirq()
+    gate = getattr(op, "gate", None)
+    if gate is not None and isinstance(gate, (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate,
+                                               cirq.MeasurementGate, cirq.PhasedXPowGate)):
+        return False  # the common gate families: unitary (or a measurement) by construction
+    if not op.qubits or cirq.is_parameterized(op) or cirq.is_measurement(op):
+        return False
+    if isinstance(op.untagged, cirq.ClassicallyControlledOperation):
+        return False
+    if cirq.has_unitary(op):
+        return False
+    # has_kraus / has_mixture may answer through a decomposition that
+    # cirq.kraus / cirq.mixture do not follow: ask for the operators
+    return cirq.mixture(op, default=None) is None and cirq.kraus(op, default=None) is None
 
 
 def pauli_terms(observable, index: dict, n: int):

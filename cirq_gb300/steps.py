@@ -37,6 +37,9 @@ class _GpuStep(cirq.StepResult):
         self._measurements = measurements
         self._host = None
 
+    def _qid_shape_(self):
+        return (2,) * len(self._qubits)
+
     def sample(self, qubits, repetitions: int = 1, seed: Any = None) -> np.ndarray:
         """Draws from |psi|^2 (or diag rho) on the device; no collapse
         (``cirq-core/cirq/sim/state_vector.py:170-232``)."""
