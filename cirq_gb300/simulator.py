@@ -113,17 +113,12 @@ class _GpuSimulatorBase:
         return self._engine
 
     def _noisy_ops(self, program, qubits):
-        from cirq_gb300.ir import flatten_ops
-
+        """Noise is placed before compiling, by the entry points
+        (_reference_noisy_circuit, then a noise-free clone): a program that
+        reaches the compiler with a noise model still attached is a bug."""
         if self.noise is cirq.NO_NOISE:
             return None
-        if not self._dm:
-            raise NotImplementedError(
-                "cirq_gb300.Simulator has no noisy state-vector trajectories; "
-                "use cirq_gb300.DensityMatrixSimulator for noise"
-            )
-        moments = self.noise.noisy_moments(program, sorted(qubits))
-        return flatten_ops(cirq.Circuit(cirq.flatten_to_ops_or_moments(moments)))
+        raise RuntimeError("internal: a noise model reached the compiler unplaced")
 
     def _noiseless(self):
         """This simulator without its noise model (engine, caches and random

@@ -174,13 +174,12 @@ def records_relevant(ops):
 
 
 def circuit_ops(sim, program, qubits, resolver):
-    """The resolved, noise-inserted operations of a circuit (measurements
-    included: noise after a mid-circuit measurement acts on later ops)."""
-    resolved = cirq.resolve_parameters(program, resolver)
+    """The resolved operations of a circuit whose noise is already placed
+    (measurements included)."""
     if sim.noise is not cirq.NO_NOISE:
-        moments = sim.noise.noisy_moments(resolved, sorted(qubits))
-        resolved = cirq.Circuit(cirq.flatten_to_ops_or_moments(moments))
-    return flatten_ops(resolved)
+        # the entry points place noise first (_reference_noisy_circuit)
+        raise RuntimeError("internal: a noise model reached the trajectory runner unplaced")
+    return flatten_ops(cirq.resolve_parameters(program, resolver))
 
 
 _MAX_SLOT_PROGRAMS = 256  # one-op programs kept per simulator
