@@ -33,7 +33,7 @@ from cirq_gb300._cirq_env import ensure_cirq
 from cirq_gb300.engine import Engine, default_engine
 from cirq_gb300.ir import BitGate, is_diagonal, pauli_terms
 from cirq_gb300.planner import MIN_TILE_BITS, Planner
-from cirq_gb300.program import CompiledCircuit, split_measurements
+from cirq_gb300.program import _expr_values, CompiledCircuit, split_measurements
 
 cirq = ensure_cirq()
 
@@ -125,8 +125,25 @@ class AdjointProgram:
         cache_u: dict = {}
         values: dict = {}  # expression -> value at this point, shared by all gates
         out = {}
+        gens = self.__dict__.setdefault("_generators", {})
         for j, (kind, i, si) in enumerate(self._rev_src):
             src = fwd.sources[i]
+            if kind != "dagger" and src.eigen is not None and src.transform == "u":
+                # U = sum_k exp(i pi t (h_k + s)) P_k with orthogonal projectors, so
+                # dU/dtheta U^dagger = i pi (dt/dtheta) sum_k (h_k + s) P_k: a fixed
+                # generator times the exponent's derivative at this point
+                key = (i, si)
+                g = gens.get(key)
+                if g is None:
+                    import sympy
+
+                    comps, shift, expr = src.eigen
+                    gen = 1j * np.pi * sum((h + shift) * np.asarray(p, dtype=np.complex128) for h, p in comps)
+                    g = gens[key] = (gen, sympy.diff(expr, self.symbols[si]))
+                gen, dexpr = g
+                dt = _expr_values(dexpr, [resolver], values)[0]
+                out[j] = (dt * gen)[None]
+                continue
             if i not in cache_u:
                 cache_u[i] = gates[i][0] if gates is not None else src.matrices([resolver], values)[0]
             u = cache_u[i]

@@ -30,6 +30,7 @@ nested qubit sets; this planner grows genuine k-bit blocks instead.
 from __future__ import annotations
 
 import dataclasses
+import functools
 from typing import Sequence
 
 import numpy as np
@@ -92,25 +93,45 @@ class _Probe:
         return (1 if self.diagonal else 2 ** len(self.bits)) + ovh
 
 
-def _sub_index(size_bits: int, pos: Sequence[int]) -> tuple[np.ndarray, np.ndarray]:
+# The index tables below depend only on a step's static shape; they are
+# cached (read-only arrays) because recipes are replayed for every sweep point.
+
+
+def _frozen(*arrays):
+    for a in arrays:
+        a.flags.writeable = False
+    return arrays if len(arrays) > 1 else arrays[0]
+
+
+@functools.lru_cache(maxsize=8192)
+def _sub_index_cached(size_bits: int, pos: tuple) -> tuple[np.ndarray, np.ndarray]:
     idx = np.arange(2**size_bits)
     sub = np.zeros_like(idx)
     mask = 0
     for i, p in enumerate(pos):
         sub |= ((idx >> p) & 1) << i
         mask |= 1 << p
-    return sub, idx & ~mask
+    return _frozen(sub, idx & ~mask)
+
+
+def _sub_index(size_bits: int, pos: Sequence[int]) -> tuple[np.ndarray, np.ndarray]:
+    return _sub_index_cached(int(size_bits), tuple(int(p) for p in pos))
+
+
+@functools.lru_cache(maxsize=8192)
+def _expand_index(k: int, pos: tuple):
+    sub, rest = _sub_index_cached(k, pos)
+    return _frozen(sub[:, None].copy(), sub[None, :].copy(), rest[:, None] == rest[None, :])
 
 
 def _expand(G: np.ndarray, pos: Sequence[int], k: int) -> np.ndarray:
     """(P, 2^kg, 2^kg) gate on target positions `pos` -> (P, 2^k, 2^k)."""
-    sub, rest = _sub_index(k, pos)
-    same = rest[:, None] == rest[None, :]
-    return G[:, sub[:, None], sub[None, :]] * same
+    rows, cols, same = _expand_index(int(k), tuple(int(p) for p in pos))
+    return G[:, rows, cols] * same
 
 
-def _diag_index(nsel: int, k: int, tpos, spos) -> np.ndarray:
-    """Gate sub-index for every (selector value, target index): shape (2^nsel, 2^k)."""
+@functools.lru_cache(maxsize=8192)
+def _diag_index_cached(nsel: int, k: int, tpos: tuple, spos: tuple) -> np.ndarray:
     s = np.arange(2**nsel)[:, None]
     t = np.arange(2**k)[None, :]
     sub = np.zeros((2**nsel, 2**k), dtype=np.int64)
@@ -119,7 +140,22 @@ def _diag_index(nsel: int, k: int, tpos, spos) -> np.ndarray:
             sub = sub | (((t >> tp) & 1) << j)
         else:
             sub = sub | (((s >> sp) & 1) << j)
-    return sub
+    return _frozen(sub)
+
+
+def _diag_index(nsel: int, k: int, tpos, spos) -> np.ndarray:
+    """Gate sub-index for every (selector value, target index): shape (2^nsel, 2^k)."""
+    norm = lambda xs: tuple(None if x is None else int(x) for x in xs)  # noqa: E731
+    return _diag_index_cached(int(nsel), int(k), norm(tpos), norm(spos))
+
+
+@functools.lru_cache(maxsize=4096)
+def _s2t_index(ns: int, i: int) -> tuple[np.ndarray, np.ndarray]:
+    sidx = np.arange(ns)
+    keep = sidx[((sidx >> i) & 1) == 0]
+    lo = ((keep & ((1 << i) - 1)) | ((keep >> (i + 1)) << i))
+    keep = keep[np.argsort(lo)]
+    return _frozen(keep, keep | (1 << i))
 
 
 class _Replayer:
@@ -137,15 +173,10 @@ class _Replayer:
             n = step[1]
             return np.concatenate([M] * (2**n), axis=1)
         if kind == "s2t":  # selector i becomes the new highest target bit
-            i = step[1]
-            sidx = np.arange(ns)
-            keep = sidx[((sidx >> i) & 1) == 0]
-            lo = ((keep & ((1 << i) - 1)) | ((keep >> (i + 1)) << i))
-            order = np.argsort(lo)
-            keep = keep[order]
+            keep, keep_hi = _s2t_index(ns, int(step[1]))
             out = np.zeros((P, ns // 2, 2 * d, 2 * d), dtype=M.dtype)
             out[:, :, :d, :d] = M[:, keep]
-            out[:, :, d:, d:] = M[:, keep | (1 << i)]
+            out[:, :, d:, d:] = M[:, keep_hi]
             return out
         if kind == "mul":  # left-multiply a non-diagonal gate on target positions
             _, gi, pos = step
@@ -184,17 +215,16 @@ class PassPlan:
     ops: list  # _Dense / _Diag
 
 
-def _snap(m) -> np.ndarray:
-    """Matrix entries as stored in the complex64 pool: real and imaginary
-    parts below 1e-12 become exact zeros, so that a gate at an integer or
-    half-integer exponent (X**1 from its eigen-decomposition, whose phases
-    carry ~1e-16 residues) is the exact permutation / phase matrix the
+def _snap(pool: np.ndarray) -> np.ndarray:
+    """Matrix entries as stored in the complex64 pool, in place: real and
+    imaginary parts below 1e-12 become exact zeros, so that a gate at an
+    integer or half-integer exponent (X**1 from its eigen-decomposition, whose
+    phases carry ~1e-16 residues) is the exact permutation / phase matrix the
     reference's specialised code applies.  complex64 cannot resolve such
     parts next to O(1) entries in any case."""
-    m = np.asarray(m, dtype=np.complex128)
-    re = np.where(np.abs(m.real) < 1e-12, 0.0, m.real)
-    im = np.where(np.abs(m.imag) < 1e-12, 0.0, m.imag)
-    return re + 1j * im
+    for part in (pool.real, pool.imag):
+        part[np.abs(part) < 1e-12] = 0
+    return pool
 
 
 @dataclasses.dataclass
@@ -237,23 +267,23 @@ class Plan:
                     M = _Replayer.dense_step(M, step, gates)
                 if perm is not None:
                     M = M[:, :, perm[:, None], perm[None, :]]
-                out[:, off : off + ns * d * d] = _snap(M.reshape(npoints, -1))
+                out[:, off : off + ns * d * d] = M.reshape(npoints, -1)
             elif kind in ("probe", "probe_diag"):
                 (b,) = shape
                 G = np.asarray(gates[recipe[0][1]])
                 if kind == "probe_diag":
-                    out[:, off : off + 2**b] = _snap(np.diagonal(G, axis1=1, axis2=2))
+                    out[:, off : off + 2**b] = np.diagonal(G, axis1=1, axis2=2)
                 else:
                     if perm is not None:
                         G = G[:, perm[:, None], perm[None, :]]
-                    out[:, off : off + 4**b] = _snap(G.reshape(npoints, -1))
+                    out[:, off : off + 4**b] = G.reshape(npoints, -1)
             else:
                 (b,) = shape
                 D = np.ones((npoints, 1), dtype=np.complex128)
                 for step in recipe:
                     D = _Replayer.diag_step(D, step, gates)
-                out[:, off : off + 2**b] = _snap(D)
-        return out
+                out[:, off : off + 2**b] = D
+        return _snap(out)
 
 
 class Planner:
@@ -693,12 +723,12 @@ class Planner:
                     data = op.d[0]
                     layout.append(("diag", op.recipe, off, (len(op.bits),), None))
                 r["mat"] = off
-                chunks.append(_snap(data).astype(np.complex64))
+                chunks.append(np.asarray(data).astype(np.complex64))
                 off += len(data)
                 if off & 1:
                     chunks.append(np.zeros(1, np.complex64))
                     off += 1
-        pool = np.concatenate(chunks) if chunks else np.zeros(2, np.complex64)
+        pool = _snap(np.concatenate(chunks)) if chunks else np.zeros(2, np.complex64)
         return Plan(
             nbits=nbits,
             passes=passes,

@@ -69,6 +69,62 @@ def _generic_unitary(d: int) -> np.ndarray:
     return q
 
 
+_EXPR_FORMS: dict = {}  # sympy expression -> how to evaluate it (see _expr_form)
+
+
+def _expr_form(expr):
+    """("sym", s) | ("lin", c, s) for c * s | ("const", v) | ("fn", f, symbols)
+    with f a ``sympy.lambdify`` function, cached per expression."""
+    form = _EXPR_FORMS.get(expr)
+    if form is not None:
+        return form
+    import sympy
+
+    if isinstance(expr, sympy.Symbol):
+        form = ("sym", expr)
+    elif not getattr(expr, "free_symbols", None):
+        form = ("const", float(expr))
+    else:
+        coeff, rest = expr.as_coeff_Mul()
+        if isinstance(rest, sympy.Symbol) and coeff.is_number:
+            form = ("lin", float(coeff), rest)
+        else:
+            syms = tuple(sorted(expr.free_symbols, key=str))
+            form = ("fn", sympy.lambdify(syms, expr, "numpy"), syms)
+    if len(_EXPR_FORMS) > 4096:
+        _EXPR_FORMS.clear()
+    _EXPR_FORMS[expr] = form
+    return form
+
+
+def _expr_values(expr, resolvers, values: dict | None) -> np.ndarray:
+    """Per-resolver float values of an exponent expression.
+
+    Free symbols are resolved by each resolver (value_of, so symbol-to-symbol
+    mappings resolve as in the reference) once per batch; the expression is
+    then evaluated from those values (a constant times a symbol directly,
+    anything else by a cached ``sympy.lambdify`` function) rather than by
+    sympy substitution per resolver.  `values` caches results across the
+    sources of one batch."""
+    if values is not None:
+        v = values.get(expr)
+        if v is not None:
+            return v
+    form = _expr_form(expr)
+    if form[0] == "sym":
+        v = np.array([float(r.value_of(expr)) for r in resolvers])
+    elif form[0] == "const":
+        v = np.full(len(resolvers), form[1])
+    elif form[0] == "lin":
+        v = form[1] * _expr_values(form[2], resolvers, values)
+    else:
+        args = [_expr_values(x, resolvers, values) for x in form[2]]
+        v = np.broadcast_to(np.asarray(form[1](*args), dtype=np.float64), (len(resolvers),)).copy()
+    if values is not None:
+        values[expr] = v
+    return v
+
+
 @dataclasses.dataclass
 class OpSource:
     """How to produce one BitGate's matrix for a batch of resolvers."""
@@ -84,7 +140,7 @@ class OpSource:
         values across the sources of one batch (gates sharing a symbol)."""
         P = len(resolvers)
         if self.const is not None:
-            return np.broadcast_to(self.const, (P,) + self.const.shape)
+            return self.const[None] if P == 1 else np.broadcast_to(self.const, (P,) + self.const.shape)
         if self.slot is not None:
             d = 2 ** len(self.op.qubits)
             mats = []
@@ -96,11 +152,7 @@ class OpSource:
         resolvers = [getattr(r, "base", r) for r in resolvers]
         if self.eigen is not None:
             comps, shift, expr = self.eigen
-            t = None if values is None else values.get(expr)
-            if t is None:
-                t = np.array([float(r.value_of(expr)) for r in resolvers])
-                if values is not None:
-                    values[expr] = t
+            t = _expr_values(expr, resolvers, values)
             out = 0
             for h, proj in comps:
                 out = out + np.exp(1j * np.pi * t * (h + shift))[:, None, None] * proj[None]
@@ -139,16 +191,8 @@ class OpSource:
             if dexpr == 0:
                 return None
 
-            def evaluate(e):
-                v = None if values is None else values.get(e)
-                if v is None:
-                    v = np.array([float(r.value_of(e)) for r in resolvers])
-                    if values is not None:
-                        values[e] = v
-                return v
-
-            t = evaluate(expr)
-            dt = evaluate(dexpr)
+            t = _expr_values(expr, [getattr(r, "base", r) for r in resolvers], values)
+            dt = _expr_values(dexpr, [getattr(r, "base", r) for r in resolvers], values)
             out = 0
             for h, proj in comps:
                 f = 1j * np.pi * (h + shift) * np.exp(1j * np.pi * t * (h + shift)) * dt
@@ -319,9 +363,52 @@ class CompiledCircuit:
         self.sources.append(src)
         self.gates.append(BitGate(bits=bits, matrix=None, diagonal=False, tag=len(self.sources) - 1))
 
+    def _eigen_groups(self) -> list:
+        """Parameterised EigenGate sources grouped by (matrix size, number of
+        eigencomponents): (source indices, exponent expressions, (S, K)
+        half-turns h + shift, (S, K, d, d) projectors, (S,) conjugate flags)."""
+        groups = self.__dict__.get("_eigen_group_cache")
+        if groups is None:
+            by_key: dict = {}
+            for i, src in enumerate(self.sources):
+                if src.const is not None or src.slot is not None or src.eigen is None:
+                    continue
+                if src.transform not in ("u", "conj"):
+                    continue
+                comps, shift, expr = src.eigen
+                d = comps[0][1].shape[0]
+                by_key.setdefault((d, len(comps)), []).append((i, src, comps, shift, expr))
+            groups = []
+            for items in by_key.values():
+                idx = [it[0] for it in items]
+                exprs = [it[4] for it in items]
+                H = np.array([[h + it[3] for h, _ in it[2]] for it in items], dtype=np.float64)
+                Pm = np.array([[np.asarray(p, dtype=np.complex128) for _, p in it[2]] for it in items])
+                conj = np.array([it[1].transform == "conj" for it in items])
+                groups.append((idx, exprs, H, Pm, conj))
+            self.__dict__["_eigen_group_cache"] = groups
+        return groups
+
     def gate_batch(self, resolvers) -> dict:
+        """Every source's (P, d, d) matrices for the resolvers.  Parameterised
+        EigenGates are evaluated together per group (one einsum of the
+        phases exp(i pi t (h + shift)) with the projectors), the rest one by
+        one (OpSource.matrices)."""
         values: dict = {}
-        return {i: s.matrices(resolvers, values) for i, s in enumerate(self.sources)}
+        out: dict = {}
+        plain = [r.base if hasattr(r, "base") else r for r in resolvers]
+        for idx, exprs, H, Pm, conj in self._eigen_groups():
+            T = np.stack([_expr_values(e, plain, values) for e in exprs])  # (S, P)
+            phase = np.exp(1j * np.pi * T[:, :, None] * H[:, None, :])  # (S, P, K)
+            M = np.einsum("spk,skij->spij", phase, Pm)
+            if conj.any():
+                M[conj] = np.conjugate(M[conj])
+            for j, i in enumerate(idx):
+                out[i] = M[j]
+        for i, s in enumerate(self.sources):
+            if i not in out:
+                out[i] = s.matrices(resolvers, values)
+        return out
 
     def _plan_resolvers(self, resolvers):
         batch = self.gate_batch(resolvers)
