@@ -182,7 +182,7 @@ class _Replayer:
             _, gi, pos = step
             k = int(np.log2(d))
             F = _expand(gates[gi], pos, k)  # (P, d, d)
-            return np.einsum("pij,psjk->psik", F, M)
+            return np.matmul(F[:, None], M)  # batched over points and selector values
         if kind == "dmul":  # row-scale by a diagonal gate over (targets, selectors)
             _, gi, tpos, spos = step
             k = int(np.log2(d))
@@ -215,6 +215,9 @@ class PassPlan:
     ops: list  # _Dense / _Diag
 
 
+_F32_1E12 = int(np.array(1e-12, dtype=np.float32).view(np.int32))
+
+
 def _snap(pool: np.ndarray) -> np.ndarray:
     """Matrix entries as stored in the complex64 pool, in place: real and
     imaginary parts below 1e-12 become exact zeros, so that a gate at an
@@ -222,6 +225,12 @@ def _snap(pool: np.ndarray) -> np.ndarray:
     phases carry ~1e-16 residues) is the exact permutation / phase matrix the
     reference's specialised code applies.  complex64 cannot resolve such
     parts next to O(1) entries in any case."""
+    if pool.dtype == np.complex64:
+        # |x| < 1e-12 on the float32 bit pattern (sign bit cleared), without
+        # the temporaries of abs()
+        bits = pool.view(np.int32)
+        np.copyto(bits, 0, where=(bits & 0x7FFFFFFF) < _F32_1E12)
+        return pool
     for part in (pool.real, pool.imag):
         part[np.abs(part) < 1e-12] = 0
     return pool
