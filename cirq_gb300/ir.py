@@ -108,6 +108,19 @@ def flatten_ops(circuit) -> list:
     return ops
 
 
+def is_measurement_op(op) -> bool:
+    """cirq.is_measurement, answered without the protocol for the common
+    gate families (unitary by construction) and for measurement gates."""
+    cirq = _cirq()
+    gate = getattr(op, "gate", None)
+    if gate is not None:
+        if isinstance(gate, cirq.MeasurementGate):
+            return True
+        if isinstance(gate, (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)):
+            return False
+    return cirq.is_measurement(op)
+
+
 def _needs_decomposition(op) -> bool:
     cirq = _cirq()
     gate = getattr(op, "gate", None)

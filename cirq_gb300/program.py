@@ -243,23 +243,26 @@ def split_measurements(circuit):
     cirq = _cirq()
     from cirq_gb300.ir import flatten_ops
 
+    from cirq_gb300.ir import is_measurement_op
+
     ops = flatten_ops(circuit)
-    if not any(cirq.is_measurement(op) for op in ops):
+    flags = [is_measurement_op(op) for op in ops]
+    if not any(flags):
         return ops, []
     # terminal: no operation other than a measurement acts on a measured
     # qubit afterwards (measurements commute with one another, so repeated or
     # overlapping final measurements all read one sampled basis state)
     measured: set = set()
-    for op in ops:
-        if cirq.is_measurement(op):
+    for op, is_meas in zip(ops, flags):
+        if is_meas:
             measured.update(op.qubits)
         elif measured.intersection(op.qubits):
             raise NotImplementedError(
                 "cirq_gb300 simulates measurements only at the end of the circuit "
                 "(mid-circuit measurement needs per-repetition trajectories)"
             )
-    body = [op for op in ops if not cirq.is_measurement(op)]
-    meas = [op for op in ops if cirq.is_measurement(op)]
+    body = [op for op, m in zip(ops, flags) if not m]
+    meas = [op for op, m in zip(ops, flags) if m]
     for op in meas:
         if not isinstance(op.gate, cirq.MeasurementGate):
             raise NotImplementedError(f"unsupported measurement {op!r}")

@@ -213,9 +213,7 @@ class _GpuSimulatorBase:
         for r in resolvers or [cirq.ParamResolver({})]:
             _check_all_resolved(program, r)
         body, meas = split_measurements(program)
-        noisy = self._noisy_ops(cirq.Circuit(body), qubits) if body else None
-        if noisy is not None:
-            body = noisy
+        self._noisy_ops(None, qubits)  # noise is placed by the entry points
         compiled = self._compile(body, qubits, resolvers or [cirq.ParamResolver({})])
         return qubits, resolvers, compiled, meas
 

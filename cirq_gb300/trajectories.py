@@ -97,15 +97,20 @@ def conditions_hold(op, records: dict, measured: dict) -> bool:
 
 def needs_trajectories(ops, dm: bool) -> bool:
     """True when a flattened op list cannot be simulated once and sampled."""
+    from cirq_gb300.ir import is_measurement_op
+
+    unitary_families = (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)
     seen_measure = False
     for op in ops:
         if is_classically_controlled(op):
             return True
-        if cirq.is_measurement(op):
+        if is_measurement_op(op):
             seen_measure = True
             continue
         if seen_measure and op.qubits:
             return True  # an operation after a measurement
+        if isinstance(getattr(op, "gate", None), unitary_families):
+            continue
         if not dm and not cirq.is_parameterized(op) and not cirq.has_unitary(op):
             return True
     return False
