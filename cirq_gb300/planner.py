@@ -217,23 +217,30 @@ class PassPlan:
 
 _F32_1E12 = int(np.array(1e-12, dtype=np.float32).view(np.int32))
 
+# recipe step kinds that read a gate matrix (gate index at step[1]) and the
+# kinds that only reshape; anything else disables point grouping for an op
+_GATE_STEPS = ("mul", "dmul", "dd", "init_diag", "init_dense", "probe")
+_GATE_FREE_STEPS = ("tx", "sx", "s2t", "dx")
+
 
 def _snap(pool: np.ndarray) -> np.ndarray:
-    """Matrix entries as stored in the complex64 pool, in place: real and
+    """Matrix entries as stored in the complex64 pool: real and
     imaginary parts below 1e-12 become exact zeros, so that a gate at an
     integer or half-integer exponent (X**1 from its eigen-decomposition, whose
     phases carry ~1e-16 residues) is the exact permutation / phase matrix the
     reference's specialised code applies.  complex64 cannot resolve such
     parts next to O(1) entries in any case."""
     if pool.dtype == np.complex64:
-        # |x| < 1e-12 on the float32 bit pattern (sign bit cleared), without
-        # the temporaries of abs()
+        # in place: |x| < 1e-12 on the float32 bit pattern (sign bit cleared),
+        # without the temporaries of abs()
         bits = pool.view(np.int32)
         np.copyto(bits, 0, where=(bits & 0x7FFFFFFF) < _F32_1E12)
         return pool
-    for part in (pool.real, pool.imag):
-        part[np.abs(part) < 1e-12] = 0
-    return pool
+    # a (P, entries) block of one op, possibly a view of the caller's gates:
+    # a new array
+    re = np.where(np.abs(pool.real) < 1e-12, 0.0, pool.real)
+    im = np.where(np.abs(pool.imag) < 1e-12, 0.0, pool.imag)
+    return re + 1j * im
 
 
 @dataclasses.dataclass
@@ -262,11 +269,95 @@ class Plan:
                 tot += op.cost(0.0)
         return tot
 
-    def pool_for(self, gates: dict, npoints: int) -> np.ndarray:
+    def pool_for(self, gates: dict, npoints: int, codes: dict | None = None) -> np.ndarray:
         """Recomputes the matrix pool for a batch: gates[gi] is (P, d, d).
+
+        `codes` (optional) gives, for some gates, a (P,) integer array that
+        is equal for points whose matrices are equal (trajectories: the index
+        of the drawn unitary); gates broadcast over the points (zero stride)
+        count as equal everywhere.  Each op is then built once per distinct
+        combination of its gates and gathered to the points.
 
         Returns complex64 (P, pool_len).
         """
+        out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
+        dedupe = npoints > 1 and (codes is not None or any(
+            np.asarray(g).ndim and np.asarray(g).strides[0] == 0 for g in gates.values()))
+        for li, (kind, recipe, off, shape, perm) in enumerate(self.layout):
+            if dedupe:
+                gis, rep, inverse = self._point_groups(recipe, gates, npoints, codes or {})
+                if rep is not None and gis:
+                    sub = {gi: np.asarray(gates[gi])[rep] for gi in gis}
+                    block = _snap(self._pool_entry(kind, recipe, shape, perm, sub, len(rep)))
+                    out[:, off : off + block.shape[1]] = block[inverse]
+                    continue
+            block = _snap(self._pool_entry(kind, recipe, shape, perm, gates, npoints))
+            out[:, off : off + block.shape[1]] = block
+        return out
+
+    @staticmethod
+    def _recipe_gates(recipe):
+        """Sorted gate indices a recipe reads, or None if it has a step kind
+        this scan does not know (the op is then built point by point)."""
+        out: set = set()
+        for step in recipe:
+            kind = step[0]
+            if kind in _GATE_STEPS:
+                out.add(step[1])
+            elif kind == "diag_as_dense":
+                nested = Plan._recipe_gates(step[1])
+                if nested is None:
+                    return None
+                out.update(nested)
+            elif kind not in _GATE_FREE_STEPS:
+                return None
+        return sorted(out)
+
+    def _point_groups(self, recipe, gates, npoints, codes):
+        """(gate indices, representative points, inverse map) of the distinct
+        gate combinations of one op; rep is None when the points differ."""
+        gis = self._recipe_gates(recipe)
+        if not gis:
+            return gis, None, None
+        cols = []
+        for gi in gis:
+            g = np.asarray(gates[gi])
+            if gi in codes:
+                cols.append(np.asarray(codes[gi]))
+            elif g.strides[0] != 0:
+                return gis, None, None
+        if not cols:
+            return gis, np.zeros(1, dtype=np.int64), np.zeros(npoints, dtype=np.int64)
+        key = np.stack(cols, axis=1)
+        _, rep, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
+        if len(rep) * 2 > npoints:
+            return gis, None, None  # too few repeats to pay for the gather
+        return gis, rep, inverse.reshape(-1)
+
+    def _pool_entry(self, kind, recipe, shape, perm, gates, npoints) -> np.ndarray:
+        """One op's matrices / table for the points: (P, entries)."""
+        if kind == "dense":
+            ns, d = shape
+            M = np.broadcast_to(np.eye(1, dtype=np.complex128), (npoints, 1, 1, 1)).copy()
+            for step in recipe:
+                M = _Replayer.dense_step(M, step, gates)
+            if perm is not None:
+                M = M[:, :, perm[:, None], perm[None, :]]
+            return M.reshape(npoints, -1)
+        if kind in ("probe", "probe_diag"):
+            G = np.asarray(gates[recipe[0][1]])
+            if kind == "probe_diag":
+                return np.diagonal(G, axis1=1, axis2=2)
+            if perm is not None:
+                G = G[:, perm[:, None], perm[None, :]]
+            return G.reshape(npoints, -1)
+        D = np.ones((npoints, 1), dtype=np.complex128)
+        for step in recipe:
+            D = _Replayer.diag_step(D, step, gates)
+        return D
+
+    def _pool_for_reference(self, gates: dict, npoints: int) -> np.ndarray:
+        """pool_for without grouping (kept for tests of the grouping)."""
         out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
         for kind, recipe, off, shape, perm in self.layout:
             if kind == "dense":

@@ -457,12 +457,17 @@ class CompiledCircuit:
             return np.broadcast_to(self.plan.pool, (len(resolvers), len(self.plan.pool)))
         return self.pool_from_batch(self.gate_batch(resolvers), len(resolvers))
 
-    def pool_from_batch(self, batch: dict, npoints: int) -> np.ndarray:
-        """Matrix pools from already evaluated gate matrices (gate_batch)."""
+    def pool_from_batch(self, batch: dict, npoints: int, codes: dict | None = None) -> np.ndarray:
+        """Matrix pools from already evaluated gate matrices (gate_batch).
+        `codes[source index]` (optional): (P,) ints equal where that source's
+        matrices are equal (see Plan.pool_for)."""
         if not self.parameterized:
             return np.broadcast_to(self.plan.pool, (npoints, len(self.plan.pool)))
         sub = {j: np.asarray(batch[i]) for j, i in enumerate(self.kept)}
-        return self.plan.pool_for(sub, npoints)
+        sub_codes = None
+        if codes:
+            sub_codes = {j: codes[i] for j, i in enumerate(self.kept) if i in codes}
+        return self.plan.pool_for(sub, npoints, sub_codes)
 
     def global_phase(self, resolver) -> complex:
         """Product of the global-phase operations (used for 0-qubit circuits)."""

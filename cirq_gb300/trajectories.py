@@ -299,19 +299,34 @@ class TrajectoryRunner:
         return recs, mats
 
     # ---- host-side draws ---------------------------------------------------
-    def _draw_mixtures(self, reps: int) -> list[dict]:
+    def _draw_mixtures(self, reps: int) -> dict:
+        """slot -> (its unitaries (n, d, d), each trajectory's choice (reps,)),
+        drawn with the mixture's probabilities (the reference's mixture
+        sampling, cirq-core/cirq/sim/state_vector_simulation_state.py:183-205)."""
         prng = self.sim._prng
-        picks = [dict() for _ in range(reps)]
+        draws = {}
+        mixtures: dict = {}  # a mixture depends on the gate only, not on its qubits
         for it in self.items:
             if not isinstance(it, Segment):
                 continue
             for sid, op in it.slots:
-                probs, unitaries = zip(*cirq.mixture(op))
-                p = np.asarray(probs, dtype=np.float64)
-                choice = prng.choice(len(unitaries), size=reps, p=p / p.sum())
-                for r in range(reps):
-                    picks[r][sid] = unitaries[choice[r]]
-        return picks
+                key = getattr(op, "gate", None)
+                try:
+                    hash(key)
+                except TypeError:  # an unhashable gate: no caching
+                    key = None
+                if key is None or key not in mixtures:
+                    probs, unitaries = zip(*cirq.mixture(op))
+                    entry = (np.asarray(probs, dtype=np.float64),
+                             np.array([np.asarray(u, dtype=np.complex128) for u in unitaries]))
+                    if key is not None:
+                        mixtures[key] = entry
+                else:
+                    entry = mixtures[key]
+                p, U = entry
+                choice = prng.choice(len(U), size=reps, p=p / p.sum())
+                draws[sid] = (U, choice)
+        return draws
 
     # ---- one trajectory ------------------------------------------------------
     def run(self, initial_state, picks: dict, pools: list, rep: int):
@@ -376,18 +391,37 @@ class TrajectoryRunner:
         eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("kraus", it.slot), pool))
 
     def prepare(self, reps: int):
-        """Draws the mixtures of `reps` trajectories; returns (picks, pools)."""
-        picks = self._draw_mixtures(reps)
+        """Draws the mixtures of `reps` trajectories; returns (picks, pools):
+        per-trajectory dicts for the channel draws made later, and each
+        segment's (reps, pool_len) matrix pools (None without slots)."""
+        draws = self._draw_mixtures(reps)
+        picks = [dict() for _ in range(reps)]
         pools = []
         for j, it in enumerate(self.items):
             c = self.compiled[j]
             if isinstance(it, Segment) and c.plan.npasses and it.slots:
-                pools.append(c.pool([TrajectoryPoint(self.resolver, p) for p in picks]))
-            elif isinstance(it, Segment) and c.plan.npasses:
-                pools.append(None)
+                batch, codes = self._segment_batch(c, draws, reps)
+                pools.append(c.pool_from_batch(batch, reps, codes))
             else:
                 pools.append(None)
         return picks, pools
+
+    def _segment_batch(self, c, draws: dict, reps: int):
+        """A segment's gate matrices for `reps` trajectories: slots from the
+        draws (with their choice indices as codes, so fused ops are built once
+        per distinct combination), everything else once at the base point."""
+        values: dict = {}
+        base = [self.resolver]
+        batch, codes = {}, {}
+        for i, src in enumerate(c.sources):
+            if src.slot is not None:
+                U, choice = draws[src.slot]
+                batch[i] = U[choice]
+                codes[i] = choice
+            else:
+                m = src.matrices(base, values)
+                batch[i] = np.broadcast_to(m[0], (reps,) + m.shape[1:])
+        return batch, codes
 
 
 def pad_records(per_rep: list[dict]) -> dict[str, np.ndarray]:
@@ -472,8 +506,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
 
         def run_slot(compiled, mats, k, start):
             """One-slot program with a per-trajectory matrix (mats: (k, d, d))."""
-            pts = [TrajectoryPoint(resolver, {0: m}) for m in mats]
-            pool = np.ascontiguousarray(compiled.pool(pts), dtype=np.complex64)
+            pool = np.ascontiguousarray(compiled.pool_from_batch({0: np.asarray(mats)}, k), dtype=np.complex64)
             plen = pool.shape[1]
             if plen & 1:
                 pool = np.concatenate([pool, np.zeros((k, 1), np.complex64)], axis=1)

@@ -129,3 +129,35 @@ def test_conditions_resolve_like_the_reference():
         pass
     else:
         raise AssertionError("expected ValueError")
+
+
+def test_grouped_pool_replay_matches_point_by_point():
+    """Trajectory pools built once per distinct combination of drawn
+    unitaries (choice codes, broadcast gates) equal the point-by-point
+    replay."""
+    q = cirq.LineQubit.range(4)
+    ops = flatten_ops(cirq.Circuit(
+        cirq.H.on_each(*q), cirq.depolarize(0.3).on(q[0]), cirq.CNOT(q[0], q[1]),
+        cirq.bit_flip(0.2).on(q[2]), cirq.CZ(q[1], q[2]), cirq.ry(0.4).on(q[3]),
+        cirq.phase_flip(0.25).on(q[3]), cirq.CNOT(q[3], q[0]),
+    ))
+    items, _ = tj.build_items(ops, dm=False)
+    seg = items[0]
+    c = CompiledCircuit(seg.ops, q, dm=False, planner=Planner(tile_bits=10, kmax=3),
+                        resolvers=[cirq.ParamResolver({})])
+    rng = np.random.default_rng(0)
+    reps = 40
+    batch, codes = {}, {}
+    for i, src in enumerate(c.sources):
+        if src.slot is not None:
+            probs, us = zip(*cirq.mixture(src.op.op if hasattr(src.op, "op") else src.op))
+            U = np.array([np.asarray(u, dtype=complex) for u in us])
+            choice = rng.integers(0, len(U), size=reps)
+            batch[i], codes[i] = U[choice], choice
+        else:
+            m = src.matrices([cirq.ParamResolver({})])
+            batch[i] = np.broadcast_to(m[0], (reps,) + m.shape[1:])
+    grouped = c.pool_from_batch(batch, reps, codes)
+    sub = {j: np.ascontiguousarray(batch[i]) for j, i in enumerate(c.kept)}
+    plain = c.plan._pool_for_reference(sub, reps)
+    np.testing.assert_allclose(grouped, plain, atol=1e-6)
