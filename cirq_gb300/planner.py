@@ -283,6 +283,7 @@ class Plan:
         out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
         dedupe = npoints > 1 and (codes is not None or any(
             np.asarray(g).ndim and np.asarray(g).strides[0] == 0 for g in gates.values()))
+        regions = []  # (offset, width) written point by point, snapped in place below
         for li, (kind, recipe, off, shape, perm) in enumerate(self.layout):
             if dedupe:
                 gis, rep, inverse = self._point_groups(recipe, gates, npoints, codes or {})
@@ -291,8 +292,13 @@ class Plan:
                     block = _snap(self._pool_entry(kind, recipe, shape, perm, sub, len(rep)))
                     out[:, off : off + block.shape[1]] = block[inverse]
                     continue
-            block = _snap(self._pool_entry(kind, recipe, shape, perm, gates, npoints))
+            block = self._pool_entry(kind, recipe, shape, perm, gates, npoints)
             out[:, off : off + block.shape[1]] = block
+            regions.append((off, block.shape[1]))
+        if not dedupe:
+            return _snap(out)
+        for off, width in regions:
+            _snap(out[:, off : off + width])
         return out
 
     @staticmethod
