@@ -42,6 +42,8 @@ from cirq_gb300 import trajectories as _traj
 cirq = ensure_cirq()
 
 _MAX_CACHE = 64  # compiled circuits kept per simulator (trajectory segments count too)
+_MAX_STATE_BITS = 34  # widest device state run() simulates in one piece (2^34 amplitudes: 128 GiB)
+_PART = "\x00"  # separator of the internal measurement keys of untangled parts
 
 
 def _check_dtype(dtype):
@@ -434,12 +436,78 @@ class _GpuSimulatorBase:
         return {k: np.array(v).swapaxes(0, 1) for k, v in results.items()}
 
     # ---- SimulatesSamples ---------------------------------------------------
+    def _run_untangled(self, circuit, param_resolver, repetitions):
+        """run() of a circuit whose qubits fall into components that no
+        operation joins, one component at a time.  The components are
+        independent, so the joint distribution of the records is the product
+        of theirs, which is what the reference samples from its product
+        state (cirq-core/cirq/sim/simulation_product_state.py).  A
+        measurement across components is split into one measurement per
+        component (internal keys); its bits are reassembled in the original
+        order, repetition by repetition.  Components without a measurement
+        are not simulated.  Returns None when the circuit does not split
+        (one component, classical control, or a confusion map across
+        components)."""
+        from cirq_gb300.ir import flatten_ops, is_measurement_op
+
+        ops = flatten_ops(circuit)
+        parts = _untangled_parts(ops)
+        if parts is None or len(parts) < 2:
+            return None
+        where = {q: i for i, part in enumerate(parts) for q in part}
+        sub_ops: list = [[] for _ in parts]
+        measured = [False] * len(parts)
+        assembly: dict = {}  # key -> [(pieces [(internal key, bit positions)], width)] per instance
+        for op in ops:
+            if not op.qubits:
+                continue  # a global phase changes no sample
+            gate = getattr(op, "gate", None)
+            if not is_measurement_op(op):
+                sub_ops[where[op.qubits[0]]].append(op)
+                continue
+            if not isinstance(gate, cirq.MeasurementGate):
+                return None
+            key = cirq.measurement_key_name(op)
+            t = len(assembly.setdefault(key, []))
+            inv = gate.full_invert_mask()
+            groups: dict = {}
+            for pos, q in enumerate(op.qubits):
+                groups.setdefault(where[q], []).append(pos)
+            pieces = []
+            for c, positions in groups.items():
+                sub_key = f"{_PART}{key}{_PART}{t}{_PART}{c}"
+                kwargs = {"key": sub_key, "invert_mask": tuple(inv[p] for p in positions)}
+                if gate.confusion_map:  # within one component (checked above)
+                    kwargs["confusion_map"] = gate.confusion_map
+                sub_ops[c].append(cirq.measure(*[op.qubits[p] for p in positions], **kwargs))
+                measured[c] = True
+                pieces.append((sub_key, positions))
+            assembly[key].append((pieces, len(op.qubits)))
+        records: dict = {}
+        for c, ops_c in enumerate(sub_ops):
+            if measured[c]:
+                records.update(self._run(cirq.Circuit(ops_c), param_resolver, repetitions))
+        out = {}
+        for key, instances in assembly.items():
+            width = max(w for _, w in instances)
+            dtype = next(iter(records.values())).dtype if records else np.uint8
+            arr = np.zeros((repetitions, len(instances), width), dtype=dtype)
+            for t, (pieces, _) in enumerate(instances):
+                for sub_key, positions in pieces:
+                    arr[:, t, positions] = records[sub_key][:, 0, :]
+            out[key] = arr
+        return out
+
     def _run(self, circuit, param_resolver, repetitions) -> dict[str, np.ndarray]:
         param_resolver = param_resolver or cirq.ParamResolver({})
         _check_all_resolved(circuit, param_resolver)
         if self.noise is not cirq.NO_NOISE:
             return self._noiseless()._run(self._reference_noisy_circuit(circuit, "run"), param_resolver, repetitions)
         qubits = tuple(sorted(circuit.all_qubits()))
+        if self._split_untangled_states and len(qubits) * (2 if self._dm else 1) > _MAX_STATE_BITS:
+            rec = self._run_untangled(circuit, param_resolver, repetitions)
+            if rec is not None:
+                return rec
         if self._traj_needed(circuit):
             if not self._dm:
                 ops = _traj.circuit_ops(self, circuit, qubits, param_resolver)
@@ -458,6 +526,44 @@ class _GpuSimulatorBase:
         pool = compiled.pool([param_resolver])[0]
         state = self._evolve(compiled, pool, 0)
         return self._sample_records(state, compiled, meas, repetitions)
+
+
+def _untangled_parts(ops) -> list[list] | None:
+    """Qubit components of a flattened op list that no operation joins
+    (union-find over the qubits of multi-qubit non-measurement operations;
+    measurements do not entangle), or None when the split is not valid:
+    classical control, or a confusion map across components."""
+    from cirq_gb300 import trajectories as tj
+    from cirq_gb300.ir import is_measurement_op
+
+    parent: dict = {}
+
+    def find(x):
+        while parent.setdefault(x, x) != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for op in ops:
+        for q in op.qubits:
+            find(q)
+        if tj.is_classically_controlled(op):
+            return None
+        if len(op.qubits) > 1 and not is_measurement_op(op):
+            r = find(op.qubits[0])
+            for q in op.qubits[1:]:
+                parent[find(q)] = r
+    comps: dict = {}
+    for q in sorted(parent):
+        comps.setdefault(find(q), []).append(q)
+    parts = list(comps.values())
+    where = {q: i for i, part in enumerate(parts) for q in part}
+    for op in ops:
+        gate = getattr(op, "gate", None)
+        if isinstance(gate, cirq.MeasurementGate) and gate.confusion_map:
+            if len({where[q] for q in op.qubits}) > 1:
+                return None
+    return parts
 
 
 class _Borrowed:

@@ -187,3 +187,68 @@ def test_overlapping_final_measurements(emu):
         np.testing.assert_array_equal(m["a"][:, 0], m["not a"][:, 0] ^ 1)
         np.testing.assert_array_equal(m["a"][:, 0] * 2 + m["b"][:, 0], m["ab"][:, 0] * 2 + m["ab"][:, 1])
         assert 20 <= int(m["b"].sum()) <= 180
+
+
+def _blocks_circuit(nblocks, seed):
+    """Independent 3-qubit blocks (H, CNOT chain, a rotation): a GHZ-like
+    pair per block and one rotated qubit."""
+    rng = np.random.default_rng(seed)
+    q = cirq.LineQubit.range(3 * nblocks)
+    ops = []
+    thetas = rng.uniform(0.3, 2.5, size=nblocks)
+    for b in range(nblocks):
+        a, c, d = q[3 * b], q[3 * b + 1], q[3 * b + 2]
+        ops += [cirq.H(a), cirq.CNOT(a, c), cirq.ry(float(thetas[b])).on(d), cirq.CZ(c, d)]
+    return q, cirq.Circuit(ops), thetas
+
+
+def test_run_of_untangled_circuits_beyond_the_device_state(emu):
+    """36 qubits in 12 independent blocks (a 2^36 state would not fit):
+    run() simulates the blocks one at a time and reassembles the records."""
+    q, body, thetas = _blocks_circuit(12, seed=3)
+    c = body + cirq.measure(*q, key="all") + cirq.measure(q[0], q[4], key="pair")
+    reps = 400
+    res = cirq_gb300.Simulator(seed=9).run(c, repetitions=reps)
+    ref = cirq.Simulator(seed=9).run(c, repetitions=5)
+    assert res.records["all"].shape == (reps,) + ref.records["all"].shape[1:] == (reps, 1, 36)
+    assert res.records["pair"].shape == (reps, 1, 2)
+    bits = res.records["all"][:, 0, :]
+    # within every block the first two qubits agree (H + CNOT)
+    np.testing.assert_array_equal(bits[:, 0::3], bits[:, 1::3])
+    # the rotated qubit of each block: P(1) = sin^2(theta / 2)
+    for b in range(12):
+        p1 = np.sin(thetas[b] / 2) ** 2
+        n1 = int(bits[:, 3 * b + 2].sum())
+        assert scipy.stats.binomtest(n1, reps, p1).pvalue > 1e-4
+    # the split measurement reads the same sampled state
+    np.testing.assert_array_equal(res.records["pair"][:, 0, 0], bits[:, 0])
+    np.testing.assert_array_equal(res.records["pair"][:, 0, 1], bits[:, 4])
+
+
+def test_unmeasured_components_are_not_simulated(emu):
+    q = cirq.LineQubit.range(40)
+    big = cirq.Circuit(cirq.H(q[0]), *[cirq.CNOT(q[i], q[i + 1]) for i in range(33)])  # 34 entangled qubits
+    small = cirq.Circuit(cirq.X(q[36]), cirq.H(q[38]))
+    c = big + small + cirq.measure(q[36], q[38], key="m")
+    res = cirq_gb300.Simulator(seed=1).run(c, repetitions=200)
+    m = res.records["m"][:, 0, :]
+    assert (m[:, 0] == 1).all() and 0.3 < m[:, 1].mean() < 0.7
+
+
+def test_noisy_density_matrix_run_of_untangled_blocks(emu):
+    """18 qubits on the density-matrix simulator (2n = 36 bits): noise placed
+    on the whole circuit first, then the blocks run one by one."""
+    q, body, thetas = _blocks_circuit(6, seed=4)
+    c = body + cirq.measure(*q, key="m")
+    noise = cirq.amplitude_damp(0.2)
+    dm = cirq_gb300.DensityMatrixSimulator(noise=noise, seed=2)
+    reps = 600
+    bits = dm.run(c, repetitions=reps).records["m"][:, 0, :]
+    placed = dm._reference_noisy_circuit(c, "run")
+    for b in range(6):
+        qs = q[3 * b : 3 * b + 3]
+        block = cirq.Circuit(op for op in placed.all_operations()
+                             if set(op.qubits) <= set(qs) and not cirq.is_measurement(op))
+        p = np.real(np.diag(simulate_density_matrix(block, qubit_order=qs)))
+        idx = bits[:, 3 * b : 3 * b + 3].astype(int) @ np.array([4, 2, 1])
+        assert _chi2_p(np.bincount(idx, minlength=8), p) > 1e-4
