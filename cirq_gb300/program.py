@@ -269,6 +269,9 @@ def split_measurements(circuit):
     return body, meas
 
 
+MAX_STATE_BITS = 40  # widest state the engine's ABI accepts (gbq_run and friends)
+
+
 class CompiledCircuit:
     """Structure + plan of a circuit over a fixed qubit order (see module doc)."""
 
@@ -286,6 +289,12 @@ class CompiledCircuit:
         self.n = len(qubits)
         self.dm = dm
         self.nbits = 2 * self.n if dm else self.n
+        if self.nbits > MAX_STATE_BITS:
+            # the reference's numpy allocation fails the same way
+            raise MemoryError(
+                f"Unable to allocate a state of {self.nbits} bits (2^{self.nbits} complex64 amplitudes): "
+                f"at most {MAX_STATE_BITS} bits fit a device state"
+            )
         # device width: narrow registers run padded with |0> high bits
         self.nbits_dev = max(self.nbits, MIN_TILE_BITS)
         index = {q: i for i, q in enumerate(self.qubits)}

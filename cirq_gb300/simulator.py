@@ -436,31 +436,33 @@ class _GpuSimulatorBase:
         return {k: np.array(v).swapaxes(0, 1) for k, v in results.items()}
 
     # ---- SimulatesSamples ---------------------------------------------------
-    def _run_untangled(self, circuit, param_resolver, repetitions):
-        """run() of a circuit whose qubits fall into components that no
-        operation joins, one component at a time.  The components are
-        independent, so the joint distribution of the records is the product
-        of theirs, which is what the reference samples from its product
-        state (cirq-core/cirq/sim/simulation_product_state.py).  A
-        measurement across components is split into one measurement per
-        component (internal keys); its bits are reassembled in the original
-        order, repetition by repetition.  Components without a measurement
-        are not simulated.  Returns None when the circuit does not split
-        (one component, classical control, or a confusion map across
-        components)."""
-        from cirq_gb300.ir import flatten_ops, is_measurement_op
+    @staticmethod
+    def _split_untangled(ops, extra_qubits=()):
+        """(parts, per-part op lists, measured flags, assembly, phase ops) of
+        a flattened op list whose qubits fall into components no operation
+        joins, or None (see _untangled_parts).  A measurement across
+        components becomes one measurement per component under internal
+        keys; assembly[key] lists, per instance, the (internal key, bit
+        positions) pieces and the width.  `extra_qubits` (idle qubits of a
+        qubit order) become components of their own."""
+        from cirq_gb300.ir import is_measurement_op
 
-        ops = flatten_ops(circuit)
         parts = _untangled_parts(ops)
-        if parts is None or len(parts) < 2:
+        if parts is None:
+            return None
+        seen = {q for part in parts for q in part}
+        parts = parts + [[q] for q in extra_qubits if q not in seen]
+        if len(parts) < 2:
             return None
         where = {q: i for i, part in enumerate(parts) for q in part}
         sub_ops: list = [[] for _ in parts]
         measured = [False] * len(parts)
-        assembly: dict = {}  # key -> [(pieces [(internal key, bit positions)], width)] per instance
+        assembly: dict = {}
+        phases = []
         for op in ops:
             if not op.qubits:
-                continue  # a global phase changes no sample
+                phases.append(op)
+                continue
             gate = getattr(op, "gate", None)
             if not is_measurement_op(op):
                 sub_ops[where[op.qubits[0]]].append(op)
@@ -477,12 +479,29 @@ class _GpuSimulatorBase:
             for c, positions in groups.items():
                 sub_key = f"{_PART}{key}{_PART}{t}{_PART}{c}"
                 kwargs = {"key": sub_key, "invert_mask": tuple(inv[p] for p in positions)}
-                if gate.confusion_map:  # within one component (checked above)
+                if gate.confusion_map:  # within one component (checked by _untangled_parts)
                     kwargs["confusion_map"] = gate.confusion_map
                 sub_ops[c].append(cirq.measure(*[op.qubits[p] for p in positions], **kwargs))
                 measured[c] = True
                 pieces.append((sub_key, positions))
             assembly[key].append((pieces, len(op.qubits)))
+        return parts, sub_ops, measured, assembly, phases
+
+    def _run_untangled(self, circuit, param_resolver, repetitions):
+        """run() of a circuit whose qubits fall into components that no
+        operation joins, one component at a time.  The components are
+        independent, so the joint distribution of the records is the product
+        of theirs, which is what the reference samples from its product
+        state (cirq-core/cirq/sim/simulation_product_state.py).  Measurement
+        bits split across components are reassembled in the original order,
+        repetition by repetition; components without a measurement are not
+        simulated.  Returns None when the circuit does not split."""
+        from cirq_gb300.ir import flatten_ops
+
+        split = self._split_untangled(flatten_ops(circuit))
+        if split is None:
+            return None
+        parts, sub_ops, measured, assembly, _ = split
         records: dict = {}
         for c, ops_c in enumerate(sub_ops):
             if measured[c]:
@@ -497,6 +516,64 @@ class _GpuSimulatorBase:
                     arr[:, t, positions] = records[sub_key][:, 0, :]
             out[key] = arr
         return out
+
+    def _simulate_untangled(self, program, params, qubit_order, initial_state):
+        """simulate() of a circuit wider than one device state whose qubits
+        fall into untangled components: each component is simulated alone
+        and the results are held as the reference's own product state
+        (cirq.SimulationProductState of per-component states, merged only on
+        demand, as the reference's split_untangled_states does).  Yields
+        trial results, or returns None when the circuit does not split or
+        the initial state is not a basis index."""
+        from cirq_gb300.ir import flatten_ops
+
+        if initial_state is not None and not isinstance(initial_state, (int, np.integer)):
+            return None
+        qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+        split = self._split_untangled(flatten_ops(program), extra_qubits=qubits)
+        if split is None:
+            return None
+        parts, sub_ops, _, assembly, phase_ops = split
+        index = {q: i for i, q in enumerate(qubits)}
+        basis = int(initial_state or 0)
+        n = len(qubits)
+
+        def results():
+            for r in cirq.to_resolvers(params):
+                _check_all_resolved(program, r)
+                states: dict = {}
+                meas_parts: dict = {}
+                for c, part in enumerate(parts):
+                    order = sorted(part, key=lambda q: index[q])
+                    sub_basis = 0
+                    for q in order:
+                        sub_basis = (sub_basis << 1) | ((basis >> (n - 1 - index[q])) & 1)
+                    res = self.simulate(cirq.Circuit(sub_ops[c]), r, qubit_order=order, initial_state=sub_basis)
+                    st = res._final_simulator_state
+                    for q in order:
+                        states[q] = st
+                    meas_parts.update(res.measurements)
+                phase = 1.0 + 0j
+                for op in cirq.resolve_parameters(phase_ops, r):
+                    phase *= complex(np.asarray(cirq.unitary(op)).reshape(-1)[0])
+                if self._dm:
+                    states[None] = cirq.DensityMatrixSimulationState(
+                        qubits=(), initial_state=np.ones((1, 1)), dtype=np.complex64)
+                else:
+                    states[None] = cirq.StateVectorSimulationState(
+                        qubits=(), initial_state=np.array([phase], dtype=np.complex64), dtype=np.complex64)
+                product = cirq.SimulationProductState(states, qubits, split_untangled_states=True)
+                meas = {}
+                for key, instances in assembly.items():
+                    pieces, width = instances[-1]  # simulate() reports a key's last instance
+                    bits = np.zeros(width, dtype=np.uint8)
+                    for sub_key, positions in pieces:
+                        bits[positions] = meas_parts[sub_key]
+                    meas[key] = bits
+                cls = cirq.DensityMatrixTrialResult if self._dm else cirq.StateVectorTrialResult
+                yield cls(params=r, measurements=meas, final_simulator_state=product)
+
+        return results()
 
     def _run(self, circuit, param_resolver, repetitions) -> dict[str, np.ndarray]:
         param_resolver = param_resolver or cirq.ParamResolver({})
@@ -681,6 +758,13 @@ class Simulator(
                 self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
             )
             return
+        if self._split_untangled_states:
+            width = len(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+            if width * (2 if self._dm else 1) > _MAX_STATE_BITS:
+                parts = self._simulate_untangled(program, params, qubit_order, initial_state)
+                if parts is not None:
+                    yield from parts
+                    return
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine
@@ -829,6 +913,13 @@ class DensityMatrixSimulator(
                 self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
             )
             return
+        if self._split_untangled_states:
+            width = len(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
+            if width * (2 if self._dm else 1) > _MAX_STATE_BITS:
+                parts = self._simulate_untangled(program, params, qubit_order, initial_state)
+                if parts is not None:
+                    yield from parts
+                    return
         if self._traj_needed(program):
             qubits = tuple(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
             eng = self.engine

@@ -252,3 +252,26 @@ def test_noisy_density_matrix_run_of_untangled_blocks(emu):
         p = np.real(np.diag(simulate_density_matrix(block, qubit_order=qs)))
         idx = bits[:, 3 * b : 3 * b + 3].astype(int) @ np.array([4, 2, 1])
         assert _chi2_p(np.bincount(idx, minlength=8), p) > 1e-4
+
+
+def test_simulate_of_untangled_circuits_beyond_the_device_state(emu):
+    """simulate() of 36 untangled qubits: a product state of the blocks
+    (the reference's SimulationProductState, merged only on demand)."""
+    q, body, thetas = _blocks_circuit(12, seed=5)
+    c = body + cirq.measure(q[0], q[3], key="m")
+    res = cirq_gb300.Simulator(seed=3).simulate(c)
+    st = res._final_simulator_state
+    assert isinstance(st, cirq.SimulationProductState)
+    assert set(st.qubits) == set(q)
+    m = res.measurements["m"]
+    assert m.shape == (2,)
+    # an unmeasured block's state equals the oracle's
+    blk = st.sim_states[q[6]]
+    want = simulate_state_vector(cirq.Circuit(op for op in body.all_operations() if set(op.qubits) <= set(q[6:9])),
+                                 qubit_order=q[6:9])
+    np.testing.assert_allclose(blk.target_tensor.reshape(-1), want, atol=1e-5)
+    # a measured block collapsed to its record: q[0] and q[1] agree with m[0]
+    b0 = st.sim_states[q[0]].target_tensor.reshape(-1)
+    probs = np.abs(b0) ** 2
+    i = int(np.argmax(probs))
+    assert ((i >> 2) & 1) == m[0] and ((i >> 1) & 1) == m[0]
