@@ -18,8 +18,8 @@ Printed JSON line (rank 0):
 
 `--impl reference` times the reference (cirq.Simulator, complex64) on the
 host cores instead and prints the reference line.  Under torchrun with N > 1
-every rank simulates its own replica (replicas only: the workload has no
-cross-GPU exchange on one-GPU machines); value = N x gates / max time over ranks.
+every rank simulates its own replica (replicas only: the workload is one
+state per GPU, with no exchange step); value = N x gates / max time over ranks.
 """
 
 from __future__ import annotations
