@@ -166,3 +166,55 @@ def test_expectations_amplitudes_and_sweeps_match_the_reference(emu, seed):
         r = cirq.ParamResolver({"a": 0.3, "b": -0.4})
         np.testing.assert_allclose(ours.compute_amplitudes(c, bits, r), ref.compute_amplitudes(c, bits, r),
                                    atol=1e-5)
+
+
+def _measurement_circuit(rng, q):
+    """Random circuit exercising measurement semantics: mid-circuit
+    measurements (repeated keys included), classical controls on earlier
+    keys, invert masks, and a terminal measurement with a confusion map."""
+    n = len(q)
+    ops = []
+    keys = []
+    for step in range(int(rng.integers(3, 7))):
+        a = q[int(rng.integers(0, n))]
+        b = q[int(rng.integers(0, n))]
+        ops.append(cirq.ry(float(rng.uniform(0.3, 2.8))).on(a))
+        if a != b:
+            ops.append(cirq.CNOT(a, b))
+        r = rng.random()
+        if r < 0.35:
+            key = f"k{int(rng.integers(0, 3))}"
+            inv = (bool(rng.integers(0, 2)),)
+            ops.append(cirq.measure(a, key=key, invert_mask=inv))
+            keys.append(key)
+        elif r < 0.55 and keys:
+            ops.append(cirq.X(b).with_classical_controls(keys[int(rng.integers(0, len(keys)))]))
+    confusion = np.array([[0.9, 0.1], [0.2, 0.8]])
+    ops.append(cirq.measure(q[0], key="t", confusion_map={(0,): confusion}))
+    ops.append(cirq.measure(*q, key="all"))
+    return cirq.Circuit(ops, strategy=cirq.InsertStrategy.NEW)
+
+
+def _outcome_codes(result, key):
+    """One integer per repetition from all instances and bits of a key."""
+    rec = np.asarray(result.records[key]).astype(np.int64)
+    flat = rec.reshape(rec.shape[0], -1)
+    return flat @ (1 << np.arange(flat.shape[1] - 1, -1, -1))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_measurement_semantics_match_the_reference(emu, seed):
+    rng = np.random.default_rng(4000 + seed)
+    q = cirq.LineQubit.range(3)
+    c = _measurement_circuit(rng, q)
+    noise = [None, cirq.depolarize(0.05)][seed % 2]
+    dm = seed % 4 >= 2
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    reps = 500
+    want = ref_cls(noise=noise, seed=seed).run(c, repetitions=reps)
+    got = ours_cls(noise=noise, seed=seed + 7).run(c, repetitions=reps)
+    assert set(got.records) == set(want.records)
+    for key in want.records:
+        assert got.records[key].shape == want.records[key].shape, key
+        assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, (seed, key)
