@@ -152,10 +152,15 @@ struct Ctx {
 int ensure_scratch(Ctx* c, size_t bytes);
 int ensure_host_scratch(Ctx* c, size_t bytes);
 
-// Launchers (one translation unit per tile width).
+// Launchers (one translation unit per tile width; the 11- and 12-bit
+// two-state passes, and for 12 bits those with shared-memory dense ops, have
+// units of their own so the widest units compile in parallel).
 int launch_pass_l10(Ctx* c, const PassArgs& a, bool dual);
 int launch_pass_l11(Ctx* c, const PassArgs& a, bool dual);
+int launch_pass_l11_dual(Ctx* c, const PassArgs& a);
 int launch_pass_l12(Ctx* c, const PassArgs& a, bool dual);
+int launch_pass_l12_dual(Ctx* c, const PassArgs& a);
+int launch_pass_l12_dual_dense(Ctx* c, const PassArgs& a);
 int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
 int build_mma_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInfo& ti, uint64_t inmask,
                    MmaArgs& A);

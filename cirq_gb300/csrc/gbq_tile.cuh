@@ -1102,16 +1102,6 @@ inline bool ws_enabled() {
   return on == 1;
 }
 
-// Pipeline depth: 2 by default; GBQ_STAGES=3 selects three buffers.
-inline int pipeline_stages() {
-  static int st = -1;
-  if (st < 0) {
-    const char* e = getenv("GBQ_STAGES");
-    st = (e && atoi(e) == 3) ? 3 : 2;
-  }
-  return st;
-}
-
 // Widest register dense op of a pass.
 inline int pass_rkmax(const PassArgs& a) {
   int k = 0;
@@ -1136,7 +1126,6 @@ int launch_tile_pass(Ctx* c, const PassArgs& a) {
     // two-state (adjoint) passes of width <= 2 register ops: the lean variant
     if (pass_rkmax(a) <= 2) return launch_tile_pass_stages<LT, 0, true, 2, 2>(c, a);
   }
-  if (pipeline_stages() == 3) return launch_tile_pass_stages<LT, KMAX, DUAL, 3, 4>(c, a);
   return launch_tile_pass_stages<LT, KMAX, DUAL, 2, 4>(c, a);
 }
 
