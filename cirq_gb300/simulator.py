@@ -269,10 +269,8 @@ class _GpuSimulatorBase:
         records: dict[str, list] = {}
         for op in meas_ops:
             gate = op.gate
-            bits = [(idx >> (n - 1 - index[q])) & 1 for q in op.qubits]
-            inv = gate.full_invert_mask()
-            bits = [b ^ 1 if inv[i] else b for i, b in enumerate(bits)]
-            records.setdefault(gate.key, []).append(bits)
+            bits = np.array([[(idx >> (n - 1 - index[q])) & 1 for q in op.qubits]], dtype=np.int8)
+            records.setdefault(gate.key, []).append(_recorded_in_place(bits, op, self._prng)[0])
         # collapse: keep the sampled outcome, renormalise
         if self._dm:
             full_mask = mask | (mask << n)
@@ -315,15 +313,8 @@ class _GpuSimulatorBase:
             p = eng.norm2(state, n)
             if p > 0:
                 eng.scale(state, n, 1.0 / math.sqrt(p))
-        gate = op.gate
-        inv = gate.full_invert_mask()
         bits = np.array([[(idx >> (n - 1 - index[q])) & 1 for q in op.qubits]], dtype=np.int8)
-        for i in range(bits.shape[1]):
-            if inv[i]:
-                bits[0, i] ^= 1
-        if gate.confusion_map:
-            _confuse(bits, op.qubits, gate.confusion_map, self._prng)
-        return [int(b) for b in bits[0]]
+        return [int(b) for b in _recorded_in_place(bits, op, self._prng)[0]]
 
     def _traj_needed(self, program) -> bool:
         """Does this circuit need per-repetition trajectories?"""
@@ -660,6 +651,23 @@ class _Borrowed:
 
     def download(self, host):
         return self._buf.download(host)
+
+
+def _recorded_in_place(bits: np.ndarray, op, prng) -> np.ndarray:
+    """The record of a measurement performed in place (simulate(), and
+    run() with measurements that are not all terminal): its confusion map
+    first, then its invert mask, as SimulationState.measure does
+    (cirq-core/cirq/sim/simulation_state.py:70-98).  `bits` is
+    (repetitions, qubits), mutated and returned.  Terminal sampling in
+    run() applies them the other way round (_records_from_samples)."""
+    gate = op.gate
+    if gate.confusion_map:
+        _confuse(bits, op.qubits, gate.confusion_map, prng)
+    inv = gate.full_invert_mask()
+    for i in range(bits.shape[1]):
+        if inv[i]:
+            bits[:, i] ^= bits[:, i] < 2
+    return bits
 
 
 def _confuse(bits, qubits, confusion_map, prng) -> None:

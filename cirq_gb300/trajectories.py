@@ -471,6 +471,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
     mid-circuit measurement covers more than 5 qubits (the caller then runs
     trajectories one by one)."""
     from cirq_gb300.engine import Engine
+    from cirq_gb300.simulator import _recorded_in_place
 
     if reps < 1:
         return None
@@ -580,12 +581,12 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                                 row |= ((int(outcome[r]) >> jq) & 1) << (m - 1 - jq)
                             mats_k[r, row, row] = 1.0 / np.sqrt(prob[r])
                         run_slot(proj[j], mats_k, k, start)
-                        inv = op.gate.full_invert_mask()
                         key = cirq.measurement_key_name(op)
                         measured.setdefault(key, []).append(op.qubits)
+                        raw = ((outcome[:, None] >> np.arange(m)[None, :]) & 1).astype(np.int8)
+                        rec = _recorded_in_place(raw, op, prng)
                         for r in range(k):
-                            bits = [((int(outcome[r]) >> jq) & 1) ^ int(inv[jq]) for jq in range(m)]
-                            records[start + r].setdefault(key, []).append(bits)
+                            records[start + r].setdefault(key, []).append([int(b) for b in rec[r]])
                 if terminal:
                     samples[start : start + k] = eng.points_sample(states, n, k, prng.random_sample(k))
         finally:

@@ -149,3 +149,33 @@ def test_simulation_state_initial_states():
     dst = cirq.DensityMatrixSimulationState(qubits=qs, initial_state=5, dtype=np.complex64)
     rho = cirq_gb300.DensityMatrixSimulator().simulate(c, initial_state=dst).final_density_matrix
     assert np.max(np.abs(rho - simulate_density_matrix(c, initial_state=5))) < 2e-6
+
+
+_CONFUSION = np.array([[0.9, 0.1], [0.2, 0.8]])
+
+
+@pytest.mark.parametrize("dm", [False, True])
+@pytest.mark.parametrize("where", ["terminal", "mid", "control"])
+def test_invert_mask_and_confusion_map_orders(dm, where):
+    """A qubit in |0>, measured with an invert mask and a confusion map: the
+    record is 1 with p 0.9 where the measurement is performed in place
+    (confusion, then invert) and 0.8 where run() samples terminal
+    measurements at the end (invert, then confusion); a classical control
+    reads the recorded value."""
+    q0, q1 = cirq.LineQubit.range(2)
+    ops = [cirq.I(q0), cirq.I(q1),
+           cirq.measure(q0, key="a", invert_mask=(True,), confusion_map={(0,): _CONFUSION})]
+    if where == "mid":
+        ops.append(cirq.H(q0))
+    elif where == "control":
+        ops.append(cirq.X(q1).with_classical_controls("a"))
+    ops.append(cirq.measure(q1, key="b"))
+    c = cirq.Circuit(ops, strategy=cirq.InsertStrategy.NEW)
+    sim = (cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator)(seed=11)
+    res = sim.run(c, repetitions=4000)
+    p1 = float(np.mean(res.records["a"][:, 0, 0]))
+    assert abs(p1 - (0.8 if where == "terminal" else 0.9)) < 0.03
+    if where == "control":
+        np.testing.assert_array_equal(res.records["b"][:, 0, 0], res.records["a"][:, 0, 0])
+    got = [int(sim.simulate(cirq.Circuit(ops[2])).measurements["a"][0]) for _ in range(300)]
+    assert abs(np.mean(got) - 0.9) < 0.07

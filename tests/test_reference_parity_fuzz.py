@@ -218,3 +218,52 @@ def test_measurement_semantics_match_the_reference(emu, seed):
     for key in want.records:
         assert got.records[key].shape == want.records[key].shape, key
         assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, (seed, key)
+
+
+_CONFUSION = np.array([[0.9, 0.1], [0.2, 0.8]])
+
+
+def _confused_circuit(terminal: bool, mid_then_control: bool):
+    """One qubit in |0>, measured with an invert mask and a confusion map:
+    the reference records 1 with p 0.9 where it measures in place (confuse,
+    then invert: simulation_state.py:94-95) and 0.8 where it samples terminal
+    measurements at the end of run() (invert, then confuse:
+    simulator.py:803-808)."""
+    q0, q1 = cirq.LineQubit.range(2)
+    m = cirq.measure(q0, key="a", invert_mask=(True,), confusion_map={(0,): _CONFUSION})
+    ops = [cirq.I(q0), cirq.I(q1), m]
+    if not terminal:
+        ops.append(cirq.X(q1).with_classical_controls("a") if mid_then_control else cirq.H(q0))
+    ops.append(cirq.measure(q1, key="b"))
+    return cirq.Circuit(ops, strategy=cirq.InsertStrategy.NEW)
+
+
+@pytest.mark.parametrize("dm", [False, True])
+@pytest.mark.parametrize("terminal,control", [(True, False), (False, False), (False, True)])
+def test_invert_mask_and_confusion_map_orders_match_the_reference(emu, dm, terminal, control):
+    c = _confused_circuit(terminal, control)
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    reps = 2000
+    want = ref_cls(seed=3).run(c, repetitions=reps)
+    got = ours_cls(seed=4).run(c, repetitions=reps)
+    for key in ("a", "b"):
+        assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, key
+    p1 = float(np.mean(got.records["a"][:, 0, 0]))
+    assert abs(p1 - (0.8 if terminal else 0.9)) < 0.04
+    if control:
+        # the condition reads the recorded (confused, inverted) value
+        np.testing.assert_array_equal(got.records["b"][:, 0, 0], got.records["a"][:, 0, 0])
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_simulate_applies_confusion_maps_as_the_reference(emu, dm):
+    """simulate() measures in place: confusion, then the invert mask."""
+    q = cirq.LineQubit(0)
+    c = cirq.Circuit(cirq.measure(q, key="a", invert_mask=(True,), confusion_map={(0,): _CONFUSION}))
+    ours = (cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator)(seed=5)
+    got = np.array([int(ours.simulate(c).measurements["a"][0]) for _ in range(600)])
+    ref = (cirq.DensityMatrixSimulator if dm else cirq.Simulator)(seed=6)
+    want = np.array([int(ref.simulate(c).measurements["a"][0]) for _ in range(600)])
+    assert _two_sample_p(want, got) > 1e-3
+    assert abs(got.mean() - 0.9) < 0.05
