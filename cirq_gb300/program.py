@@ -492,7 +492,53 @@ def _param_has_unitary(op, resolver) -> bool:
     return cirq.has_unitary(cirq.resolve_parameters(op, resolver))
 
 
+class _ByIdentity:
+    """Cache-key stand-in for an operation that has neither a hash nor
+    operators to key on: equal only to itself (the cache entry holds it,
+    so its id stays unique)."""
+
+    __slots__ = ("op",)
+
+    def __init__(self, op):
+        self.op = op
+
+    def __hash__(self):
+        return id(self.op)
+
+    def __eq__(self, other):
+        return isinstance(other, _ByIdentity) and other.op is self.op
+
+
+def _op_key(op) -> Any:
+    """An operation as part of a cache key.  Unhashable operations (user
+    KrausChannel / MixedUnitaryChannel / MatrixGate-like gates with array
+    fields, PauliString operations) are keyed on the exact bytes of their
+    operators, with their type, qubits and measurement keys."""
+    try:
+        hash(op)
+        return op
+    except TypeError:
+        pass
+    if isinstance(op, Slot):
+        return ("slot", _op_key(op.op), op.slot)
+    cirq = ensure_cirq()
+    if cirq.is_parameterized(op) or isinstance(op.untagged, cirq.ClassicallyControlledOperation):
+        return _ByIdentity(op)
+    head = (type(op.untagged).__name__, tuple(op.qubits), tuple(sorted(map(str, cirq.measurement_key_objs(op)))))
+    u = cirq.unitary(op, default=None)
+    if u is not None:
+        return head + ("u", np.asarray(u, dtype=np.complex128).tobytes())
+    mix = cirq.mixture(op, default=None)
+    if mix is not None:
+        return head + ("m",) + tuple((float(p), np.asarray(m, dtype=np.complex128).tobytes()) for p, m in mix)
+    kraus = cirq.kraus(op, default=None)
+    if kraus is not None:
+        return head + ("k",) + tuple(np.asarray(k, dtype=np.complex128).tobytes() for k in kraus)
+    return _ByIdentity(op)
+
+
 def structure_key(ops, qubits, dm, planner: Planner, noise_repr: str = "") -> Any:
     """A cache key for the compiled structure of an op list (parameter values of
     unparameterised gates are part of the structure)."""
-    return (tuple(ops), tuple(qubits), dm, planner.tile_bits, planner.kmax, planner.budget, noise_repr)
+    return (tuple(_op_key(op) for op in ops), tuple(qubits), dm, planner.tile_bits, planner.kmax, planner.budget,
+            noise_repr)

@@ -37,6 +37,7 @@ from cirq_gb300.engine import Engine, default_engine
 from cirq_gb300.ir import pauli_terms
 from cirq_gb300.planner import Planner
 from cirq_gb300.program import CompiledCircuit, split_measurements, structure_key
+from cirq_gb300 import qudits as _qudits
 from cirq_gb300 import trajectories as _traj
 
 cirq = ensure_cirq()
@@ -353,14 +354,12 @@ class _GpuSimulatorBase:
             return initial_state, qubit_order
         merged = initial_state.create_merged_state()
         qubits = tuple(merged.qubits)
-        if any(q.dimension != 2 for q in qubits):
-            raise NotImplementedError("only qubit initial states are supported")
-        n = len(qubits)
+        size = int(np.prod([q.dimension for q in qubits], dtype=np.int64))
         tensor = np.asarray(merged.target_tensor)
         if isinstance(merged, cirq.DensityMatrixSimulationState):
             if not self._dm:
                 raise ValueError("a density-matrix initial state needs cirq_gb300.DensityMatrixSimulator")
-            raw = tensor.reshape(2**n, 2**n)
+            raw = tensor.reshape(size, size)
         elif isinstance(merged, cirq.StateVectorSimulationState):
             raw = tensor.reshape(-1)
         else:
@@ -381,6 +380,8 @@ class _GpuSimulatorBase:
         from cirq_gb300.steps import moment_steps
 
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
+        if _qudits.has_qudits(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(circuit.all_qubits())):
+            return _qudits.moment_steps(self, circuit, param_resolver, qubit_order, initial_state)
         return moment_steps(self, circuit, param_resolver, qubit_order, initial_state)
 
     def _traj_expectations(self, program, pslist, params, qubit_order, initial_state):
@@ -414,15 +415,16 @@ class _GpuSimulatorBase:
         index = {q: i for i, q in enumerate(compiled.qubits)}
         results: dict[str, list] = {}
         for op in meas_ops:
-            gate = op.gate
             out = np.zeros((repetitions, len(op.qubits)), dtype=np.int8)
-            inv = gate.full_invert_mask()
             for i, q in enumerate(op.qubits):
                 out[:, i] = (samples >> (n - 1 - index[q])) & 1
+            out, gate, qids = _qudits.recorded_view(op, out)
+            inv = gate.full_invert_mask()
+            for i in range(out.shape[1]):
                 if inv[i]:
                     out[:, i] ^= out[:, i] < 2
             if gate.confusion_map:
-                _confuse(out, op.qubits, gate.confusion_map, self._prng)
+                _confuse(out, qids, gate.confusion_map, self._prng)
             results.setdefault(gate.key, []).append(out)
         return {k: np.array(v).swapaxes(0, 1) for k, v in results.items()}
 
@@ -572,6 +574,8 @@ class _GpuSimulatorBase:
         if self.noise is not cirq.NO_NOISE:
             return self._noiseless()._run(self._reference_noisy_circuit(circuit, "run"), param_resolver, repetitions)
         qubits = tuple(sorted(circuit.all_qubits()))
+        if _qudits.has_qudits(qubits):
+            return _qudits.run(self, circuit, param_resolver, repetitions)
         if self._split_untangled_states and len(qubits) * (2 if self._dm else 1) > _MAX_STATE_BITS:
             rec = self._run_untangled(circuit, param_resolver, repetitions)
             if rec is not None:
@@ -658,11 +662,12 @@ def _recorded_in_place(bits: np.ndarray, op, prng) -> np.ndarray:
     run() with measurements that are not all terminal): its confusion map
     first, then its invert mask, as SimulationState.measure does
     (cirq-core/cirq/sim/simulation_state.py:70-98).  `bits` is
-    (repetitions, qubits), mutated and returned.  Terminal sampling in
-    run() applies them the other way round (_records_from_samples)."""
-    gate = op.gate
+    (repetitions, qubits); a qudit measurement's record is its levels.
+    Terminal sampling in run() applies them the other way round
+    (_records_from_samples)."""
+    bits, gate, qids = _qudits.recorded_view(op, bits)
     if gate.confusion_map:
-        _confuse(bits, op.qubits, gate.confusion_map, prng)
+        _confuse(bits, qids, gate.confusion_map, prng)
     inv = gate.full_invert_mask()
     for i in range(bits.shape[1]):
         if inv[i]:
@@ -673,18 +678,20 @@ def _recorded_in_place(bits: np.ndarray, op, prng) -> np.ndarray:
 def _confuse(bits, qubits, confusion_map, prng) -> None:
     """Applies measurement confusion matrices per repetition, as
     StepResult._confuse_results does (cirq-core/cirq/sim/simulator.py:822-844)."""
+    dims = [q.dimension for q in qubits]
     for rep in bits:
         for indices, confuser in confusion_map.items():
-            row = cirq.big_endian_digits_to_int((rep[k] for k in indices), base=[2] * len(indices))
+            mat_dims = [dims[k] for k in indices]
+            row = cirq.big_endian_digits_to_int((rep[k] for k in indices), base=mat_dims)
             new_val = prng.choice(len(confuser), p=confuser[row])
-            new_bits = cirq.big_endian_int_to_digits(new_val, base=[2] * len(indices))
+            new_bits = cirq.big_endian_int_to_digits(new_val, base=mat_dims)
             for i, k in enumerate(indices):
                 rep[k] = new_bits[i]
 
 
 def _state_vector_result(params, measurements, qubits, vec: np.ndarray):
     """Builds a genuine cirq.StateVectorTrialResult around `vec` without copying it."""
-    shape = (2,) * len(qubits)
+    shape = tuple(q.dimension for q in qubits)
     try:
         from cirq.sim.state_vector_simulation_state import _BufferedStateVector
 
@@ -710,13 +717,14 @@ def _density_matrix_result(params, measurements, qubits, rho: np.ndarray):
     reference's re-validation (an eigen-decomposition of the 2^n x 2^n matrix
     on the host, seconds at 13 qubits); rho comes from trace-preserving
     channels applied on the device."""
-    n = len(qubits)
+    shape = tuple(q.dimension for q in qubits)
+    size = int(np.prod(shape, dtype=np.int64))
     try:
         from cirq.sim.density_matrix_simulation_state import _BufferedDensityMatrix
 
         st = cirq.DensityMatrixSimulationState.__new__(cirq.DensityMatrixSimulationState)
         empty = np.empty(0, dtype=np.complex64)
-        buffered = _BufferedDensityMatrix(rho.reshape((2,) * (2 * n)), [empty, empty, empty])
+        buffered = _BufferedDensityMatrix(rho.reshape(shape + shape), [empty, empty, empty])
         cirq.SimulationState.__init__(st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None)
     except Exception:  # pragma: no cover - public-constructor route (validates, copies)
         st = cirq.DensityMatrixSimulationState(qubits=tuple(qubits), initial_state=rho, dtype=np.complex64)
@@ -725,7 +733,7 @@ def _density_matrix_result(params, measurements, qubits, rho: np.ndarray):
     # state tensor (density_matrix_simulator.py:369-374: 44 ms at 13 qubits);
     # the downloaded matrix is already a fresh array, so it is handed over
     if hasattr(res, "_final_density_matrix"):
-        res._final_density_matrix = rho.reshape(2**n, 2**n)
+        res._final_density_matrix = rho.reshape(size, size)
     return res
 
 
@@ -765,6 +773,9 @@ class Simulator(
             yield from self._noiseless().simulate_sweep_iter(
                 self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
             )
+            return
+        if _qudits.has_qudits(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits())):
+            yield from _qudits.simulate_sweep(self, program, params, qubit_order, initial_state)
             return
         if self._split_untangled_states:
             width = len(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
@@ -834,6 +845,9 @@ class Simulator(
                 self._reference_noisy_circuit(program, "simulate"), pslist, params, qubit_order,
                 initial_state, permit_terminal_measurements=True,
             )
+            return
+        if _qudits.has_qudits(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits())):
+            yield from _qudits.expectation_values(self, program, pslist, params, qubit_order, initial_state)
             return
         if self._traj_needed(program) or program.has_measurements():
             # the reference evaluates the final state of simulate(), which
@@ -905,6 +919,10 @@ class DensityMatrixSimulator(
             return eng.new_state(2 * n, basis=(i << n) | i, nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("unwrap SimulationState initial states first")
+        if isinstance(initial_state, np.ndarray) and initial_state.dtype != np.complex64:
+            # the reference casts an array to the simulator's dtype first
+            # (cirq-core/cirq/sim/density_matrix_simulation_state.py:84-89)
+            initial_state = initial_state.astype(np.complex64)
         rho = cirq.to_valid_density_matrix(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
         return eng.new_state(2 * n, initial=rho.reshape(-1), nbits_dev=compiled.nbits_dev, into=into)
 
@@ -920,6 +938,9 @@ class DensityMatrixSimulator(
             yield from self._noiseless().simulate_sweep_iter(
                 self._reference_noisy_circuit(program, "simulate"), params, qubit_order, initial_state
             )
+            return
+        if _qudits.has_qudits(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits())):
+            yield from _qudits.simulate_sweep(self, program, params, qubit_order, initial_state)
             return
         if self._split_untangled_states:
             width = len(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits()))
@@ -983,6 +1004,9 @@ class DensityMatrixSimulator(
                 self._reference_noisy_circuit(program, "simulate"), pslist, params, qubit_order,
                 initial_state, permit_terminal_measurements=True,
             )
+            return
+        if _qudits.has_qudits(cirq.QubitOrder.as_qubit_order(qubit_order).order_for(program.all_qubits())):
+            yield from _qudits.expectation_values(self, program, pslist, params, qubit_order, initial_state)
             return
         if self._traj_needed(program) or program.has_measurements():
             yield from self._traj_expectations(program, pslist, params, qubit_order, initial_state)

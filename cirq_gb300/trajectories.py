@@ -40,6 +40,7 @@ import numpy as np
 from cirq_gb300._cirq_env import ensure_cirq
 from cirq_gb300.ir import UnsupportedOperation, flatten_ops
 from cirq_gb300.program import Slot, TrajectoryPoint
+from cirq_gb300.qudits import record_qids
 
 cirq = ensure_cirq()
 
@@ -360,7 +361,7 @@ class TrajectoryRunner:
                 bits = sim._measure_op(state, self.empty, it.op)
                 key = cirq.measurement_key_name(it.op)
                 records.setdefault(key, []).append(bits)
-                measured.setdefault(key, []).append(it.op.qubits)
+                measured.setdefault(key, []).append(record_qids(it.op))
             elif isinstance(it, Conditional):
                 c = self.compiled[j]
                 if c.plan.npasses and conditions_hold(it.op, records, measured):
@@ -582,7 +583,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                             mats_k[r, row, row] = 1.0 / np.sqrt(prob[r])
                         run_slot(proj[j], mats_k, k, start)
                         key = cirq.measurement_key_name(op)
-                        measured.setdefault(key, []).append(op.qubits)
+                        measured.setdefault(key, []).append(record_qids(op))
                         raw = ((outcome[:, None] >> np.arange(m)[None, :]) & 1).astype(np.int8)
                         rec = _recorded_in_place(raw, op, prng)
                         for r in range(k):

@@ -49,7 +49,8 @@ def simulate_state_vector(
     qubit_order=None,
     initial_state: int | np.ndarray = 0,
 ) -> np.ndarray:
-    """Final state vector (complex128, flattened big-endian) of a unitary circuit.
+    """Final state vector (complex128, flattened big-endian) of a unitary
+    circuit over qids of any dimension (mixed radix, as the reference).
 
     Measurements are skipped (they are terminal in every caller); any other
     non-unitary operation raises ``TypeError`` as the reference does for ops
@@ -59,13 +60,15 @@ def simulate_state_vector(
     qubit_order = cirq.QubitOrder.DEFAULT if qubit_order is None else qubit_order
     qubits = _ordered_qubits(circuit, qubit_order)
     n = len(qubits)
+    dims = tuple(q.dimension for q in qubits)
+    size = int(np.prod(dims, dtype=np.int64))
     index = {q: i for i, q in enumerate(qubits)}
     if isinstance(initial_state, (int, np.integer)):
-        psi = np.zeros(2**n, dtype=np.complex128)
+        psi = np.zeros(size, dtype=np.complex128)
         psi[int(initial_state)] = 1
     else:
         psi = np.asarray(initial_state, dtype=np.complex128).reshape(-1).copy()
-    t = psi.reshape((2,) * n) if n else psi
+    t = psi.reshape(dims) if n else psi
     for op in _ops(circuit, param_resolver):
         if cirq.is_measurement(op):
             continue
@@ -83,7 +86,8 @@ def simulate_density_matrix(
     noise=None,
     initial_state: int = 0,
 ) -> np.ndarray:
-    """Final density matrix (complex128, 2^n x 2^n) of a possibly noisy circuit.
+    """Final density matrix (complex128, D x D for D the product of the qid
+    dimensions) of a possibly noisy circuit.
 
     Unitary ops use ``apply_unitary_dm`` and channels ``apply_kraus_dm``,
     restating the strategy order of ``protocols.apply_channel``
@@ -95,10 +99,12 @@ def simulate_density_matrix(
     qubit_order = cirq.QubitOrder.DEFAULT if qubit_order is None else qubit_order
     qubits = _ordered_qubits(circuit, qubit_order)
     n = len(qubits)
+    dims = tuple(q.dimension for q in qubits)
+    size = int(np.prod(dims, dtype=np.int64))
     index = {q: i for i, q in enumerate(qubits)}
-    rho = np.zeros((2**n, 2**n), dtype=np.complex128)
+    rho = np.zeros((size, size), dtype=np.complex128)
     rho[initial_state, initial_state] = 1
-    t = rho.reshape((2,) * (2 * n))
+    t = rho.reshape(dims + dims)
     resolved = cirq.resolve_parameters(circuit, param_resolver or cirq.ParamResolver({}))
     if noise is not None:
         model = cirq.NoiseModel.from_noise_model_like(noise)
@@ -113,7 +119,7 @@ def simulate_density_matrix(
                 t = apply_unitary_dm(t, n, axes, cirq.unitary(op))
             else:
                 t = apply_kraus_dm(t, n, axes, cirq.kraus(op))
-    return np.asarray(t).reshape(2**n, 2**n)
+    return np.asarray(t).reshape(size, size)
 
 
 def pauli_sum_terms(observable, qubit_index) -> list[tuple[complex, dict[int, str]]]:

@@ -27,14 +27,16 @@ def apply_matrix(tensor: np.ndarray, axes: Sequence[int], matrix: np.ndarray) ->
     """Left-multiplies ``matrix`` onto ``axes`` of ``tensor``; returns a new tensor.
 
     Restates ``targeted_left_multiply`` (``cirq-core/cirq/linalg/transformations.py:105-172``):
-    the 2^k x 2^k matrix is viewed as a (2,)*2k tensor whose first k axes are
+    the matrix over the target axes (dimension d_j each: 2 for qubits) is
+    viewed as a (d_0..d_{k-1}, d_0..d_{k-1}) tensor whose first k axes are
     output axes and last k input axes, ``axes[0]`` being the most significant
-    matrix-index bit; the contraction replaces each target axis by the
+    matrix-index digit; the contraction replaces each target axis by the
     corresponding output axis.
     """
     k = len(axes)
     d = tensor.ndim
-    m = np.asarray(matrix).reshape((2,) * (2 * k))
+    dims = tuple(tensor.shape[a] for a in axes)
+    m = np.asarray(matrix).reshape(dims + dims)
     work = list(range(k))
     data = list(range(k, k + d))
     inp = work + [data[a] for a in axes]

@@ -179,6 +179,14 @@ def main(ref_path: str) -> None:
         cirq.Simulator(dtype=np.complex128).simulate(_wide_controlled_circuit(cirq)).final_state_vector
     )
 
+    qc, qorder = _qudit_circuit(cirq)
+    out["qudit_sv_c128"] = (
+        cirq.Simulator(dtype=np.complex128).simulate(qc, qubit_order=qorder, initial_state=17).final_state_vector
+    )
+    out["qudit_dm_c128"] = (
+        cirq.DensityMatrixSimulator(dtype=np.complex128).simulate(_qudit_noisy_circuit(cirq)).final_density_matrix
+    )
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     with open(os.path.join(HERE, "golden_meta.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py with cirq {cirq.__version__}\n")
@@ -271,6 +279,83 @@ def _wide_controlled_circuit(cirq):
         cirq.rz(0.3).on(q[7]).controlled_by(*q[1:6]),
         cirq.CZ(q[0], q[7]),
         cirq.Y(q[2]).controlled_by(q[0], q[1], q[3], q[4], q[5], q[7], control_values=[1, 0, 1, 1, 0, 1]),
+    )
+
+
+def _givens(d: int, i: int, j: int, theta: float, phi: float) -> np.ndarray:
+    """A rotation by theta (with phase phi) in the (i, j) plane of d levels."""
+    g = np.eye(d, dtype=np.complex128)
+    c, s = np.cos(theta), np.sin(theta)
+    g[i, i], g[j, j] = c, c
+    g[i, j], g[j, i] = -s * np.exp(-1j * phi), s * np.exp(1j * phi)
+    return g
+
+
+def _qudit_unitary(d: int, seed: int) -> np.ndarray:
+    """A dense d-level unitary from closed-form factors (Givens rotations
+    and phases), identical on every machine."""
+    u = np.diag(np.exp(1j * (0.3 + 0.17 * seed) * np.arange(d) ** 2))
+    for k in range(2 * d):
+        i, j = k % d, (k * (seed + 2) + 1) % d
+        if i != j:
+            u = _givens(d, i, j, 0.4 + 0.11 * k + 0.07 * seed, 0.2 * k - 0.3 * seed) @ u
+    return u
+
+
+def _qudit_circuit(cirq):
+    """Qids of dimensions 3, 2, 4 and 5 (8 index bits) with one- and two-qid
+    unitaries; simulated with a custom qubit order."""
+    q3, q2, q4, q5 = cirq.LineQid(0, 3), cirq.LineQubit(1), cirq.LineQid(2, 4), cirq.LineQid(3, 5)
+    dft4 = np.exp(2j * np.pi * np.outer(np.arange(4), np.arange(4)) / 4) / 2
+    c = cirq.Circuit(
+        cirq.MatrixGate(_qudit_unitary(3, 1), qid_shape=(3,)).on(q3),
+        cirq.H(q2),
+        cirq.MatrixGate(dft4, qid_shape=(4,)).on(q4),
+        cirq.MatrixGate(_qudit_unitary(5, 2), qid_shape=(5,)).on(q5),
+        cirq.MatrixGate(_qudit_unitary(6, 3), qid_shape=(3, 2)).on(q3, q2),
+        cirq.MatrixGate(_qudit_unitary(20, 4), qid_shape=(4, 5)).on(q4, q5),
+        cirq.rz(0.4).on(q2),
+        cirq.MatrixGate(_qudit_unitary(12, 5), qid_shape=(3, 4)).on(q3, q4),
+    )
+    return c, [q5, q2, q3, q4]
+
+
+def _qudit_noisy_circuit(cirq):
+    """Qutrit and ququart channels (damping, a mixture, a reset) between
+    unitaries, for the density-matrix simulator."""
+    q3, q2, q4 = cirq.LineQid(0, 3), cirq.LineQubit(1), cirq.LineQid(2, 4)
+    g = 0.25
+    k0 = np.diag([1.0, np.sqrt(1 - g), np.sqrt(1 - g)]).astype(np.complex128)
+    k1 = np.zeros((3, 3), dtype=np.complex128)
+    k1[0, 1] = np.sqrt(g)
+    k2 = np.zeros((3, 3), dtype=np.complex128)
+    k2[1, 2] = np.sqrt(g)
+    shift = np.roll(np.eye(4), 1, axis=0)
+
+    class QutritDamping(cirq.Gate):
+        def _qid_shape_(self):
+            return (3,)
+
+        def _kraus_(self):
+            return [k0, k1, k2]
+
+    class QuartShift(cirq.Gate):
+        def _qid_shape_(self):
+            return (4,)
+
+        def _mixture_(self):
+            return [(0.7, np.eye(4)), (0.3, shift)]
+
+    return cirq.Circuit(
+        cirq.MatrixGate(_qudit_unitary(3, 6), qid_shape=(3,)).on(q3),
+        cirq.H(q2),
+        cirq.MatrixGate(_qudit_unitary(4, 7), qid_shape=(4,)).on(q4),
+        cirq.MatrixGate(_qudit_unitary(6, 8), qid_shape=(3, 2)).on(q3, q2),
+        QutritDamping().on(q3),
+        QuartShift().on(q4),
+        cirq.MatrixGate(_qudit_unitary(8, 9), qid_shape=(2, 4)).on(q2, q4),
+        cirq.ResetChannel(dimension=3).on(q3),
+        cirq.MatrixGate(_qudit_unitary(3, 10), qid_shape=(3,)).on(q3),
     )
 
 

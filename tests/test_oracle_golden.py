@@ -126,6 +126,18 @@ def test_wide_controlled_gates():
     np.testing.assert_allclose(oc.simulate_state_vector(c), GOLD["wide_controlled_c128"], atol=1e-12)
 
 
+def test_qudit_circuits():
+    """Qids of dimensions 2..5: mixed-radix states and qudit channels."""
+    import make_zoo
+
+    mg = make_zoo.golden_module()
+    c, order = mg._qudit_circuit(cirq)
+    got = oc.simulate_state_vector(c, qubit_order=order, initial_state=17)
+    np.testing.assert_allclose(got, GOLD["qudit_sv_c128"], atol=1e-12)
+    rho = oc.simulate_density_matrix(mg._qudit_noisy_circuit(cirq))
+    np.testing.assert_allclose(rho, GOLD["qudit_dm_c128"], atol=1e-12)
+
+
 def test_noise_placement_of_the_density_matrix_simulator():
     """Noise placed by the package's host-side rule (prefix / suffix split of
     the reference's density-matrix simulator) + the oracle's arithmetic

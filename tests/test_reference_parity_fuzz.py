@@ -267,3 +267,17 @@ def test_simulate_applies_confusion_maps_as_the_reference(emu, dm):
     want = np.array([int(ref.simulate(c).measurements["a"][0]) for _ in range(600)])
     assert _two_sample_p(want, got) > 1e-3
     assert abs(got.mean() - 0.9) < 0.05
+
+
+def test_complex128_array_initial_states_are_cast_as_the_reference(emu):
+    q = cirq.LineQubit.range(2)
+    c = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q), cirq.amplitude_damp(0.2).on(q[1]))
+    rho = cirq.testing.random_density_matrix(4, random_state=4)
+    assert rho.dtype == np.complex128
+    want = cirq.DensityMatrixSimulator().simulate(c, initial_state=rho).final_density_matrix
+    got = cirq_gb300.DensityMatrixSimulator().simulate(c, initial_state=rho).final_density_matrix
+    np.testing.assert_allclose(got, want, atol=1e-5)
+    vec = cirq.testing.random_superposition(4, random_state=5)
+    u = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q))
+    np.testing.assert_allclose(cirq_gb300.Simulator().simulate(u, initial_state=vec).final_state_vector,
+                               cirq.Simulator().simulate(u, initial_state=vec).final_state_vector, atol=1e-5)
