@@ -110,7 +110,8 @@ def flatten_ops(circuit) -> list:
 
 def is_measurement_op(op) -> bool:
     """cirq.is_measurement, answered without the protocol for the common
-    gate families (unitary by construction) and for measurement gates."""
+    gate families (unitary by construction) and for measurement gates.  A
+    channel with a measurement key is a channel here (is_keyed_channel)."""
     cirq = _cirq()
     gate = getattr(op, "gate", None)
     if gate is not None:
@@ -118,7 +119,21 @@ def is_measurement_op(op) -> bool:
             return True
         if isinstance(gate, (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)):
             return False
-    return cirq.is_measurement(op)
+    return cirq.is_measurement(op) and not is_keyed_channel(op)
+
+
+def is_keyed_channel(op) -> bool:
+    """A mixture or Kraus channel with a measurement key: the state-vector
+    simulator records the index of the operator that acted
+    (cirq-core/cirq/sim/state_vector_simulation_state.py:183-257,
+    ``record_channel_measurement``); the density-matrix simulator applies the
+    channel and records nothing."""
+    cirq = _cirq()
+    if isinstance(getattr(op, "gate", None), cirq.MeasurementGate):
+        return False
+    if isinstance(op.untagged, cirq.ClassicallyControlledOperation):
+        return False
+    return cirq.is_measurement(op) and (cirq.has_mixture(op) or cirq.has_kraus(op))
 
 
 def _needs_decomposition(op) -> bool:

@@ -429,8 +429,7 @@ class _GpuSimulatorBase:
         return {k: np.array(v).swapaxes(0, 1) for k, v in results.items()}
 
     # ---- SimulatesSamples ---------------------------------------------------
-    @staticmethod
-    def _split_untangled(ops, extra_qubits=()):
+    def _split_untangled(self, ops, extra_qubits=()):
         """(parts, per-part op lists, measured flags, assembly, phase ops) of
         a flattened op list whose qubits fall into components no operation
         joins, or None (see _untangled_parts).  A measurement across
@@ -438,8 +437,10 @@ class _GpuSimulatorBase:
         keys; assembly[key] lists, per instance, the (internal key, bit
         positions) pieces and the width.  `extra_qubits` (idle qubits of a
         qubit order) become components of their own."""
-        from cirq_gb300.ir import is_measurement_op
+        from cirq_gb300.ir import is_keyed_channel, is_measurement_op
 
+        if not self._dm and any(is_keyed_channel(op) for op in ops):
+            return None  # channel records stay with the whole state
         parts = _untangled_parts(ops)
         if parts is None:
             return None

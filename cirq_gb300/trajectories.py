@@ -38,7 +38,7 @@ from typing import Any
 import numpy as np
 
 from cirq_gb300._cirq_env import ensure_cirq
-from cirq_gb300.ir import UnsupportedOperation, flatten_ops
+from cirq_gb300.ir import UnsupportedOperation, flatten_ops, is_keyed_channel
 from cirq_gb300.program import Slot, TrajectoryPoint
 from cirq_gb300.qudits import record_qids
 
@@ -67,15 +67,24 @@ class Measure:
 class Channel:
     op: Any
     slot: int
+    key: str | None = None  # a keyed channel records the index of its drawn operator
 
 
 @dataclasses.dataclass
 class Conditional:
-    """A classically controlled unitary: applied in a trajectory when all of
-    its conditions hold on that trajectory's records so far."""
+    """A classically controlled operation: applied in a trajectory when all
+    of its conditions hold on that trajectory's records so far
+    (``ClassicallyControlledOperation._act_on_``,
+    cirq-core/cirq/ops/classically_controlled_operation.py)."""
 
     op: Any  # the ClassicallyControlledOperation (untagged)
-    inner: Any  # the controlled unitary op
+    inner: Any  # the controlled operation
+    # "program": a compiled program (a unitary; on the density-matrix
+    # simulator also a channel, as its superoperator); "channel": a Kraus
+    # draw in slot `slot` (state-vector simulator).  The reference forbids
+    # classical control of operations with measurement keys.
+    kind: str = "program"
+    slot: int = -1
 
 
 def is_classically_controlled(op) -> bool:
@@ -86,13 +95,17 @@ def conditions_hold(op, records: dict, measured: dict) -> bool:
     """Evaluates a ClassicallyControlledOperation's conditions with the
     reference's own Condition.resolve (cirq-core/cirq/value/condition.py)
     on the trajectory's records: records[key] = [bits, ...] (as recorded,
-    invert masks applied), measured[key] = [qubits, ...] of each instance.
+    invert masks applied), measured[key] = [qubits, ...] of each instance
+    (None for a keyed channel's record, [operator index]).
     A condition on a key not measured yet raises ValueError, as the
     reference does."""
+    channel = {k for k, v in measured.items() if v and v[0] is None}  # keyed channels' records
     keyed = {cirq.MeasurementKey.parse_serialized(k): [tuple(int(b) for b in bits) for bits in v]
-             for k, v in records.items()}
-    qubits = {cirq.MeasurementKey.parse_serialized(k): [tuple(q) for q in v] for k, v in measured.items()}
-    store = cirq.ClassicalDataDictionaryStore(_records=keyed, _measured_qubits=qubits)
+             for k, v in records.items() if k not in channel}
+    chans = {cirq.MeasurementKey.parse_serialized(k): [int(v[0]) for v in records[k]] for k in channel}
+    qubits = {cirq.MeasurementKey.parse_serialized(k): [tuple(q) for q in v] for k, v in measured.items()
+              if k not in channel}
+    store = cirq.ClassicalDataDictionaryStore(_records=keyed, _measured_qubits=qubits, _channel_records=chans)
     return all(c.resolve(store) for c in op.classical_controls)
 
 
@@ -135,10 +148,31 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
         if is_classically_controlled(op):
             cc = op.untagged
             inner = cc.without_classical_controls()
-            if cirq.is_measurement(inner) or cirq.is_parameterized(inner) or not cirq.has_unitary(inner):
-                raise UnsupportedOperation(f"classical control of a non-unitary operation: {op!r}")
+            if cirq.is_parameterized(inner):
+                raise UnsupportedOperation(f"classical control of a parameterized operation: {op!r}")
             flush()
-            items.append(Conditional(cc, inner))
+            if dm or cirq.has_unitary(inner):
+                items.append(Conditional(cc, inner, "program"))
+            elif cirq.has_kraus(inner):
+                if len(inner.qubits) > 5:
+                    raise UnsupportedOperation(f"channels on more than 5 qubits are not supported: {op!r}")
+                items.append(Conditional(cc, inner, "channel", nslot))
+                nslot += 1
+            else:
+                raise TypeError(
+                    "Can't simulate operations that don't implement SupportsUnitary, "
+                    f"SupportsConsistentApplyUnitary, SupportsMixture or is a measurement: {op!r}"
+                )
+            continue
+        if is_keyed_channel(op):
+            if dm:
+                cur.append(op)  # a channel; the density-matrix simulator records nothing
+                continue
+            if len(op.qubits) > 5:
+                raise UnsupportedOperation(f"channels on more than 5 qubits are not supported: {op!r}")
+            flush()
+            items.append(Channel(op, nslot, cirq.measurement_key_name(op)))
+            nslot += 1
             continue
         if cirq.is_measurement(op):
             if not isinstance(getattr(op, "gate", None), cirq.MeasurementGate):
@@ -224,17 +258,17 @@ class TrajectoryRunner:
         base = [cirq.ParamResolver({})]
         self.compiled = [
             sim._compile(it.ops, self.qubits, base) if isinstance(it, Segment)
-            else sim._compile([it.inner], self.qubits, base) if isinstance(it, Conditional)
+            else sim._compile([it.inner], self.qubits, base)
+            if isinstance(it, Conditional) and it.kind == "program"
             else None
             for it in self.items
         ]
         self.empty = sim._compile([], self.qubits, base)  # geometry of the state buffer
-        self.kraus_seg = {}
-        for it in self.items:
-            if isinstance(it, Channel):
-                self.kraus_seg[it.slot] = slot_program(sim, it.op.qubits, self.qubits)
-        self._kraus = {it.slot: [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(it.op)]
-                       for it in self.items if isinstance(it, Channel)}
+        # Kraus channels (drawn per trajectory), plain or classically controlled
+        channels = [it if isinstance(it, Channel) else Channel(it.inner, it.slot) for it in self.items
+                    if isinstance(it, Channel) or (isinstance(it, Conditional) and it.kind == "channel")]
+        self.kraus_seg = {c.slot: slot_program(sim, c.op.qubits, self.qubits) for c in channels}
+        self._kraus = {c.slot: [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(c.op)] for c in channels}
         # device buffers reused by every trajectory: the state and one
         # matrix pool per segment / channel
         self._state = None
@@ -358,17 +392,28 @@ class TrajectoryRunner:
                     pool = pools[j][rep] if pools[j] is not None else c.plan.pool
                     eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), pool))
             elif isinstance(it, Measure):
-                bits = sim._measure_op(state, self.empty, it.op)
-                key = cirq.measurement_key_name(it.op)
-                records.setdefault(key, []).append(bits)
-                measured.setdefault(key, []).append(record_qids(it.op))
+                self._measure(state, it.op, records, measured)
             elif isinstance(it, Conditional):
-                c = self.compiled[j]
-                if c.plan.npasses and conditions_hold(it.op, records, measured):
-                    eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), c.plan.pool))
+                if not conditions_hold(it.op, records, measured):
+                    continue
+                if it.kind == "channel":
+                    self._apply_kraus(state, Channel(it.inner, it.slot), picks)
+                else:
+                    c = self.compiled[j]
+                    if c.plan.npasses:
+                        eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), c.plan.pool))
             else:
-                self._apply_kraus(state, it, picks)
+                index = self._apply_kraus(state, it, picks)
+                if it.key is not None:
+                    records.setdefault(it.key, []).append([index])
+                    measured.setdefault(it.key, []).append(None)
         return records
+
+    def _measure(self, state, op, records: dict, measured: dict) -> None:
+        bits = self.sim._measure_op(state, self.empty, op)
+        key = cirq.measurement_key_name(op)
+        records.setdefault(key, []).append(bits)
+        measured.setdefault(key, []).append(record_qids(op))
 
     def _apply_kraus(self, state, it: Channel, picks: dict) -> None:
         eng = self.sim.engine
@@ -390,6 +435,7 @@ class TrajectoryRunner:
         c = self.kraus_seg[it.slot]
         pool = c.pool([TrajectoryPoint(self.resolver, {0: picks[it.slot]})])[0]
         eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("kraus", it.slot), pool))
+        return index
 
     def prepare(self, reps: int):
         """Draws the mixtures of `reps` trajectories; returns (picks, pools):
@@ -500,7 +546,7 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                 proj[i] = slot_program(sim, it.op.qubits, runner.qubits)
         # one-slot programs of the classically controlled unitaries
         for i, it in enumerate(body):
-            if isinstance(it, Conditional):
+            if isinstance(it, Conditional) and it.kind == "program":
                 proj[i] = slot_program(sim, it.inner.qubits, runner.qubits)
         states = eng.alloc((8 << n) * chunk)
         records: list = [dict() for _ in range(reps)]
@@ -538,13 +584,21 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                         eng.run_points(states, n, k, c.plan, pool_dev, plen)
                         eng.sync()
                         pool_dev.free()
-                    elif isinstance(it, Conditional):
+                    elif isinstance(it, Conditional) and it.kind == "program":
                         u = cirq.unitary(it.inner)
                         eye = np.eye(u.shape[0], dtype=np.complex128)
                         hold = [conditions_hold(it.op, records[start + r], measured) for r in range(k)]
                         if any(hold):
                             run_slot(proj[j], np.array([u if h else eye for h in hold]), k, start)
-                    elif isinstance(it, Channel):
+                    elif isinstance(it, (Channel, Conditional)):
+                        # a Kraus draw per trajectory; a classically controlled
+                        # channel draws only where its conditions hold
+                        hold = None
+                        if isinstance(it, Conditional):
+                            hold = np.array([conditions_hold(it.op, records[start + r], measured) for r in range(k)])
+                            if not hold.any():
+                                continue
+                            it = Channel(it.inner, it.slot)
                         ks = runner._kraus[it.slot]
                         rho = runner.channel_rdm(states, n, k, it.op)  # (k, d, d)
                         kk = np.array([K.conj().T @ K for K in ks])  # (nK, d, d)
@@ -558,7 +612,13 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
                         idx = np.where(bad, np.argmax(w, axis=1), idx)
                         wsel = w[np.arange(k), idx]
                         mats_k = np.array([ks[a] / np.sqrt(b) for a, b in zip(idx, wsel)])
+                        if hold is not None:
+                            mats_k[~hold] = np.eye(mats_k.shape[1])
                         run_slot(runner.kraus_seg[it.slot], mats_k, k, start)
+                        if it.key is not None:
+                            measured.setdefault(it.key, []).append(None)
+                            for r in range(k):
+                                records[start + r].setdefault(it.key, []).append([int(idx[r])])
                     else:  # mid-circuit measurement
                         op = it.op
                         qm = list(op.qubits)

@@ -362,3 +362,30 @@ def test_classical_control_in_simulate_and_moment_steps():
         want2 = np.zeros(8)
         want2[(a2 << 2) | (a2 << 1) | (c2 ^ (c2 & a2))] = 1
         np.testing.assert_allclose(np.abs(last.state_vector()) ** 2, want2, atol=1e-5)
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_keyed_and_classically_controlled_channels(dm):
+    """Amplitude damping (gamma 0.4) of |1>, keyed: the state-vector record
+    is 1 exactly when the decay operator acted (then q0 reads 0); the
+    density-matrix simulator records nothing.  A damping channel controlled
+    by a fair coin `a` acts only where a == 1."""
+    q0, q1, q2 = cirq.LineQubit.range(3)
+    kc = cirq.KrausChannel(cirq.kraus(cirq.amplitude_damp(0.4)), key="k")
+    c = cirq.Circuit(
+        [cirq.X(q0), cirq.X(q1), cirq.H(q2), kc.on(q0), cirq.measure(q2, key="a"),
+         cirq.amplitude_damp(0.4).on(q1).with_classical_controls("a"), cirq.measure(q0, q1, key="m")],
+        strategy=cirq.InsertStrategy.NEW,
+    )
+    sim = (cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator)(seed=5)
+    res = sim.run(c, repetitions=6000)
+    m = res.records["m"][:, 0, :].astype(int)
+    a = res.records["a"][:, 0, 0].astype(int)
+    assert abs(1 - m[:, 0].mean() - 0.4) < 0.03
+    assert abs(1 - m[a == 1, 1].mean() - 0.4) < 0.04
+    assert np.all(m[a == 0, 1] == 1)
+    if dm:
+        assert "k" not in res.records
+    else:
+        k = res.records["k"][:, 0, 0].astype(int)
+        np.testing.assert_array_equal(k, 1 - m[:, 0])

@@ -281,3 +281,78 @@ def test_complex128_array_initial_states_are_cast_as_the_reference(emu):
     u = cirq.Circuit(cirq.H(q[0]), cirq.CNOT(*q))
     np.testing.assert_allclose(cirq_gb300.Simulator().simulate(u, initial_state=vec).final_state_vector,
                                cirq.Simulator().simulate(u, initial_state=vec).final_state_vector, atol=1e-5)
+
+
+@pytest.mark.parametrize("dm", [False, True])
+@pytest.mark.parametrize("inner", ["damp", "depolarize", "reset", "reset_then_use"])
+def test_classical_control_of_non_unitary_operations(emu, dm, inner):
+    """Channels, mixtures and resets under classical control: applied in a
+    repetition only when the condition holds there."""
+    q0, q1, q2 = cirq.LineQubit.range(3)
+    body = {
+        "damp": cirq.amplitude_damp(0.6).on(q1),
+        "depolarize": cirq.depolarize(0.5).on(q1),
+        "reset": cirq.reset(q1),
+        "reset_then_use": cirq.reset(q1),
+    }[inner]
+    ops = [cirq.H(q0), cirq.X(q1), cirq.ry(0.7).on(q2), cirq.measure(q0, key="a"),
+           body.with_classical_controls("a"), cirq.H(q2)]
+    if inner == "reset_then_use":
+        ops += [cirq.measure(q1, key="c"), cirq.X(q2).with_classical_controls("c"), cirq.measure(q2, key="d")]
+    ops.append(cirq.measure(q1, q2, key="m"))
+    c = cirq.Circuit(ops, strategy=cirq.InsertStrategy.NEW)
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    reps = 1500
+    want = ref_cls(seed=1).run(c, repetitions=reps)
+    got = ours_cls(seed=2).run(c, repetitions=reps)
+    assert set(got.records) == set(want.records)
+    for key in want.records:
+        assert got.records[key].shape == want.records[key].shape, key
+        assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, key
+    joint_w = _outcome_codes(want, "a") * 4 + _outcome_codes(want, "m")
+    joint_g = _outcome_codes(got, "a") * 4 + _outcome_codes(got, "m")
+    assert _two_sample_p(joint_w, joint_g) > 1e-3
+
+
+@pytest.mark.parametrize("dm", [False, True])
+@pytest.mark.parametrize("case", ["kraus", "mixture", "control", "two_qubit"])
+def test_keyed_channels_match_the_reference(emu, dm, case):
+    """Channels with a measurement key: the state-vector simulator records
+    the index of the operator that acted (and conditions may read it); the
+    density-matrix simulator applies the channel and records nothing."""
+    q0, q1 = cirq.LineQubit.range(2)
+    kc = cirq.KrausChannel(cirq.kraus(cirq.amplitude_damp(0.4)), key="k")
+    mc = cirq.MixedUnitaryChannel([(0.3, np.eye(2)), (0.7, cirq.unitary(cirq.X))], key="k")
+    ops = [cirq.X(q0), cirq.H(q1)]
+    if case == "kraus":
+        ops.append(kc.on(q0))
+    elif case == "mixture":
+        ops.append(mc.on(q0))
+    elif case == "control":
+        ops += [kc.on(q0), cirq.X(q1).with_classical_controls("k")]
+    else:
+        mix = cirq.mixture(cirq.asymmetric_depolarize(error_probabilities={"XZ": 0.3, "YY": 0.2}))
+        ops.append(cirq.MixedUnitaryChannel(mix, key="k").on(q0, q1))
+    ops.append(cirq.measure(q0, q1, key="m"))
+    c = cirq.Circuit(ops, strategy=cirq.InsertStrategy.NEW)
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    if dm and case == "control":
+        with pytest.raises(ValueError, match="missing"):
+            ref_cls().run(c, repetitions=5)
+        with pytest.raises(ValueError, match="missing"):
+            ours_cls().run(c, repetitions=5)
+        return
+    reps = 1500
+    want = ref_cls(seed=1).run(c, repetitions=reps)
+    got = ours_cls(seed=2).run(c, repetitions=reps)
+    assert set(got.records) == set(want.records)
+    for key in want.records:
+        assert got.records[key].shape == want.records[key].shape, key
+        assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, key
+    if not dm:
+        joint_w = _outcome_codes(want, "k") * 4 + _outcome_codes(want, "m")
+        joint_g = _outcome_codes(got, "k") * 4 + _outcome_codes(got, "m")
+        assert _two_sample_p(joint_w, joint_g) > 1e-3
+        assert set(cirq_gb300.Simulator(seed=3).simulate(c).measurements) == {"k", "m"}

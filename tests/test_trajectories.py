@@ -91,15 +91,17 @@ def test_classical_control_becomes_a_conditional_item():
     kinds = [type(it).__name__ for it in items]
     assert kinds == ["Segment", "Measure", "Conditional", "Segment"]
     assert items[2].inner == cirq.X(q[1])
-    # a controlled channel has no unitary to apply per trajectory
-    bad = flatten_ops(cirq.Circuit(cirq.measure(q[0], key="a"),
-                                   cirq.amplitude_damp(0.1).on(q[1]).with_classical_controls("a")))
-    try:
-        tj.build_items(bad, dm=False)
-    except tj.UnsupportedOperation:
-        pass
-    else:
-        raise AssertionError("expected UnsupportedOperation")
+    assert items[2].kind == "program"
+    # a controlled channel: a Kraus draw in its own slot on the state-vector
+    # simulator, a compiled superoperator on the density-matrix simulator
+    noisy = flatten_ops(cirq.Circuit(cirq.measure(q[0], key="a"),
+                                     cirq.amplitude_damp(0.1).on(q[1]).with_classical_controls("a")))
+    items, nslot = tj.build_items(noisy, dm=False)
+    assert [(type(it).__name__, getattr(it, "kind", None)) for it in items] == [
+        ("Measure", None), ("Conditional", "channel")]
+    assert nslot == 1 and items[1].slot == 0
+    items, _ = tj.build_items(noisy, dm=True)
+    assert items[1].kind == "program"
 
 
 def test_conditions_resolve_like_the_reference():
