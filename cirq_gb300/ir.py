@@ -89,8 +89,20 @@ def flatten_ops(circuit) -> list:
     ops = []
     for moment in circuit:
         for op in moment:
-            if isinstance(op.untagged, cirq.CircuitOperation):
-                ops.extend(flatten_ops(op.untagged.mapped_circuit(deep=True)))
+            if is_loop(op):
+                ops.append(op)  # repeats a data-dependent number of times: a trajectory event
+            elif isinstance(op.untagged, cirq.CircuitOperation):
+                # one level at a time, so loops nested inside stay whole
+                ops.extend(flatten_ops(op.untagged.mapped_circuit(deep=False)))
+            elif _decomposed_measurement(op):
+                # e.g. PauliMeasurementGate: the reference acts on its
+                # decomposition (basis change, parity, a plain measurement,
+                # and back)
+                sub = cirq.decompose_once(op, default=None)
+                if sub is None:
+                    ops.append(op)
+                else:
+                    ops.extend(flatten_ops(cirq.Circuit(sub)))
             elif _wide_unitary(op):
                 ops.extend(
                     cirq.decompose(op, keep=lambda o: len(o.qubits) <= MAX_OP_QUBITS, on_stuck_raise=None)
@@ -122,6 +134,27 @@ def is_measurement_op(op) -> bool:
     return cirq.is_measurement(op) and not is_keyed_channel(op)
 
 
+def is_loop(op) -> bool:
+    """A CircuitOperation with ``repeat_until``: its body runs until the
+    condition holds on the measurement results
+    (cirq-core/cirq/circuits/circuit_operation.py ``_act_on_``)."""
+    cirq = _cirq()
+    u = op.untagged
+    return isinstance(u, cirq.CircuitOperation) and u.repeat_until is not None
+
+
+def _decomposed_measurement(op) -> bool:
+    """A measurement other than a MeasurementGate or a keyed channel."""
+    cirq = _cirq()
+    gate = getattr(op, "gate", None)
+    if gate is not None and isinstance(gate, (cirq.MeasurementGate, cirq.EigenGate, cirq.PhasedXZGate,
+                                               cirq.MatrixGate, cirq.PhasedXPowGate)):
+        return False
+    if isinstance(op.untagged, (cirq.ClassicallyControlledOperation, cirq.CircuitOperation)):
+        return False
+    return cirq.is_measurement(op) and not is_keyed_channel(op)
+
+
 def is_keyed_channel(op) -> bool:
     """A mixture or Kraus channel with a measurement key: the state-vector
     simulator records the index of the operator that acted
@@ -131,9 +164,13 @@ def is_keyed_channel(op) -> bool:
     cirq = _cirq()
     if isinstance(getattr(op, "gate", None), cirq.MeasurementGate):
         return False
-    if isinstance(op.untagged, cirq.ClassicallyControlledOperation):
+    if isinstance(op.untagged, (cirq.ClassicallyControlledOperation, cirq.CircuitOperation)):
         return False
-    return cirq.is_measurement(op) and (cirq.has_mixture(op) or cirq.has_kraus(op))
+    if not cirq.is_measurement(op):
+        return False
+    # operators of its own (has_kraus would also answer through a
+    # decomposition, as for PauliMeasurementGate)
+    return cirq.mixture(op, default=None) is not None or cirq.kraus(op, default=None) is not None
 
 
 def _needs_decomposition(op) -> bool:

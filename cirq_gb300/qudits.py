@@ -187,7 +187,9 @@ class Embedding:
             conds = untagged.classical_controls
             return [e.with_classical_controls(*conds) for e in self.op(untagged.without_classical_controls())]
         if isinstance(untagged, cirq.CircuitOperation):
-            return [e for sub in untagged.mapped_circuit(deep=True).all_operations() for e in self.op(sub)]
+            if untagged.repeat_until is not None:
+                raise NotImplementedError(f"repeat-until loops over qudits are not supported: {op!r}")
+            return [e for sub in untagged.mapped_circuit(deep=False).all_operations() for e in self.op(sub)]
         gate = getattr(op, "gate", None)
         bits = self.bits(op.qubits)
         if isinstance(gate, cirq.MeasurementGate):

@@ -75,6 +75,26 @@ def _check_all_resolved(program, resolver) -> None:
         )
 
 
+def _symbolic_repetitions(program) -> bool:
+    """Does a CircuitOperation of `program` repeat a symbolic number of
+    times?  Its structure is then known only per sweep point."""
+    for op in program.all_operations():
+        u = op.untagged
+        if isinstance(u, cirq.ClassicallyControlledOperation):
+            u = u.without_classical_controls().untagged
+        if isinstance(u, cirq.CircuitOperation):
+            if cirq.is_parameterized(u.repetitions) or _symbolic_repetitions(u.circuit):
+                return True
+    return False
+
+
+def _per_point(program, params):
+    """(resolver, resolved program) per sweep point."""
+    for r in cirq.to_resolvers(params):
+        _check_all_resolved(program, r)
+        yield r, cirq.resolve_parameters(program, r)
+
+
 class _GpuSimulatorBase:
     """Shared machinery of the state-vector and density-matrix drop-ins."""
 
@@ -572,6 +592,8 @@ class _GpuSimulatorBase:
     def _run(self, circuit, param_resolver, repetitions) -> dict[str, np.ndarray]:
         param_resolver = param_resolver or cirq.ParamResolver({})
         _check_all_resolved(circuit, param_resolver)
+        if _symbolic_repetitions(circuit):
+            circuit = cirq.resolve_parameters(circuit, param_resolver)
         if self.noise is not cirq.NO_NOISE:
             return self._noiseless()._run(self._reference_noisy_circuit(circuit, "run"), param_resolver, repetitions)
         qubits = tuple(sorted(circuit.all_qubits()))
@@ -769,6 +791,10 @@ class Simulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.StateVectorTrialResult]:
+        if _symbolic_repetitions(program):
+            for r, resolved in _per_point(program, params):
+                yield from self.simulate_sweep_iter(resolved, r, qubit_order, initial_state)
+            return
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if self.noise is not cirq.NO_NOISE:
             yield from self._noiseless().simulate_sweep_iter(
@@ -825,6 +851,12 @@ class Simulator(
         """Mirrors Simulator.simulate_expectation_values_sweep_iter
         (cirq-core/cirq/sim/sparse_simulator.py:193-218): expectation values are
         evaluated on the device from the final state, which never leaves HBM."""
+        if _symbolic_repetitions(program):
+            for r, resolved in _per_point(program, params):
+                yield from self.simulate_expectation_values_sweep_iter(
+                    resolved, observables, r, qubit_order, initial_state, permit_terminal_measurements
+                )
+            return
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if not permit_terminal_measurements and program.are_any_measurements_terminal():
             raise ValueError(
@@ -934,6 +966,10 @@ class DensityMatrixSimulator(
         qubit_order: cirq.QubitOrderOrList = cirq.QubitOrder.DEFAULT,
         initial_state: Any = None,
     ) -> Iterator[cirq.DensityMatrixTrialResult]:
+        if _symbolic_repetitions(program):
+            for r, resolved in _per_point(program, params):
+                yield from self.simulate_sweep_iter(resolved, r, qubit_order, initial_state)
+            return
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if self.noise is not cirq.NO_NOISE:
             yield from self._noiseless().simulate_sweep_iter(
@@ -990,6 +1026,12 @@ class DensityMatrixSimulator(
         """Mirrors DensityMatrixSimulator.simulate_expectation_values_sweep_iter
         (cirq-core/cirq/sim/density_matrix_simulator.py:204-236): Tr(P rho)
         is evaluated on the device."""
+        if _symbolic_repetitions(program):
+            for r, resolved in _per_point(program, params):
+                yield from self.simulate_expectation_values_sweep_iter(
+                    resolved, observables, r, qubit_order, initial_state, permit_terminal_measurements
+                )
+            return
         initial_state, qubit_order = self._unwrap_initial_state(initial_state, qubit_order)
         if not permit_terminal_measurements and program.are_any_measurements_terminal():
             raise ValueError(

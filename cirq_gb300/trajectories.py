@@ -38,7 +38,7 @@ from typing import Any
 import numpy as np
 
 from cirq_gb300._cirq_env import ensure_cirq
-from cirq_gb300.ir import UnsupportedOperation, flatten_ops, is_keyed_channel
+from cirq_gb300.ir import UnsupportedOperation, flatten_ops, is_keyed_channel, is_loop
 from cirq_gb300.program import Slot, TrajectoryPoint
 from cirq_gb300.qudits import record_qids
 
@@ -71,6 +71,24 @@ class Channel:
 
 
 @dataclasses.dataclass
+class Loop:
+    """A CircuitOperation with ``repeat_until``: in each trajectory its body
+    runs, then its condition is resolved on that trajectory's records, until
+    it holds (``CircuitOperation._act_on_``,
+    cirq-core/cirq/circuits/circuit_operation.py)."""
+
+    op: Any  # the CircuitOperation (untagged)
+
+    def body(self):
+        return self.op.replace(repeat_until=None).mapped_circuit(deep=False)
+
+    def condition(self):
+        # the condition with the operation's key mapping and path applied
+        mapped = getattr(self.op, "_mapped_repeat_until", None)
+        return mapped if mapped is not None else self.op.repeat_until
+
+
+@dataclasses.dataclass
 class Conditional:
     """A classically controlled operation: applied in a trajectory when all
     of its conditions hold on that trajectory's records so far
@@ -91,6 +109,17 @@ def is_classically_controlled(op) -> bool:
     return isinstance(op.untagged, cirq.ClassicallyControlledOperation)
 
 
+def _store(records: dict, measured: dict):
+    """A ClassicalDataDictionaryStore of one trajectory's records."""
+    channel = {k for k, v in measured.items() if v and v[0] is None}  # keyed channels' records
+    keyed = {cirq.MeasurementKey.parse_serialized(k): [tuple(int(b) for b in bits) for bits in v]
+             for k, v in records.items() if k not in channel}
+    chans = {cirq.MeasurementKey.parse_serialized(k): [int(v[0]) for v in records[k]] for k in channel}
+    qubits = {cirq.MeasurementKey.parse_serialized(k): [tuple(q) for q in v] for k, v in measured.items()
+              if k not in channel}
+    return cirq.ClassicalDataDictionaryStore(_records=keyed, _measured_qubits=qubits, _channel_records=chans)
+
+
 def conditions_hold(op, records: dict, measured: dict) -> bool:
     """Evaluates a ClassicallyControlledOperation's conditions with the
     reference's own Condition.resolve (cirq-core/cirq/value/condition.py)
@@ -99,13 +128,7 @@ def conditions_hold(op, records: dict, measured: dict) -> bool:
     (None for a keyed channel's record, [operator index]).
     A condition on a key not measured yet raises ValueError, as the
     reference does."""
-    channel = {k for k, v in measured.items() if v and v[0] is None}  # keyed channels' records
-    keyed = {cirq.MeasurementKey.parse_serialized(k): [tuple(int(b) for b in bits) for bits in v]
-             for k, v in records.items() if k not in channel}
-    chans = {cirq.MeasurementKey.parse_serialized(k): [int(v[0]) for v in records[k]] for k in channel}
-    qubits = {cirq.MeasurementKey.parse_serialized(k): [tuple(q) for q in v] for k, v in measured.items()
-              if k not in channel}
-    store = cirq.ClassicalDataDictionaryStore(_records=keyed, _measured_qubits=qubits, _channel_records=chans)
+    store = _store(records, measured)
     return all(c.resolve(store) for c in op.classical_controls)
 
 
@@ -116,7 +139,7 @@ def needs_trajectories(ops, dm: bool) -> bool:
     unitary_families = (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)
     seen_measure = False
     for op in ops:
-        if is_classically_controlled(op):
+        if is_classically_controlled(op) or is_loop(op):
             return True
         if is_measurement_op(op):
             seen_measure = True
@@ -145,6 +168,10 @@ def build_items(ops, dm: bool) -> tuple[list, int]:
         cur, cur_slots = [], []
 
     for op in ops:
+        if is_loop(op):
+            flush()
+            items.append(Loop(op.untagged))
+            continue
         if is_classically_controlled(op):
             cc = op.untagged
             inner = cc.without_classical_controls()
@@ -269,6 +296,9 @@ class TrajectoryRunner:
                     if isinstance(it, Channel) or (isinstance(it, Conditional) and it.kind == "channel")]
         self.kraus_seg = {c.slot: slot_program(sim, c.op.qubits, self.qubits) for c in channels}
         self._kraus = {c.slot: [np.asarray(k, dtype=np.complex128) for k in cirq.kraus(c.op)] for c in channels}
+        # the bodies of repeat-until loops, each with a runner of its own
+        self._loops = {j: TrajectoryRunner(sim, flatten_ops(it.body()), self.qubits, resolver)
+                       for j, it in enumerate(self.items) if isinstance(it, Loop)}
         # device buffers reused by every trajectory: the state and one
         # matrix pool per segment / channel
         self._state = None
@@ -285,6 +315,8 @@ class TrajectoryRunner:
         return buf
 
     def close(self) -> None:
+        for sub in self._loops.values():
+            sub.close()
         for buf in self._pools.values():
             buf.free()
         self._pools.clear()
@@ -393,6 +425,14 @@ class TrajectoryRunner:
                     eng.run(state, c.nbits_dev, c.plan, self._pool_dev(("seg", j), pool))
             elif isinstance(it, Measure):
                 self._measure(state, it.op, records, measured)
+            elif isinstance(it, Loop):
+                sub = self._loops[j]
+                cond = it.condition()
+                while True:
+                    sub_picks, sub_pools = sub.prepare(1)
+                    sub.apply(state, sub_picks[0], sub_pools, 0, records, measured)
+                    if cond.resolve(_store(records, measured)):
+                        break
             elif isinstance(it, Conditional):
                 if not conditions_hold(it.op, records, measured):
                     continue
@@ -528,6 +568,8 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
     for i, it in enumerate(items):
         if isinstance(it, Measure) and i < last_unitary and len(it.op.qubits) > 5:
             return None
+        if isinstance(it, Loop):
+            return None  # a data-dependent number of iterations per trajectory
     terminal = [it.op for it in items[last_unitary + 1 :]]
     body = items[: last_unitary + 1]
     runner = TrajectoryRunner(sim, ops, qubits, resolver)

@@ -389,3 +389,24 @@ def test_keyed_and_classically_controlled_channels(dm):
     else:
         k = res.records["k"][:, 0, 0].astype(int)
         np.testing.assert_array_equal(k, 1 - m[:, 0])
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_repeat_until_loops_and_pauli_measurements(dm):
+    """A loop of H + measure until the outcome is 1 runs a geometric number
+    of times (mean 2); Pauli measurements of eigenstates are deterministic
+    (ZZ of |11> -> +1, X of |+> -> +1) and XZ of a Bell state is a fair coin."""
+    q0, q1, q2 = cirq.LineQubit.range(3)
+    loop = cirq.CircuitOperation(cirq.FrozenCircuit(cirq.H(q2), cirq.measure(q2, key="m")),
+                                 repeat_until=cirq.KeyCondition(cirq.MeasurementKey("m")), use_repetition_ids=False)
+    sim = (cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator)(seed=9)
+    rec = sim.run(cirq.Circuit(loop), repetitions=3000).records["m"][:, :, 0]
+    iters = np.argmax(rec == 1, axis=1) + 1
+    assert abs(iters.mean() - 2.0) < 0.12 and iters.min() == 1
+    pm = lambda obs, *qs: cirq.PauliMeasurementGate(cirq.DensePauliString(obs), key=obs).on(*qs)
+    c = cirq.Circuit(cirq.X(q0), cirq.X(q1), pm("ZZ", q0, q1), cirq.H(q2), pm("X", q2))
+    res = sim.run(c, repetitions=500)
+    assert not res.records["ZZ"].any() and not res.records["X"].any()
+    bell = cirq.Circuit(cirq.H(q0), cirq.CNOT(q0, q1), pm("XZ", q0, q1))
+    p = sim.run(bell, repetitions=4000).records["XZ"].mean()
+    assert abs(p - 0.5) < 0.03

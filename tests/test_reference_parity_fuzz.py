@@ -356,3 +356,79 @@ def test_keyed_channels_match_the_reference(emu, dm, case):
         joint_g = _outcome_codes(got, "k") * 4 + _outcome_codes(got, "m")
         assert _two_sample_p(joint_w, joint_g) > 1e-3
         assert set(cirq_gb300.Simulator(seed=3).simulate(c).measurements) == {"k", "m"}
+
+
+def _iterations(result, key):
+    """Loop iterations per repetition: instances up to the first 1 of `key`
+    (the loop stops there; later instances are the reference's padding)."""
+    rec = np.asarray(result.records[key])[:, :, 0]
+    return np.argmax(rec == 1, axis=1) + 1
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_repeat_until_loops_match_the_reference(emu, dm):
+    """CircuitOperation(repeat_until=...): the body repeats per repetition
+    until its condition holds (a geometric number of iterations here)."""
+    q0, q1 = cirq.LineQubit.range(2)
+    body = cirq.Circuit(cirq.ry(1.2).on(q0), cirq.measure(q0, key="m"), cirq.X(q1).with_classical_controls("m"))
+    loop = cirq.CircuitOperation(body.freeze(), repeat_until=cirq.KeyCondition(cirq.MeasurementKey("m")),
+                                 use_repetition_ids=False)
+    c = cirq.Circuit(cirq.X(q1), loop, cirq.measure(q1, key="z"))
+    ref_cls = cirq.DensityMatrixSimulator if dm else cirq.Simulator
+    ours_cls = cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator
+    want = ref_cls(seed=1).run(c, repetitions=800)
+    got = ours_cls(seed=2).run(c, repetitions=800)
+    assert _two_sample_p(_iterations(want, "m"), _iterations(got, "m")) > 1e-3
+    # the controlled X fires once (in the last iteration): z = 0 always
+    assert not got.records["z"].any() and not want.records["z"].any()
+
+
+@pytest.mark.parametrize("dm", [False, True])
+@pytest.mark.parametrize("obs", ["X", "XZ", "YY", "ZXZ"])
+def test_pauli_measurement_gates_match_the_reference(emu, dm, obs):
+    """PauliMeasurementGate acts through its decomposition.  The reference's
+    density-matrix simulator leaves a non-Hermitian matrix after a
+    multi-qubit Pauli measurement, so both simulators here are compared with
+    the reference's state-vector samples."""
+    q = cirq.LineQubit.range(len(obs))
+    pm = cirq.PauliMeasurementGate(cirq.DensePauliString(obs), key="p").on(*q)
+    c = cirq.Circuit(cirq.H(q[0]), *[cirq.CNOT(q[0], x) for x in q[1:]], cirq.ry(0.6).on(q[-1]), pm,
+                     cirq.rx(0.4).on(q[0]), cirq.measure(*q, key="f"))
+    want = cirq.Simulator(seed=1).run(c, repetitions=2000)
+    got = (cirq_gb300.DensityMatrixSimulator if dm else cirq_gb300.Simulator)(seed=2).run(c, repetitions=2000)
+    for key in ("p", "f"):
+        assert got.records[key].shape == want.records[key].shape
+        assert _two_sample_p(_outcome_codes(want, key), _outcome_codes(got, key)) > 1e-3, key
+
+
+@pytest.mark.parametrize("dm", [False, True])
+def test_symbolic_repetitions_and_nested_loops_match_the_reference(emu, dm):
+    q0, q1 = cirq.LineQubit.range(2)
+    rep = cirq.CircuitOperation(cirq.FrozenCircuit(cirq.rx(0.3).on(q0), cirq.CNOT(q0, q1))) ** sympy.Symbol("a")
+    c = cirq.Circuit(cirq.H(q1), rep)
+    sweep = cirq.Points("a", [0, 1, 3, 4])
+    ref = (cirq.DensityMatrixSimulator if dm else cirq.Simulator)(dtype=np.complex128)
+    ours = cirq_gb300.DensityMatrixSimulator() if dm else cirq_gb300.Simulator()
+    for w, g in zip(ref.simulate_sweep(c, sweep), ours.simulate_sweep(c, sweep)):
+        assert g.params == w.params
+        if dm:
+            np.testing.assert_allclose(g.final_density_matrix, w.final_density_matrix, atol=1e-5)
+        else:
+            np.testing.assert_allclose(g.final_state_vector, w.final_state_vector, atol=1e-5)
+    obs = [cirq.Z(q0) * cirq.X(q1)]
+    np.testing.assert_allclose(ours.simulate_expectation_values_sweep(c, obs, sweep),
+                               ref.simulate_expectation_values_sweep(c, obs, sweep), atol=1e-5)
+    # a repeat-until loop inside a repeated CircuitOperation (repetition ids)
+    inner = cirq.CircuitOperation(
+        cirq.FrozenCircuit(cirq.H(q0), cirq.measure(q0, key="inner")),
+        repeat_until=cirq.SympyCondition(sympy.Eq(sympy.Symbol("inner"), 0)),
+    )
+    outer = cirq.CircuitOperation(cirq.FrozenCircuit(inner, cirq.X(q0), cirq.measure(q0, key="outer")),
+                                  repetitions=2, use_repetition_ids=True)
+    circuit = cirq.Circuit(outer)
+    sim = cirq_gb300.DensityMatrixSimulator(seed=3) if dm else cirq_gb300.Simulator(seed=3)
+    got = sim.run(circuit, repetitions=200)
+    want = (cirq.DensityMatrixSimulator if dm else cirq.Simulator)(seed=4).run(circuit, repetitions=200)
+    assert set(got.records) == set(want.records) == {"0:inner", "1:inner", "0:outer", "1:outer"}
+    for key in ("0:outer", "1:outer"):
+        assert got.records[key].all() and want.records[key].all()
