@@ -49,8 +49,27 @@ def is_diagonal(m: np.ndarray) -> bool:
     return not np.any(off)
 
 
+_CIRQ = None
+
+
 def _cirq():
-    return ensure_cirq()
+    global _CIRQ
+    if _CIRQ is None:
+        _CIRQ = ensure_cirq()
+    return _CIRQ
+
+
+_PLAIN_GATES = None
+
+
+def _plain_gates():
+    """Gate families that are a unitary (or a measurement) by construction:
+    a plain GateOperation of one of them needs no flattening checks."""
+    global _PLAIN_GATES
+    if _PLAIN_GATES is None:
+        cirq = _cirq()
+        _PLAIN_GATES = (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)
+    return _PLAIN_GATES
 
 
 def _is_measurement(op) -> bool:
@@ -86,9 +105,15 @@ def flatten_ops(circuit) -> list:
     operations of at most 5 qubits; one without a decomposition is kept and
     rejected by the compiler."""
     cirq = _cirq()
+    plain, gate_op, meas = _plain_gates(), cirq.GateOperation, cirq.MeasurementGate
     ops = []
     for moment in circuit:
         for op in moment:
+            if type(op) is gate_op:
+                gate = op.gate
+                if isinstance(gate, meas) or (isinstance(gate, plain) and len(op.qubits) <= MAX_OP_QUBITS):
+                    ops.append(op)
+                    continue
             if is_loop(op):
                 ops.append(op)  # repeats a data-dependent number of times: a trajectory event
             elif isinstance(op.untagged, cirq.CircuitOperation):

@@ -78,7 +78,10 @@ def _check_all_resolved(program, resolver) -> None:
 def _symbolic_repetitions(program) -> bool:
     """Does a CircuitOperation of `program` repeat a symbolic number of
     times?  Its structure is then known only per sweep point."""
+    gate_op = cirq.GateOperation
     for op in program.all_operations():
+        if type(op) is gate_op:
+            continue
         u = op.untagged
         if isinstance(u, cirq.ClassicallyControlledOperation):
             u = u.without_classical_controls().untagged

@@ -137,8 +137,18 @@ def needs_trajectories(ops, dm: bool) -> bool:
     from cirq_gb300.ir import is_measurement_op
 
     unitary_families = (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)
+    gate_op, meas = cirq.GateOperation, cirq.MeasurementGate
     seen_measure = False
     for op in ops:
+        if type(op) is gate_op:
+            gate = op.gate
+            if isinstance(gate, meas):
+                seen_measure = True
+                continue
+            if isinstance(gate, unitary_families):
+                if seen_measure:
+                    return True  # an operation after a measurement
+                continue
         if is_classically_controlled(op) or is_loop(op):
             return True
         if is_measurement_op(op):
