@@ -37,6 +37,14 @@ cirq = ensure_cirq()
 DM_MAX_QUBITS = 14
 
 
+def _state_bits(qids) -> int:
+    """Index bits of a state over `qids` (a qid of dimension d > 2 takes
+    ceil(log2 d))."""
+    from cirq_gb300.qudits import bits_for
+
+    return sum(1 if q.dimension == 2 else bits_for(q.dimension) for q in qids)
+
+
 def _sv_sim(dtype, seed, noise=None):
     from cirq_gb300.simulator import Simulator
 
@@ -72,7 +80,7 @@ def sample(
     if noise_model == cirq.NO_NOISE:
         return _sv_sim(dtype, seed).run(program, param_resolver=param_resolver, repetitions=repetitions)
     dm = _dm_sim(dtype, seed, noise_model)
-    if len(program.all_qubits()) <= DM_MAX_QUBITS:
+    if _state_bits(program.all_qubits()) <= DM_MAX_QUBITS:
         return dm.run(program, param_resolver=param_resolver, repetitions=repetitions)
     # too wide for a density matrix: trajectories of the circuit with the
     # noise placed as the density-matrix simulator places it for run()

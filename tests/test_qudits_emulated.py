@@ -351,3 +351,18 @@ def test_qudit_fixtures_vs_reference_golden(emu):
     np.testing.assert_allclose(got, GOLD["qudit_sv_c128"], atol=1e-5)
     rho = cirq_gb300.DensityMatrixSimulator().simulate(mg._qudit_noisy_circuit(cirq)).final_density_matrix
     np.testing.assert_allclose(rho, GOLD["qudit_dm_c128"], atol=1e-5)
+
+
+def test_noisy_qudit_sample_counts_state_bits(emu):
+    """cirq.sample of a noisy circuit picks the density-matrix simulator by
+    state bits: 8 qutrits are 16 bits, beyond its 14, so they run as
+    trajectories (a density matrix would need 32 bits)."""
+    from cirq_gb300 import mux
+
+    q = cirq.LineQid.range(8, dimension=3)
+    assert mux._state_bits(q) == 16 and mux._state_bits(cirq.LineQubit.range(5)) == 5
+    c = cirq.Circuit(_Shift().on(x) for x in q) + cirq.measure(*q, key="z")
+    s = cirq_gb300.sample(c, repetitions=300, seed=2, noise=cirq.NO_NOISE)
+    assert s.records["z"].shape == (300, 1, 8) and s.records["z"].max() <= 2
+    shifted = (s.records["z"][:, 0, :] > 0).mean()
+    assert abs(shifted - 0.4) < 0.05
