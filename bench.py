@@ -494,6 +494,7 @@ def main():
     ap.add_argument("--tile-bits", type=int, default=12)
     ap.add_argument("--kmax", type=int, default=4)
     ap.add_argument("--budget", type=float, default=25.0)
+    ap.add_argument("--tensor-cores", type=int, default=0, help="plan tensor-core passes with this many MMA ops per pass")
     ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -522,7 +523,10 @@ def main():
 
     eng = Engine.get(local)
     circuit, ngates = build_workload(args.n, args.depth, args.seed)
-    planner = Planner(tile_bits=args.tile_bits, kmax=args.kmax, budget=args.budget)
+    if args.tensor_cores:
+        planner = Planner(tensor=True, budget=args.tensor_cores)
+    else:
+        planner = Planner(tile_bits=args.tile_bits, kmax=args.kmax, budget=args.budget)
     t0 = time.perf_counter()
     compiled = compile_plan(circuit, planner)
     plan_s = time.perf_counter() - t0

@@ -185,7 +185,7 @@ SIGNATURES = {
     "gbq_reduce_slots": [_P, _P, _I, _I64, _P],
     "gbq_sv_norm2": [_P, _P, _I, _P],
     "gbq_sv_scale": [_P, _P, _I, _F],
-    "gbq_sv_final_renormalize": [_P, _P, _I, _P],
+    "gbq_sv_final_renormalize": [_P, _P, _I, _P, _P],
     "gbq_sample": [_P, _P, _I, _I, _P, _I64, _P],
     "gbq_probabilities": [_P, _P, _I, _I, _P],
     "gbq_sv_expect_paulis": [_P, _P, _I, _P, _I, _P],
@@ -200,6 +200,9 @@ SIGNATURES = {
     "gbq_points_expect": [_P, _P, _I, _I, _P, _I, _P],
     "gbq_points_sample": [_P, _P, _I, _I, _P, _P],
     "gbq_points_rdm": [_P, _P, _I, _I, _I, _P, _P],
+    "gbq_sv64_set_basis": [_P, _P, _I, _U64],
+    "gbq_sv64_apply": [_P, _P, _I, _I, _P, _P],
+    "gbq_sv64_compare": [_P, _P, _P, _I, _P],
 }
 _RESTYPES = {"gbq_last_error": ctypes.c_char_p}
 

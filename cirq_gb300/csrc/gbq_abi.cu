@@ -368,15 +368,18 @@ static bool is_mma_pass(const gbq_pass& p, const gbq_op* ops) {
 }
 
 // Checks one pass (and fills the kernel arguments of its kind).
+// mma: 0 = CUDA-core pass (PassArgs), 1 = 11-bit tensor-core pass (MmaArgs),
+// 2 = pipelined 12-bit tensor-core pass (TcArgs).
 static int convert_pass(const gbq_pass& p, const gbq_op* ops, int nops, int nbits, bool dual, PassArgs& a,
-                        MmaArgs& ma, bool& mma) {
+                        MmaArgs& ma, TcArgs& ta, int& mma) {
   memset(&a, 0, sizeof(a));
   uint64_t inmask = 0;
   int rc = pass_geometry(p, nops, nbits, a.ti, inmask);
   if (rc) return rc;
-  mma = is_mma_pass(p, ops);
+  mma = is_mma_pass(p, ops) ? (p.L == GBQ_TC_TILE_BITS ? 2 : 1) : 0;
   if (mma) {
     if (dual) return arg_fail("pass: tensor-core passes run on one state only");
+    if (mma == 2) return build_tc_args(p, ops, nbits, a.ti, inmask, ta);
     return build_mma_args(p, ops, nbits, a.ti, inmask, ma);
   }
   LayoutState lay;
@@ -393,9 +396,10 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
   const bool dual = lam != nullptr;
   PassArgs a;
   MmaArgs ma;
+  TcArgs ta;
   for (int q = 0; q < npasses; ++q) {
-    bool mma = false;
-    int rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, mma);
+    int mma = 0;
+    int rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, ta, mma);
     if (rc) return rc;
     a.psi = psi;
     a.lam = lam;
@@ -409,7 +413,12 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
       if (rc) return rc;
       cudaEventRecord(ev.first, c->stream);
     }
-    if (mma) {
+    if (mma == 2) {
+      ta.psi = psi;
+      ta.ti.mats = mats;
+      ta.abort = c->d_abort;
+      rc = launch_tc_pass(c, ta);
+    } else if (mma == 1) {
       ma.psi = psi;
       ma.ti.mats = mats;
       ma.abort = c->d_abort;
@@ -659,13 +668,15 @@ int gbq_validate_program(int nbits, const gbq_pass* passes, int npasses, const g
   if (npasses < 0 || (npasses && (!passes || !ops))) return arg_fail("gbq_validate_program: null program");
   PassArgs* a = new PassArgs();
   MmaArgs* ma = new MmaArgs();
+  TcArgs* ta = new TcArgs();
   int rc = GBQ_OK;
   for (int q = 0; q < npasses && rc == GBQ_OK; ++q) {
-    bool mma = false;
-    rc = convert_pass(passes[q], ops, nops, nbits, dual != 0, *a, *ma, mma);
+    int mma = 0;
+    rc = convert_pass(passes[q], ops, nops, nbits, dual != 0, *a, *ma, *ta, mma);
   }
   delete a;
   delete ma;
+  delete ta;
   return rc;
 }
 
@@ -798,7 +809,7 @@ int gbq_sv_project(gbq_ctx* c, gbq_c64* state, int nbits, uint64_t mask, uint64_
   return do_project(c, reinterpret_cast<float2*>(state), nbits, mask, value, scale);
 }
 
-int gbq_sv_final_renormalize(gbq_ctx* c, gbq_c64* state, int nbits, int* applied) {
+int gbq_sv_final_renormalize(gbq_ctx* c, gbq_c64* state, int nbits, int* applied, double* norm_out) {
   CHECK_CTX(c);
   if (!state || nbits < 0 || nbits > 40) return arg_fail("gbq_sv_final_renormalize: bad arguments");
   if (applied) *applied = 0;
@@ -806,6 +817,7 @@ int gbq_sv_final_renormalize(gbq_ctx* c, gbq_c64* state, int nbits, int* applied
   int rc = gbq_sv_norm2(c, state, nbits, &n2);
   if (rc) return rc;
   const double norm = sqrt(n2);
+  if (norm_out) *norm_out = norm;
   const double tol = 3.4526698e-4;  // sqrt(float32 eps), the reference's threshold
   if (fabs(norm - 1.0) > tol || norm == 0.0) return GBQ_OK;
   const float inv = (float)(1.0 / norm);
@@ -978,9 +990,10 @@ int gbq_run_points(gbq_ctx* c, gbq_c64* states, int nbits, int npoints, const gb
   while ((1 << pbits) < npoints) ++pbits;
   PassArgs a;
   MmaArgs ma;
+  TcArgs ta;
   for (int q = 0; q < npasses; ++q) {
-    bool mma = false;
-    int rc = convert_pass(passes[q], ops, nops, nbits, false, a, ma, mma);
+    int mma = 0;
+    int rc = convert_pass(passes[q], ops, nops, nbits, false, a, ma, ta, mma);
     if (rc) return rc;
     if (mma) return arg_fail("gbq_run_points: tensor-core passes run on one state only");
     const int L = passes[q].L;

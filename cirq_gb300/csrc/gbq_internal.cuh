@@ -125,6 +125,37 @@ struct MmaArgs {
   MmaDiagDev diags[GBQ_MAX_OPS_PER_PASS];
 };
 
+// Pipelined tensor-core pass (gbq_tc.cu): 12-bit tiles, 4-bit MMA ops.
+struct TcOpDev {
+  int64_t mat;         // pool offset of the first matrix
+  uint16_t tnext[4];   // next layout's pair-index column of target bit p
+  uint16_t rnext[8];   // ... of row bit q (0..4: lanes, 5..6: warps, 7: half)
+  int8_t nsel;
+  int8_t selg[3];      // global bit of selector s
+  int16_t bslot;       // first B-operand slot in shared memory
+  int8_t ndiag;        // diagonal ops applied to this op's result
+  int8_t diag0;
+};
+
+struct TcDiagDev {
+  int64_t mat;
+  uint16_t trow[8];  // table-index bits contributed by row bit q of the MMA op
+  uint16_t ttgt[4];  // ... by target bit p
+  int8_t k;
+  int8_t dext[8];    // table bit j <- global bit dext[j] (-1: a tile bit)
+  int8_t pad[7];
+};
+
+struct TcArgs {
+  float2* psi;
+  int* abort;        // set to 1 when a wait gives up
+  TileInfo ti;
+  int32_t nops, ndiag, nmats, pad;
+  uint16_t lcol[GBQ_TC_TILE_BITS];  // first op's layout pair-index column of tile bit b
+  TcOpDev ops[GBQ_MAX_MMA_OPS];
+  TcDiagDev diags[GBQ_MAX_OPS_PER_PASS];
+};
+
 // Error plumbing (gbq_abi.cu).
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
@@ -165,6 +196,9 @@ int launch_pass_l13(Ctx* c, const PassArgs& a, bool dual);
 int build_mma_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInfo& ti, uint64_t inmask,
                    MmaArgs& A);
 int launch_mma_pass(Ctx* c, const MmaArgs& a);
+int build_tc_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInfo& ti, uint64_t inmask,
+                  TcArgs& A);
+int launch_tc_pass(Ctx* c, const TcArgs& a);
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
 int points_rdm(Ctx* c, const float2* states, int nbits, int npoints, int k, const int* g, double* d_out);
 int points_sample(Ctx* c, const float2* states, int nbits, int npoints, const double* d_u,

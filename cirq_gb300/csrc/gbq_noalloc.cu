@@ -1,9 +1,8 @@
 // Pauli-string expectation values for callers that must not allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while a stream is being
-// captured into a CUDA graph, services whose device memory is entirely owned
-// by a host framework's pool, or latency-critical loops where cudaMalloc's
-// implicit device synchronisation is not acceptable.  gbq_sv_expect_paulis
+// Some callers cannot call cudaMalloc: services whose device memory is
+// entirely owned by a host framework's pool, or latency-critical loops where
+// cudaMalloc's implicit device synchronisation is not acceptable.  gbq_sv_expect_paulis
 // needs scratch for the term list and per-block partial sums and takes it
 // from the context's lazily grown cudaMalloc buffer; the entry point below
 // computes the same values with its scratch in a fixed, file-scope device
@@ -30,7 +29,7 @@ namespace gbq {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)4 << 20;  // GBQ_NOALLOC_SCRATCH_BYTES
-constexpr int kNoAllocGrid = 256;                         // CTAs of the partial-sum pass
+constexpr int kNoAllocCtasPerSm = 4;                      // grid of the partial-sum pass
 constexpr int kNoAllocThreads = 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -38,9 +37,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
+int g_grid_cap[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (set up once).
-int scratch_address(void** out) {
+// Device address of the scratch array on the current device and the widest
+// grid of the partial-sum pass there (kNoAllocCtasPerSm per SM), both set up
+// once per device.
+int scratch_address(void** out, int* grid_cap) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -50,13 +52,27 @@ int scratch_address(void** out) {
   }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (!g_scratch_ptr[dev]) {
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(multiprocessors)");
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     g_scratch_ptr[dev] = p;
+    g_grid_cap[dev] = (sms > 0 ? sms : 1) * kNoAllocCtasPerSm;
   }
   *out = g_scratch_ptr[dev];
+  *grid_cap = g_grid_cap[dev];
   return GBQ_OK;
+}
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Scratch bytes of a call: [terms][partials: nterms x G x 2 doubles][out: nterms x 2 doubles],
+// each part 256-byte aligned.
+size_t scratch_need(int nterms, int G) {
+  return al256((size_t)nterms * sizeof(gbq_pauli)) + al256((size_t)nterms * G * 2 * sizeof(double)) +
+         al256((size_t)nterms * 2 * sizeof(double));
 }
 
 // Grid-stride variant of k_expect_partial: a fixed grid of G CTAs, CTA b
@@ -162,25 +178,23 @@ extern "C" int gbq_sv_expect_paulis_noalloc(void* stream, const gbq_c64* state, 
       set_error("gbq_sv_expect_paulis_noalloc: pauli term acts on a qubit outside the state");
       return GBQ_ERR_ARG;
     }
+  void* base = nullptr;
+  int grid_cap = 0;
+  int rc = scratch_address(&base, &grid_cap);
+  if (rc) return rc;
   const uint64_t n = 1ull << nbits;
   uint64_t g64 = (n + kNoAllocThreads - 1) / kNoAllocThreads;
-  const int G = (int)(g64 < (uint64_t)kNoAllocGrid ? g64 : (uint64_t)kNoAllocGrid);
-  // scratch layout: [terms][partials: nterms x G x 2 doubles][out: nterms x 2 doubles]
-  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const size_t b_terms = al((size_t)nterms * sizeof(gbq_pauli));
-  const size_t b_part = al((size_t)nterms * G * 2 * sizeof(double));
-  const size_t b_out = al((size_t)nterms * 2 * sizeof(double));
-  if (b_terms + b_part + b_out > kNoAllocScratchBytes) {
+  const int G = (int)(g64 < (uint64_t)grid_cap ? g64 : (uint64_t)grid_cap);
+  if (scratch_need(nterms, G) > kNoAllocScratchBytes) {
+    int fit = (int)(kNoAllocScratchBytes / (sizeof(gbq_pauli) + (size_t)(G + 1) * 16));
+    while (fit > 0 && scratch_need(fit, G) > kNoAllocScratchBytes) --fit;
     set_error("gbq_sv_expect_paulis_noalloc: " + std::to_string(nterms) +
               " terms need more than the fixed " + std::to_string(kNoAllocScratchBytes >> 20) +
-              " MiB scratch (at most " +
-              std::to_string(kNoAllocScratchBytes / (sizeof(gbq_pauli) + (size_t)(G + 1) * 16)) +
-              " terms here); split the term list");
+              " MiB scratch (at most " + std::to_string(fit) + " terms fit for this state); split the term list");
     return GBQ_ERR_ARG;
   }
-  void* base = nullptr;
-  int rc = scratch_address(&base);
-  if (rc) return rc;
+  const size_t b_terms = al256((size_t)nterms * sizeof(gbq_pauli));
+  const size_t b_part = al256((size_t)nterms * G * 2 * sizeof(double));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   char* b = reinterpret_cast<char*>(base);
   gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(b);

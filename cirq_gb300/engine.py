@@ -264,10 +264,12 @@ class Engine:
         check(self.lib.gbq_sv_norm2(self.ctx, state.ptr, nbits, ctypes.byref(v)), "gbq_sv_norm2")
         return v.value
 
-    def final_renormalize(self, state: DeviceBuffer, nbits: int) -> bool:
+    def final_renormalize(self, state: DeviceBuffer, nbits: int) -> tuple[bool, float]:
+        """The final-state renormalisation rule on the device: (applied, norm before)."""
         v = ctypes.c_int()
-        check(self.lib.gbq_sv_final_renormalize(self.ctx, state.ptr, nbits, ctypes.byref(v)))
-        return bool(v.value)
+        nrm = ctypes.c_double()
+        check(self.lib.gbq_sv_final_renormalize(self.ctx, state.ptr, nbits, ctypes.byref(v), ctypes.byref(nrm)))
+        return bool(v.value), nrm.value
 
     def scale(self, state: DeviceBuffer, nbits: int, factor: float) -> None:
         check(self.lib.gbq_sv_scale(self.ctx, state.ptr, nbits, ctypes.c_float(factor)))

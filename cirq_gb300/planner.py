@@ -42,6 +42,10 @@ MAX_OPS = 32  # fused ops per pass; register layouts at most double the engine's
 MAX_DIAG_BITS = 8
 MAX_SEL = 3
 MIN_TILE_BITS = 10  # the engine's narrowest tile; narrower registers are padded
+TC_TILE_BITS = 12  # tensor-core passes: 12-bit tiles, 4-bit MMA blocks
+TC_K = 4
+TC_MAX_MMA_OPS = 8  # GBQ_MAX_MMA_OPS
+TC_MAX_MATS = 10  # GBQ_TC_MAX_MATS
 
 
 # ---------------------------------------------------------------- fused ops
@@ -403,17 +407,28 @@ class Planner:
         budget: float = 40.0,
         op_overhead: float = 2.0,
         use_registers: bool = True,
+        tensor: bool = False,
     ):
+        """``tensor=True`` plans tensor-core passes: 12-bit tiles whose fused
+        blocks are 4-bit MMA ops (tcgen05, three-term TF32 split) and whose
+        diagonal ops run in the MMA read-back; ``budget`` is then the number
+        of MMA ops a pass may hold (their cost does not depend on how many
+        gates a block absorbs).  A pass the tensor-core form cannot express
+        is emitted for the CUDA-core kernels instead."""
         if not 1 <= kmax <= 5:
             raise ValueError("fusion width kmax must be in 1..5")
         if not MIN_TILE_BITS <= tile_bits <= 13:
             raise ValueError(f"tile_bits must be in {MIN_TILE_BITS}..13")
+        if tensor:
+            tile_bits, kmax, low_bits = TC_TILE_BITS, TC_K, 5
+            budget = float(min(max(int(budget), 1), TC_MAX_MMA_OPS))
         self.tile_bits = tile_bits
         self.low_bits = low_bits
         self.kmax = kmax
         self.budget = budget
         self.ovh = op_overhead
         self.use_registers = use_registers
+        self.tensor = tensor
 
     # ------------------------------------------------------------------
     def plan(self, gates: Sequence[BitGate], nbits: int, batch: dict | None = None) -> Plan:
@@ -426,6 +441,11 @@ class Planner:
             batch = {i: g.matrix[None] for i, g in enumerate(gates)}
         L = min(self.tile_bits, nbits)
         m = min(self.low_bits, L)
+        # tensor-core passes take MMA selectors only when enough global bits
+        # stay outside the tile; otherwise a selector soon blocks a gate that
+        # needs its bit in the tile, and diagonal ops in the read-back are
+        # cheaper
+        self._tc_selectors = nbits - L >= 6
         remaining = list(range(len(gates)))
         pass_plans: list[PassPlan] = []
         while remaining:
@@ -443,6 +463,8 @@ class Planner:
         taken: list = []
         left: list = []
         budget = self.budget if nbits > L else float("inf")
+        if self.tensor:
+            budget += 0.5  # room for read-back diagonals beside the MMA ops
         for gi in remaining:
             g = gates[gi]
             bits = g.bits
@@ -454,6 +476,10 @@ class Planner:
             if ok and not g.diagonal:
                 need = [b for b in bits if b not in S]
                 if len(S) + len(need) > L:
+                    ok = False
+                elif self.tensor and need and any(
+                        b in op.sl for op in ops if op.kind == "dense" for b in need):
+                    # a selector of an MMA op must stay outside the tile
                     ok = False
             if ok:
                 plan = self._fusion_choice(g, gi, ops, last, S if g.diagonal else S | set(bits))
@@ -469,11 +495,16 @@ class Planner:
             self._apply_fusion(plan, g, gi, ops, last, batch)
             cost += delta
             taken.append(gi)
-        # fill the tile to exactly L bits
-        b = 0
-        while len(S) < L:
-            if b not in S:
+        # fill the tile to exactly L bits (an MMA op's selectors stay outside)
+        sels = {s for op in ops if op.kind == "dense" for s in op.sl} if self.tensor else set()
+        for b in range(nbits):
+            if len(S) >= L:
+                break
+            if b not in S and b not in sels:
                 S.add(b)
+        b = 0
+        while len(S) < L:  # (the pass then runs on the CUDA cores)
+            S.add(b)
             b += 1
         hi = sorted(x for x in S if x >= m)
         # selectors/diag bits that ended up inside S are fine: codes are resolved at emit
@@ -485,6 +516,8 @@ class Planner:
         bits = list(g.bits)
         if g.probe >= 0:
             return ((1 if g.diagonal else 2 ** len(bits)) + self.ovh, "new_probe")
+        if self.tensor:
+            return self._fusion_choice_tc(g, ops, last, S)
         c = max((last.get(b, -1) for b in bits), default=-1)
         new_cost = (2 ** len(bits) if not g.diagonal else 1) + self.ovh
         if not g.diagonal:
@@ -558,6 +591,74 @@ class Planner:
         if best is not None and best[0] < new_cost:
             return best
         return (new_cost, "new_diag")
+
+    def _fusion_choice_tc(self, g: BitGate, ops, last, S):
+        """Tensor-core pass costs: an MMA op costs 1 whatever it absorbs (it
+        is padded to 4 bits), a diagonal op in the read-back a little; MMA
+        selectors are global bits outside the tile only (a bit inside the
+        tile becomes a target)."""
+        bits = list(g.bits)
+        c = max((last.get(b, -1) for b in bits), default=-1)
+        # B operands in shared memory: 2^nsel matrices per MMA op, at most
+        # TC_MAX_MATS per pass
+        nmats = sum(2 ** len(op.sl) for op in ops if op.kind == "dense")
+        if not g.diagonal:
+            best = None
+            for d in range(max(c, 0), len(ops)):
+                op = ops[d]
+                if op.kind != "dense":
+                    continue
+                tg = set(op.tg) | set(bits)
+                if len(tg) > TC_K:
+                    continue
+                best = (0.0, "merge_dense", d)  # the latest op that fits
+            if best is not None:
+                return best
+            if c >= 0 and ops[c].kind == "diag":
+                op = ops[c]
+                loc = [b for b in op.bits if b in S]
+                glob = [b for b in op.bits if b not in S]
+                tg = set(loc) | set(bits)
+                sel_ok = not glob or getattr(self, "_tc_selectors", True)
+                if len(tg) <= TC_K and len(glob) <= MAX_SEL and nmats + 2 ** len(glob) <= TC_MAX_MATS and sel_ok:
+                    return (1.0 - 0.02, "diag_to_dense", c, loc, glob)
+            if nmats + 1 > TC_MAX_MATS:
+                return (float("inf"), "new_dense")
+            return (1.0, "new_dense")
+        lo = max(c, 0)
+        best = None
+        for d in range(len(ops) - 1, lo - 1, -1):
+            op = ops[d]
+            if op.kind == "probe":
+                continue
+            if op.kind == "dense":
+                grow_t, grow_s = [], []
+                for b in bits:
+                    if b in op.tg or b in op.sl:
+                        continue
+                    if b in S:
+                        grow_t.append(b)
+                    else:
+                        grow_s.append(b)
+                if len(op.tg) + len(grow_t) > TC_K or len(op.sl) + len(grow_s) > MAX_SEL:
+                    continue
+                if grow_s and not getattr(self, "_tc_selectors", True):
+                    continue
+                if grow_s and nmats + 2 ** len(op.sl) * (2 ** len(grow_s) - 1) > TC_MAX_MATS:
+                    continue
+                cand = (0.0, "absorb_dense", d, grow_t, grow_s)
+            else:
+                ub = list(op.bits) + [b for b in bits if b not in op.bits]
+                if len(ub) > MAX_DIAG_BITS:
+                    continue
+                cand = (0.0, "absorb_diag", d)
+            if best is None or (cand[1] == "absorb_dense" and best[1] != "absorb_dense"):
+                best = cand
+            if best[1] == "absorb_dense":
+                break
+        if best is not None:
+            return best
+        return (0.02, "new_diag")
 
     def _apply_fusion(self, plan, g: BitGate, gi: int, ops, last, batch):
         action = plan[1]
@@ -748,8 +849,54 @@ class Planner:
         return items
 
     # ---- emission -----------------------------------------------------------
+    def _tc_items(self, pp: PassPlan):
+        """The items of a tensor-core pass (("mma", op) and diagonal ("op",
+        op, False) in execution order; each diagonal runs in the read-back of
+        the MMA op before it), or None when the pass cannot take that form:
+        no dense op, probes, a matrix budget overrun, or a leading diagonal
+        on a bit the first MMA op targets (it must act before that op).
+        Dense ops are padded to 4 targets with identity bits."""
+        if pp.L != TC_TILE_BITS or pp.m < 5:
+            return None
+        tile = set(range(pp.m)) | set(pp.hi)
+        ops = list(pp.ops)
+        if any(op.kind == "probe" for op in ops):
+            return None
+        dense = [i for i, op in enumerate(ops) if op.kind == "dense"]
+        if not dense or len(dense) > TC_MAX_MMA_OPS:
+            return None
+        first = dense[0]
+        for d in ops[:first]:  # diagonals commute with an op that does not target their bits
+            if set(d.bits) & set(ops[first].tg):
+                return None
+        order = [ops[first]] + ops[:first] + ops[first + 1:]
+        nmats = 0
+        for op in order:
+            if op.kind == "dense":
+                if len(op.tg) > TC_K or any(b in tile for b in op.sl):
+                    return None
+                nmats += 2 ** len(op.sl)
+        if nmats > TC_MAX_MATS:
+            return None
+        items = []
+        for op in order:
+            if op.kind != "dense":
+                items.append(("op", op, False))
+                continue
+            if len(op.tg) < TC_K:
+                pad = [b for b in sorted(tile, reverse=True) if b not in op.tg][: TC_K - len(op.tg)]
+                step = ("tx", len(pad))
+                op.M = _Replayer.dense_step(op.M, step, {})
+                op.recipe.append(step)
+                op.tg.extend(pad)
+            items.append(("mma", op))
+        return items
+
     def _emit(self, pass_plans, nbits, ngates) -> Plan:
-        phased = [self._phases(pp) for pp in pass_plans]
+        phased = []
+        for pp in pass_plans:
+            items = self._tc_items(pp) if self.tensor else None
+            phased.append(items if items is not None else self._phases(pp))
         passes = np.zeros(len(pass_plans), dtype=_lib.PASS_DTYPE)
         nops = sum(len(items) for items in phased)
         ops = np.zeros(nops, dtype=_lib.OP_DTYPE)
@@ -780,6 +927,19 @@ class Planner:
                     r["kind"] = _lib.OP_LAYOUT
                     r["k"] = len(rb_cur)
                     r["bits"][: len(rb_cur)] = [tile_of[b] for b in rb_cur]
+                    continue
+                if item[0] == "mma":
+                    op = item[1]
+                    r["kind"] = _lib.OP_MMA
+                    r["k"] = TC_K
+                    r["nsel"] = len(op.sl)
+                    r["bits"][:TC_K] = [tile_of[b] for b in op.tg]
+                    r["sel"][: len(op.sl)] = [code(b) for b in op.sl]
+                    data = op.M[0].reshape(-1)
+                    layout.append(("dense", op.recipe, off, (op.M.shape[1], op.M.shape[2]), None))
+                    r["mat"] = off
+                    chunks.append(np.asarray(data).astype(np.complex64))
+                    off += len(data)
                     continue
                 _, op, reg = item
                 perm = None

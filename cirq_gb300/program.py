@@ -541,4 +541,4 @@ def structure_key(ops, qubits, dm, planner: Planner, noise_repr: str = "") -> An
     """A cache key for the compiled structure of an op list (parameter values of
     unparameterised gates are part of the structure)."""
     return (tuple(_op_key(op) for op in ops), tuple(qubits), dm, planner.tile_bits, planner.kmax, planner.budget,
-            noise_repr)
+            getattr(planner, "tensor", False), noise_repr)

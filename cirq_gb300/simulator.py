@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import collections
 import math
+import warnings
 from typing import Any, Iterator, Sequence
 
 import numpy as np
@@ -116,6 +117,8 @@ class _GpuSimulatorBase:
         pass_budget: float = 25.0,
         use_cuda_graphs: bool = False,
         autotune: bool = False,
+        tensor_cores: bool = False,
+        mma_ops_per_pass: int = 4,
     ):
         _check_dtype(dtype)
         self._use_graphs = use_cuda_graphs
@@ -126,7 +129,12 @@ class _GpuSimulatorBase:
         self._prng = cirq.value.parse_random_state(seed)
         self._split_untangled_states = split_untangled_states
         self._device = device
-        self.planner = Planner(tile_bits=tile_bits, kmax=fusion_max_qubits, budget=pass_budget)
+        if tensor_cores:
+            # 12-bit tiles, 4-bit blocks on the tensor cores (tcgen05, TF32
+            # three-term split); passes it cannot express run on the CUDA cores
+            self.planner = Planner(tensor=True, budget=mma_ops_per_pass)
+        else:
+            self.planner = Planner(tile_bits=tile_bits, kmax=fusion_max_qubits, budget=pass_budget)
         self._cache: collections.OrderedDict = collections.OrderedDict()
         self._slot_programs: dict = {}  # one-op trajectory programs (trajectories.slot_program)
         self._engine: Engine | None = None
@@ -715,6 +723,20 @@ def _confuse(bits, qubits, confusion_map, prng) -> None:
                 rep[k] = new_bits[i]
 
 
+def _final_renormalize(eng, state, n: int) -> None:
+    """Applies StateVectorTrialResult.final_state_vector's renormalisation rule
+    (cirq-core/cirq/sim/state_vector_simulator.py:131-146) on the device, with
+    the reference's warning when the norm is too far from 1 to renormalise."""
+    _, norm = eng.final_renormalize(state, n)
+    tol = float(np.sqrt(np.finfo(np.float32).eps))
+    if abs(norm - 1) > tol:
+        warnings.warn(
+            f"final state vector's norm={np.float32(norm)!r} is too far from 1,"
+            f" {abs(norm - 1)} > {tol}."
+            "skipping renormalization"
+        )
+
+
 def _state_vector_result(params, measurements, qubits, vec: np.ndarray):
     """Builds a genuine cirq.StateVectorTrialResult around `vec` without copying it."""
     shape = tuple(q.dimension for q in qubits)
@@ -820,7 +842,7 @@ class Simulator(
             for r in cirq.to_resolvers(params):
                 _check_all_resolved(program, r)
                 for runner, state, rec in self._traj_states(program, qubits, r, initial_state, 1):
-                    eng.final_renormalize(state, runner.n)
+                    _final_renormalize(eng, state, runner.n)
                     vec = eng.download_state(state, runner.n)
                     state.free()
                     meas = {k: np.array(v[-1], dtype=np.uint8) for k, v in rec.items()}
@@ -837,7 +859,7 @@ class Simulator(
         for p, r in enumerate(resolvers):
             state = self._evolve(compiled, pools[p], initial_state)
             measurements = self._measure_terminal(state, compiled, meas)
-            eng.final_renormalize(state, compiled.n)
+            _final_renormalize(eng, state, compiled.n)
             vec = eng.download_state(state, compiled.n)
             state.free()
             yield _state_vector_result(r, measurements, qubits, vec)

@@ -72,15 +72,21 @@ typedef struct gbq_ctx gbq_ctx;
 /* Tensor-core op: a 16 x 16 matrix on exactly 4 tile bits (bits[0..3]),
  * applied with tcgen05 MMAs in a three-term TF32 split (fp32-level
  * accuracy); selectors, if any, are global bit codes (< 0).  A pass that
- * holds an MMA op is a tensor-core pass: L = GBQ_MMA_TILE_BITS, m >= 1, its
- * first op is MMA, every other op is MMA or DIAG (a DIAG applies to the
- * result of the MMA op before it), at most GBQ_MAX_MMA_OPS MMA ops whose
- * matrices (2^nsel each) number at most GBQ_MAX_MMA_MATS; single-state runs
- * only (gbq_run, gbq_graph_create). */
+ * holds an MMA op is a tensor-core pass: its first op is MMA, every other op
+ * is MMA or DIAG (a DIAG applies to the result of the MMA op before it), at
+ * most GBQ_MAX_MMA_OPS MMA ops; single-state runs only (gbq_run,
+ * gbq_graph_create).  Two tile widths:
+ *   L = GBQ_MMA_TILE_BITS (11), m >= 1: one tile at a time per CTA, MMA
+ *     matrices (2^nsel each) at most GBQ_MAX_MMA_MATS per pass;
+ *   L = GBQ_TC_TILE_BITS (12), m >= 5: the pipelined pass (two tiles in
+ *     flight per CTA, loads, MMAs and read-backs overlapped), matrices at
+ *     most GBQ_TC_MAX_MATS per pass. */
 #define GBQ_OP_MMA 9
 #define GBQ_MMA_TILE_BITS 11
 #define GBQ_MAX_MMA_OPS 8
 #define GBQ_MAX_MMA_MATS 6
+#define GBQ_TC_TILE_BITS 12
+#define GBQ_TC_MAX_MATS 10
 
 #define GBQ_MAX_OPS_PER_PASS 64
 #define GBQ_MAX_TILE_BITS 13
@@ -211,9 +217,12 @@ int gbq_sv_project(gbq_ctx* ctx, gbq_c64* state, int nbits, uint64_t mask, uint6
 /* state *= scale (device, in place). */
 int gbq_sv_scale(gbq_ctx* ctx, gbq_c64* state, int nbits, float scale);
 /* Final-state renormalisation rule of state_vector_simulator.py:131-146,
- * evaluated on the device: renormalises in place only when that reduces the
- * round-off of the total probability.  *applied = 1 when it did. */
-int gbq_sv_final_renormalize(gbq_ctx* ctx, gbq_c64* state, int nbits, int* applied);
+ * evaluated on the device: renormalises in place only when the norm is
+ * within sqrt(float32 eps) of 1 and dividing by it reduces the round-off of
+ * the total probability.  *applied = 1 when it did; *norm (optional)
+ * receives the norm before the call (the reference warns when it is too far
+ * from 1). */
+int gbq_sv_final_renormalize(gbq_ctx* ctx, gbq_c64* state, int nbits, int* applied, double* norm);
 
 /* Inverse-CDF sampling of R basis indices from |psi|^2 (dm = 0) or from the
  * diagonal of a density matrix of nbits qubits (dm = 1).  u[r] in [0, 1) are
@@ -236,10 +245,9 @@ int gbq_sv_expect_paulis(gbq_ctx* ctx, const gbq_c64* state, int nbits, const gb
                          int nterms, double* out);
 /* Same values as gbq_sv_expect_paulis, for callers that cannot allocate
  * device memory (no counterpart in the reference: Cirq's simulators run in
- * host memory).  Such callers include code running while a stream is being
- * captured into a CUDA graph, services whose device memory belongs to a host
- * framework's pool, and loops that cannot afford cudaMalloc's implicit
- * device synchronisation.  This entry point allocates nothing: its scratch
+ * host memory).  Such callers include services whose device memory belongs
+ * to a host framework's pool, and loops that cannot afford cudaMalloc's
+ * implicit device synchronisation.  This entry point allocates nothing: its scratch
  * is a fixed GBQ_NOALLOC_SCRATCH_BYTES array in the library's device image,
  * present on every GPU that loads the library until the process exits, and
  * found with cudaGetSymbolAddress the first time it is called on a device --
@@ -247,12 +255,29 @@ int gbq_sv_expect_paulis(gbq_ctx* ctx, const gbq_c64* state, int nbits, const gb
  * array, `terms` and `out` are host arrays (2 doubles per term, as for
  * gbq_sv_expect_paulis); work is ordered on `stream` (a cudaStream_t, NULL
  * for the default stream) and the call returns after it finished.  Term lists
- * too long for the scratch (about 1000 terms) are rejected with GBQ_ERR_ARG.
+ * too long for the scratch (about 400 terms for states of 18 or more qubits on a
+ * 152-SM GPU, more for smaller states) are rejected with GBQ_ERR_ARG.
  * All calls share the scratch: calls that overlap on the GPU race and must
  * be serialised by the caller. */
 #define GBQ_NOALLOC_SCRATCH_BYTES (4u << 20)
 int gbq_sv_expect_paulis_noalloc(void* stream, const gbq_c64* state, int nbits,
                                  const gbq_pauli* terms, int nterms, double* out);
+/* Complex128 gate-by-gate passes (no counterpart in the reference's
+ * complex64 path; they restate linalg.targeted_left_multiply,
+ * cirq-core/cirq/linalg/transformations.py:105-172, in double precision,
+ * one gate per pass, no fusion, no tiles).  They evolve an independent
+ * double-precision copy of a circuit's state on the GPU, against which the
+ * complex64 tile passes are checked at widths the CPU oracle cannot reach.
+ * `state` is a device array of 2^nbits (re, im) double pairs (nbits <= 36). */
+int gbq_sv64_set_basis(gbq_ctx* ctx, void* state, int nbits, uint64_t index);
+/* Applies a 2^k x 2^k complex matrix (row-major (re, im) doubles, host
+ * array; matrix-index bit j <-> state index bit bits[j]) for 1 <= k <= 3. */
+int gbq_sv64_apply(gbq_ctx* ctx, void* state, int nbits, int k, const int32_t* bits,
+                   const double* matrix);
+/* out[0] = max_i |state64_i - state32_i|, out[1] = sum |state64_i|^2,
+ * out[2] = sum |state32_i|^2 (host array of 3 doubles). */
+int gbq_sv64_compare(gbq_ctx* ctx, const void* state64, const gbq_c64* state32, int nbits,
+                     double* out);
 /* Density-matrix counterpart: coef_t Tr(P_t rho) for rho of nbits qubits
  * (cirq-core/cirq/ops/pauli_string.py:734-760). */
 int gbq_dm_expect_paulis(gbq_ctx* ctx, const gbq_c64* rho, int nbits, const gbq_pauli* terms,

@@ -155,18 +155,18 @@ class EmuEngine:
     def download_state(self, state, nbits, pinned=True) -> np.ndarray:
         return np.asarray(_buf(state).arr[: 1 << nbits]).astype(np.complex64)
 
-    def final_renormalize(self, state, nbits) -> bool:
+    def final_renormalize(self, state, nbits) -> tuple[bool, float]:
         """gbq_sv_final_renormalize: the rule of state_vector_simulator.py:131-146
-        at complex64."""
+        at complex64; returns (applied, norm before)."""
         v = _buf(state).arr[: 1 << nbits].astype(np.complex64)
-        norm = np.linalg.norm(v)
+        norm = float(np.linalg.norm(v.astype(np.complex128)))
         if abs(norm - 1) > np.sqrt(np.finfo(np.float32).eps):
-            return False
-        vn = (v / norm).astype(np.complex64)
+            return False, norm
+        vn = (v / np.float32(norm)).astype(np.complex64)
         if abs(np.vdot(vn, vn) - 1) - abs(np.vdot(v, v) - 1) < 0:
             _buf(state).arr[: 1 << nbits] = vn
-            return True
-        return False
+            return True, norm
+        return False, norm
 
     def norm2(self, state, nbits) -> float:
         return float(np.sum(np.abs(_buf(state).arr[: 1 << nbits]) ** 2))

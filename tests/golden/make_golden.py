@@ -2,7 +2,9 @@
 
 Run from the repository root in a checkout that has the reference source:
 
-    python tests/golden/make_golden.py [/path/to/Cirq/cirq-core]
+    python tests/golden/make_golden.py /path/to/Cirq/cirq-core
+
+(or set ``CIRQ_REFERENCE_PATH`` to that directory instead of passing it).
 
 The reference's own simulators (``cirq.Simulator``,
 ``cirq.DensityMatrixSimulator``) and protocols produce every array stored
@@ -360,4 +362,7 @@ def _qudit_noisy_circuit(cirq):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/cirq-core")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CIRQ_REFERENCE_PATH")
+    if not ref:
+        sys.exit("usage: make_golden.py <path to the reference's cirq-core> (or set CIRQ_REFERENCE_PATH)")
+    main(ref)

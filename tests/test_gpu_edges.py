@@ -179,3 +179,95 @@ def test_invert_mask_and_confusion_map_orders(dm, where):
         np.testing.assert_array_equal(res.records["b"][:, 0, 0], res.records["a"][:, 0, 0])
     got = [int(sim.simulate(cirq.Circuit(ops[2])).measurements["a"][0]) for _ in range(300)]
     assert abs(np.mean(got) - 0.9) < 0.07
+
+
+@pytest.mark.parametrize("delta,renormalized", [(3e-3, False), (5e-4, False), (2e-4, True), (1e-5, True)])
+def test_device_final_renormalization_rule(delta, renormalized):
+    """gbq_sv_final_renormalize on states whose norm is 1 + delta, on both
+    sides of the reference's sqrt(eps) threshold
+    (cirq-core/cirq/sim/state_vector_simulator.py:131-146): beyond it the
+    state is returned unchanged (the reference warns and skips), within it
+    the state is divided by its norm because that reduces the round-off of
+    the total probability."""
+    import ctypes
+
+    from cirq_gb300 import _lib
+    from oracle.statevector import renormalize_like_cirq
+
+    n = 14
+    psi = simulate_state_vector(workloads.random_layer_circuit(n, 6, seed=77)).astype(np.complex64)
+    psi = (psi * np.float32(1 + delta)).astype(np.complex64)
+    eng = cirq_gb300.Simulator().engine
+    state = eng.upload(psi)
+    applied = ctypes.c_int(-1)
+    norm = ctypes.c_double()
+    _lib.check(eng.lib.gbq_sv_final_renormalize(eng.ctx, state.ptr, n, ctypes.byref(applied), ctypes.byref(norm)),
+               "renormalize")
+    assert abs(norm.value - np.linalg.norm(psi.astype(np.complex128))) < 1e-6
+    got = np.zeros_like(psi)
+    state.download(got)
+    want = renormalize_like_cirq(psi)
+    assert applied.value == int(renormalized)
+    assert np.array_equal(want, psi) == (not renormalized)  # the oracle takes the same branch
+    if renormalized:
+        np.testing.assert_allclose(got, psi / np.linalg.norm(psi.astype(np.complex128)), atol=1e-7)
+        assert abs(np.linalg.norm(got.astype(np.complex128)) - 1) < 1e-6
+    else:
+        np.testing.assert_array_equal(got, psi)
+
+
+def test_final_state_vector_of_an_unnormalized_initial_state():
+    """The public path: an initial state off by more than sqrt(eps) comes
+    back as simulated (no renormalisation), as in the reference."""
+    q = cirq.LineQubit.range(12)
+    c = workloads.random_layer_circuit(12, 3, seed=5)
+    init = np.zeros(2**12, dtype=np.complex64)
+    init[0] = 1.01
+    with pytest.warns(UserWarning, match="skipping renormalization"):
+        ref = cirq.Simulator(dtype=np.complex64).simulate(c, qubit_order=q, initial_state=init).final_state_vector
+    with pytest.warns(UserWarning, match="skipping renormalization"):
+        got = cirq_gb300.Simulator().simulate(c, qubit_order=q, initial_state=init).final_state_vector
+    np.testing.assert_allclose(got, ref, atol=1e-5)
+    assert abs(np.linalg.norm(got) - 1.01) < 1e-5
+
+
+def _two_halves(n_half, depth):
+    """Two independent random-layer registers of n_half qubits each."""
+    a = workloads.random_layer_circuit(n_half, depth, seed=81)
+    b = workloads.random_layer_circuit(n_half, depth, seed=82)
+    qb = {cirq.LineQubit(i): cirq.LineQubit(n_half + i) for i in range(n_half)}
+    return a, b.transform_qubits(lambda x: qb[x]), a + b.transform_qubits(lambda x: qb[x])
+
+
+def test_untangled_36_qubit_simulate_per_component_vs_oracle():
+    """simulate() of 36 qubits in two untangled 18-qubit halves (a 2^36 state
+    does not fit one GPU): each half is simulated alone and held in the
+    reference's product state (cirq-core/cirq/sim/simulation_product_state.py:31-181)."""
+    a, b, c = _two_halves(18, 6)
+    res = cirq_gb300.Simulator().simulate(c)
+    st = res._final_simulator_state
+    assert isinstance(st, cirq.SimulationProductState)
+    for half in (a, b):
+        q = sorted(half.all_qubits())
+        comp = st.sim_states[q[0]]
+        assert set(comp.qubits) == set(q)
+        got = comp.target_tensor.reshape(-1)
+        want = simulate_state_vector(half, qubit_order=list(comp.qubits))
+        assert np.max(np.abs(got - want)) < 1e-5
+
+
+def test_untangled_36_qubit_run_per_component_vs_oracle():
+    a, b, c = _two_halves(18, 6)
+    q = sorted(c.all_qubits())
+    reps = 4000
+    bits = cirq_gb300.Simulator(seed=4).run(c + cirq.measure(*q, key="m"), repetitions=reps).measurements["m"]
+    assert bits.shape == (reps, 36)
+    import scipy.stats
+
+    for off, half in ((0, a), (18, b)):
+        psi = simulate_state_vector(half, qubit_order=sorted(half.all_qubits()))
+        p = (np.abs(psi) ** 2).reshape((8, -1)).sum(axis=1)  # first three qubits of the half
+        idx = bits[:, off : off + 3].astype(int) @ np.array([4, 2, 1])
+        counts = np.bincount(idx, minlength=8)
+        keep = p * reps >= 5
+        assert scipy.stats.chisquare(counts[keep], p[keep] * counts[keep].sum() / p[keep].sum()).pvalue > 1e-4

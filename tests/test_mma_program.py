@@ -45,7 +45,7 @@ def _one_pass(bits=(0, 3, 7, 9), L=11, first_kind=_lib.OP_MMA, k=4, sel=()):
 @pytest.mark.parametrize(
     "kwargs,needle",
     [
-        (dict(L=12), "11-bit tiles"),
+        (dict(L=13), "11-bit tiles"),
         (dict(first_kind=_lib.OP_DIAG, k=2, bits=(0, 1)), "first op"),
         (dict(k=3, bits=(0, 3, 7)), "exactly 4"),
         (dict(bits=(0, 3, 3, 9)), "distinct"),
