@@ -206,6 +206,55 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
     return float(np.mean(times)), int(compiled.plan.pool.nbytes), int(vec_bytes)
 
 
+def e2e_phases(circuit, planner_kwargs, repeats: int = 2):
+    """Where the time of one Simulator.simulate() goes, step by step, with a
+    device synchronisation after each step (so the steps do not overlap):
+    compile (translation + planning; only on the first call, later calls hit
+    the compile cache), pool (the fused matrices of the point), passes (pool
+    upload, basis state and every tile pass), renormalise (the final-state
+    rule: a norm pass, and a scale pass when it applies), d2h (the state into
+    pinned host memory) and assemble (the cirq result object).  Returns
+    {"first": {...}, "cached": {...}} in seconds."""
+    cirq = _cirq()
+    import cirq_gb300
+    from cirq_gb300 import simulator as sim_mod
+
+    sim = cirq_gb300.Simulator(**planner_kwargs)
+    eng = sim.engine
+    out = {}
+    for rep in range(repeats + 1):
+        ph = {}
+        t = time.perf_counter()
+        qubits, resolvers, compiled, meas = sim._prepare(circuit, cirq.QubitOrder.DEFAULT, cirq.ParamResolver({}))
+        ph["compile"] = time.perf_counter() - t
+        t = time.perf_counter()
+        pool = compiled.pool(resolvers or [cirq.ParamResolver({})])
+        ph["pool"] = time.perf_counter() - t
+        t = time.perf_counter()
+        state = sim._evolve(compiled, pool[0], None)
+        eng.sync()
+        ph["passes"] = time.perf_counter() - t
+        t = time.perf_counter()
+        sim_mod._final_renormalize(eng, state, compiled.n)
+        eng.sync()
+        ph["renormalise"] = time.perf_counter() - t
+        t = time.perf_counter()
+        vec = eng.download_state(state, compiled.n)
+        ph["d2h"] = time.perf_counter() - t
+        state.free()
+        t = time.perf_counter()
+        res = sim_mod._state_vector_result(cirq.ParamResolver({}), {}, qubits, vec)
+        ph["assemble"] = time.perf_counter() - t
+        ph["total"] = sum(ph.values())
+        del res, vec
+        if rep == 0:
+            out["first"] = ph
+        else:
+            prev = out.get("cached")
+            out["cached"] = ph if prev is None or ph["total"] < prev["total"] else prev
+    return {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in out.items()}
+
+
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
     """The slowest rank's time (every rank gets it); identity without torch.distributed."""
     if dist is None:
@@ -558,9 +607,11 @@ def main():
     e2e = None
     if not args.no_e2e and rank == 0:
         kw = dict(tile_bits=args.tile_bits, fusion_max_qubits=args.kmax, pass_budget=args.budget)
+        if args.tensor_cores:
+            kw = dict(tensor_cores=True, mma_ops_per_pass=args.tensor_cores)
         e2e_s, h2d, d2h = e2e_steps(circuit, kw, steps=min(args.steps, 3), warmup=1)
         e2e = {"value": ngates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "s_per_step": e2e_s}
+               "s_per_step": e2e_s, "phases_s": e2e_phases(circuit, kw)}
 
     sweep = None
     if not args.no_sweep and rank == 0:

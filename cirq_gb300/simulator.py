@@ -710,17 +710,31 @@ def _recorded_in_place(bits: np.ndarray, op, prng) -> np.ndarray:
 
 
 def _confuse(bits, qubits, confusion_map, prng) -> None:
-    """Applies measurement confusion matrices per repetition, as
-    StepResult._confuse_results does (cirq-core/cirq/sim/simulator.py:822-844)."""
+    """Applies measurement confusion matrices to every repetition (rows of
+    `bits`, in place), with the distribution of
+    StepResult._confuse_results (cirq-core/cirq/sim/simulator.py:822-844):
+    for each map entry in order, the entry's digits (big-endian, mixed
+    radix) pick a row of its confusion matrix and the new digits are drawn
+    from that row.  All repetitions are drawn at once per entry (one
+    inverse-CDF lookup per repetition) instead of one prng.choice per
+    repetition and entry; entries still apply in order, so overlapping
+    entries see the digits the earlier ones wrote."""
     dims = [q.dimension for q in qubits]
-    for rep in bits:
-        for indices, confuser in confusion_map.items():
-            mat_dims = [dims[k] for k in indices]
-            row = cirq.big_endian_digits_to_int((rep[k] for k in indices), base=mat_dims)
-            new_val = prng.choice(len(confuser), p=confuser[row])
-            new_bits = cirq.big_endian_int_to_digits(new_val, base=mat_dims)
-            for i, k in enumerate(indices):
-                rep[k] = new_bits[i]
+    nrep = bits.shape[0]
+    if nrep == 0:
+        return
+    for indices, confuser in confusion_map.items():
+        mat_dims = [dims[k] for k in indices]
+        conf = np.asarray(confuser, dtype=np.float64)
+        row = np.zeros(nrep, dtype=np.int64)
+        for k, d in zip(indices, mat_dims):
+            row = row * d + bits[:, k].astype(np.int64)
+        cdf = np.cumsum(conf, axis=1)
+        u = prng.random_sample(nrep) * cdf[:, -1][row]
+        new_val = np.minimum((u[:, None] >= cdf[row]).sum(axis=1), conf.shape[1] - 1)
+        for k, d in reversed(list(zip(indices, mat_dims))):
+            bits[:, k] = (new_val % d).astype(bits.dtype)
+            new_val //= d
 
 
 def _final_renormalize(eng, state, n: int) -> None:
@@ -737,18 +751,25 @@ def _final_renormalize(eng, state, n: int) -> None:
         )
 
 
+def _state_vector_state_private(qubits, vec: np.ndarray, shape):
+    """A cirq.StateVectorSimulationState around `vec` (no copy), built from the
+    reference's _BufferedStateVector and SimulationState.__init__."""
+    from cirq.sim.state_vector_simulation_state import _BufferedStateVector
+
+    st = cirq.StateVectorSimulationState.__new__(cirq.StateVectorSimulationState)
+    buffered = _BufferedStateVector(vec.reshape(shape), np.empty(0, dtype=np.complex64))
+    cirq.SimulationState.__init__(st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None)
+    return st
+
+
 def _state_vector_result(params, measurements, qubits, vec: np.ndarray):
-    """Builds a genuine cirq.StateVectorTrialResult around `vec` without copying it."""
+    """Builds a genuine cirq.StateVectorTrialResult around `vec` without copying
+    it; if the reference's internals have changed, through its public
+    constructor instead (which copies and validates)."""
     shape = tuple(q.dimension for q in qubits)
     try:
-        from cirq.sim.state_vector_simulation_state import _BufferedStateVector
-
-        st = cirq.StateVectorSimulationState.__new__(cirq.StateVectorSimulationState)
-        buffered = _BufferedStateVector(vec.reshape(shape), np.empty(0, dtype=np.complex64))
-        cirq.SimulationState.__init__(
-            st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None
-        )
-    except Exception:  # pragma: no cover - public-constructor route (copies vec)
+        st = _state_vector_state_private(qubits, vec, shape)
+    except Exception:
         st = cirq.StateVectorSimulationState(
             qubits=tuple(qubits), initial_state=vec.reshape(shape), dtype=np.complex64
         )
@@ -760,6 +781,19 @@ def _state_vector_result(params, measurements, qubits, vec: np.ndarray):
     return res
 
 
+def _density_matrix_state_private(qubits, rho: np.ndarray, shape):
+    """A cirq.DensityMatrixSimulationState around `rho` (no copy, no
+    validation), built from the reference's _BufferedDensityMatrix and
+    SimulationState.__init__."""
+    from cirq.sim.density_matrix_simulation_state import _BufferedDensityMatrix
+
+    st = cirq.DensityMatrixSimulationState.__new__(cirq.DensityMatrixSimulationState)
+    empty = np.empty(0, dtype=np.complex64)
+    buffered = _BufferedDensityMatrix(rho.reshape(shape + shape), [empty, empty, empty])
+    cirq.SimulationState.__init__(st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None)
+    return st
+
+
 def _density_matrix_result(params, measurements, qubits, rho: np.ndarray):
     """Builds a genuine cirq.DensityMatrixTrialResult around `rho` without the
     reference's re-validation (an eigen-decomposition of the 2^n x 2^n matrix
@@ -768,14 +802,11 @@ def _density_matrix_result(params, measurements, qubits, rho: np.ndarray):
     shape = tuple(q.dimension for q in qubits)
     size = int(np.prod(shape, dtype=np.int64))
     try:
-        from cirq.sim.density_matrix_simulation_state import _BufferedDensityMatrix
-
-        st = cirq.DensityMatrixSimulationState.__new__(cirq.DensityMatrixSimulationState)
-        empty = np.empty(0, dtype=np.complex64)
-        buffered = _BufferedDensityMatrix(rho.reshape(shape + shape), [empty, empty, empty])
-        cirq.SimulationState.__init__(st, state=buffered, prng=None, qubits=tuple(qubits), classical_data=None)
-    except Exception:  # pragma: no cover - public-constructor route (validates, copies)
-        st = cirq.DensityMatrixSimulationState(qubits=tuple(qubits), initial_state=rho, dtype=np.complex64)
+        st = _density_matrix_state_private(qubits, rho, shape)
+    except Exception:  # the public constructor validates and copies
+        st = cirq.DensityMatrixSimulationState(
+            qubits=tuple(qubits), initial_state=rho.reshape(shape + shape), dtype=np.complex64
+        )
     res = cirq.DensityMatrixTrialResult(params=params, measurements=measurements, final_simulator_state=st)
     # the reference fills final_density_matrix lazily with a host copy of the
     # state tensor (density_matrix_simulator.py:369-374: 44 ms at 13 qubits);
