@@ -305,12 +305,67 @@ def reference_gate_rates(n: int, circuit, sample_1q: int = 2, sample_2q: int = 1
     return t1, t2, desc
 
 
-def reference_rate(n, circuit):
+def component_sizes(circuit):
+    """Per moment of `circuit`, the size of every operation's untangled
+    component when the reference's default simulator (split_untangled_states
+    on, cirq-core/cirq/sim/simulation_product_state.py) applies it: qubits
+    join a component when an operation acts on them together."""
+    parent = {q: q for q in circuit.all_qubits()}
+    size = {q: 1 for q in parent}
+
+    def find(q):
+        while parent[q] != q:
+            parent[q] = parent[parent[q]]
+            q = parent[q]
+        return q
+
+    out = []
+    for moment in circuit:
+        sizes = []
+        for op in moment:
+            roots = list({find(q) for q in op.qubits})
+            for r in roots[1:]:
+                parent[r] = roots[0]
+                size[roots[0]] += size[r]
+            sizes.append(size[find(op.qubits[0])])
+        out.append(sizes)
+    return out
+
+
+def reference_rate(n, circuit, max_component: int = 22):
+    """Gate-updates/s of the reference's default cirq.Simulator(complex64)
+    (product states on) on the workload: the moments whose components stay
+    within `max_component` qubits are simulated in full by the reference
+    itself; every later gate is charged the measured dense per-gate rate on
+    an n-qubit state (reference_gate_rates) scaled by 2^(component size - n),
+    the size of the tensor it acts on.  Returns (rate, seconds, description)."""
+    cirq = _cirq()
     ops = list(circuit.all_operations())
-    n1 = sum(1 for op in ops if len(op.qubits) == 1)
-    n2 = len(ops) - n1
+    sizes = component_sizes(circuit)
+    k = 0
+    while k < len(sizes) and max(sizes[k], default=0) <= max_component:
+        k += 1
+    moments = list(circuit)
+    prefix = cirq.Circuit(moments[:k])
+    qubits = sorted(circuit.all_qubits())
+    sim = cirq.Simulator(dtype=np.complex64)  # the default configuration
+    t = time.perf_counter()
+    sim.simulate(prefix, qubit_order=qubits)
+    t_prefix = time.perf_counter() - t
     t1, t2, desc = reference_gate_rates(n, circuit)
-    secs = n1 * t1 + n2 * t2
+    rest = 0.0
+    nrest = 0
+    for moment, sz in zip(moments[k:], sizes[k:]):
+        for op, s in zip(moment, sz):
+            rest += (t1 if len(op.qubits) == 1 else t2) * 2.0 ** (s - n)
+            nrest += 1
+    secs = t_prefix + rest
+    nprefix = len(list(prefix.all_operations()))
+    desc = (
+        f"default cirq.Simulator (product states on): the first {k} moments ({nprefix} gates, components "
+        f"<= {max_component} qubits) simulated in full in {t_prefix:.2f} s; the other {nrest} gates charged "
+        f"the dense per-gate rate on the component they act on ({desc})"
+    )
     return len(ops) / secs, secs, desc
 
 
@@ -376,9 +431,22 @@ def adjoint_bench(n: int = 24, layers: int = 10, terms: int = 300, reps: int = 3
     t = time.perf_counter()
     ps = adjoint.parameter_shift_gradient(sim, circuit, ham, symbols, values, indices=idx)
     t_ps = (time.perf_counter() - t) * len(symbols) / len(idx)
+    # algorithmic HBM bytes of one gradient: forward passes (one read + one
+    # write of psi), lam = H psi (one read of psi per group of terms with the
+    # same X mask, one write of lam), <lam|psi> (two reads) and the reverse
+    # two-state passes (read + write of psi and lam)
+    amp = 8 * (1 << prog.nbits)
+    xgroups = len({t[0] for t in prog.terms})
+    alg_bytes = (2 * prog.forward.plan.npasses + xgroups + 1 + 2 + 4 * prog.reverse.npasses) * amp
+    peak, peak_kind = peaks()
     return {
         "workload": f"HEA {n}q x {layers} layers ({len(symbols)} params), H = {terms} Pauli strings",
         "grads_per_s": 1.0 / t_adj,
+        "hbm_bytes_per_grad": alg_bytes,
+        "passes": {"forward": int(prog.forward.plan.npasses), "reverse_two_state": int(prog.reverse.npasses),
+                   "h_psi_x_groups": xgroups},
+        "hbm_frac_of_wall_time": alg_bytes / t_adj / 1e9 / peak,
+        "hbm_frac_note": f"algorithmic bytes / wall time per gradient (host work included) / {peak_kind} hbm_gbs",
         "s_per_grad": t_adj,
         "param_shift_s_per_grad": t_ps,
         "param_shift_sample": f"{len(idx)} of {len(symbols)} parameters timed, extrapolated",
@@ -445,14 +513,75 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
     t = time.perf_counter()
     vals_p = batch.simulate_expectation_values_batch(jobs, persistent=True)
     dt_p = time.perf_counter() - t
+    # algorithmic HBM bytes: per point, every pass reads and writes its state,
+    # then one read of the state per group of terms with the same X mask
+    alg_bytes = 0
+    for job in jobs:
+        amp = 8 * (1 << job.compiled.nbits_dev)
+        xg = len({t[0] for obs in job.terms for t in obs})
+        alg_bytes += len(job.resolvers) * (2 * job.compiled.plan.npasses + xg) * amp
+    peak, peak_kind = peaks()
     return {
         "workload": f"QAOA p={p}, {points} points over widths {list(widths)}",
         "points_per_s": points / dt,
+        "hbm_bytes_total": alg_bytes,
+        "passes_per_point": {str(j.n): int(j.compiled.plan.npasses) for j in jobs},
+        "hbm_frac_of_wall_time": alg_bytes / dt / 1e9 / peak,
+        "hbm_frac_note": f"algorithmic bytes / wall time (host pool building included) / {peak_kind} hbm_gbs",
         "s_total": dt,
         "mode": "points of a job evolved together (one tile-pass launch per pass)",
         "persistent_single_launch_s_total": dt_p,
         "max_abs_diff_between_modes": float(max(np.abs(a - b).max() for a, b in zip(vals, vals_p))),
         "mean_expectation": float(np.mean([np.real(v).mean() for v in vals])),
+    }
+
+
+def c1_bench(n: int = 20, depth: int = 20, reps: int = 10_000, calls: int = 5):
+    """The CPU-runnable configuration: 20 qubits, depth 20 (590 gates).
+    simulate() latency (first call, with planning, and cached) and
+    run(repetitions=10^4) measuring every qubit, through the public API,
+    beside the reference's cirq.Simulator(dtype=complex64) on the same
+    circuits in the same process (one host core: numpy's path is
+    single-threaded).  The 8 MiB state fits in L2, so there is no HBM
+    roofline here: the figures are latencies."""
+    cirq = _cirq()
+    import cirq_gb300
+
+    circuit, ngates = build_workload(n, depth, 0)
+    q = sorted(circuit.all_qubits())
+    measured = circuit + cirq.measure(*q, key="m")
+
+    def timed(fn, k):
+        best = None
+        for _ in range(k):
+            t = time.perf_counter()
+            fn()
+            dt = time.perf_counter() - t
+            best = dt if best is None else min(best, dt)
+        return best
+
+    sim = cirq_gb300.Simulator()
+    t = time.perf_counter()
+    sim.simulate(circuit).final_state_vector
+    first = time.perf_counter() - t
+    ours_sim = timed(lambda: sim.simulate(circuit).final_state_vector, calls)
+    sim.run(measured, repetitions=reps)
+    ours_run = timed(lambda: sim.run(measured, repetitions=reps), calls)
+    ref = cirq.Simulator(dtype=np.complex64)
+    ref_sim = timed(lambda: ref.simulate(circuit).final_state_vector, 1)
+    ref_run = timed(lambda: ref.run(measured, repetitions=reps), 1)
+    return {
+        "workload": f"random-layer circuit {n}q depth {depth} ({ngates} gates), seed 0",
+        "simulate_s_first_call": first,
+        "simulate_s": ours_sim,
+        "run_10k_s": ours_run,
+        "reference_simulate_s": ref_sim,
+        "reference_run_10k_s": ref_run,
+        "speedup_simulate": ref_sim / ours_sim,
+        "speedup_run": ref_run / ours_run,
+        "gate_updates_per_s": ngates / ours_sim,
+        "reference_cores": 1,
+        "note": "state (8 MiB) is L2-resident: latency figures, no HBM roofline",
     }
 
 
@@ -638,7 +767,8 @@ def main():
 
     extra = {}
     if not args.no_extra and rank == 0:
-        for name, fn in (("adjoint", adjoint_bench), ("density_matrix", density_bench), ("batch_sweep", batch_bench),
+        for name, fn in (("c1_20q", c1_bench), ("adjoint", adjoint_bench), ("density_matrix", density_bench),
+                         ("batch_sweep", batch_bench),
                          ("width_33", width33_bench), ("tensor_core_pass", mma_bench)):
             try:
                 extra[name] = fn()

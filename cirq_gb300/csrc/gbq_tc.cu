@@ -16,18 +16,19 @@
 // linalg.targeted_left_multiply (cirq-core/cirq/linalg/transformations.py:105-172)
 // and the gates' _apply_unitary_ (cirq-core/cirq/ops/common_gates.py).
 //
-// Warp roles (one CTA per SM, 288 threads):
-//   warps 0-3  epilogue: tcgen05.ld of their 32-lane quarter of the
-//              accumulators, the pass's diagonal ops on CUDA cores, the hi/lo
-//              split, and the write of the next op's A operand in shared
-//              memory (or of the natural-order tile after the last op); they
-//              also split each freshly loaded tile;
-//   warp 4     one thread issues the MMAs and commits them to an mbarrier;
-//   warps 5-8  producers: cp.async loads of tiles into the first op's A
-//              layout, 16-byte streaming stores of finished tiles.
-// Each CTA owns two slots (A_hi + A_lo, 64 KB each) that hold two tiles at
-// different stages, so the tensor pipe runs one tile's MMAs while the
-// epilogue warps read back the other's and the producers stream the next.
+// One CTA per SM (448 threads) runs two independent slot pipelines; each
+// slot (A_hi + A_lo, 64 KB) holds one tile and has its own warps:
+//   4 epilogue warps  tcgen05.ld of their 32-lane quarter of the slot's
+//                     accumulators, the pass's diagonal ops on CUDA cores,
+//                     the hi/lo split, and the write of the next op's A
+//                     operand in shared memory (or of the natural-order tile
+//                     after the last op); they also split each loaded tile;
+//   1 MMA warp        one thread issues the slot's MMAs and commits them to
+//                     an mbarrier;
+//   2 producer warps  cp.async loads of the slot's tiles into the first op's
+//                     A layout, 16-byte streaming stores of finished tiles.
+// The slots take alternate tiles, so the tensor pipe runs one slot's MMAs
+// while the other slot's warps read back, split, load or store.
 // Slot s has four mbarriers: full (loaded), ready (A written, accumulator
 // free: next op may issue), done (MMAs complete), final (natural-order tile
 // written).  Every wait is bounded: a wait that runs out raises the CTA's
@@ -54,12 +55,14 @@ constexpr int kTBytes = kTS * 8;       // 32 KB
 constexpr int kTHalfBytes = kTBytes / 2;
 constexpr int kTMatBytes = 8192;       // one matrix: hi and lo real forms, 4 KB each
 constexpr int kTMaxMats = GBQ_TC_MAX_MATS;
-constexpr int kTEpi = 4, kTProd = 4;
-constexpr int kTThreads = 32 * (kTEpi + 1 + kTProd);
-constexpr int kTProdThreads = 32 * kTProd;
+constexpr int kTEpi = 4, kTProd = 2;   // per slot: epilogue warps, producer warps
+constexpr int kTMmaWarp0 = 2 * kTEpi;  // one MMA-issuing warp per slot
+constexpr int kTProdWarp0 = kTMmaWarp0 + 2;
+constexpr int kTThreads = 32 * (kTProdWarp0 + 2 * kTProd);
+constexpr int kTProdThreads = 32 * kTProd;  // per slot
 constexpr int kTSmem = 4 * kTBytes + kTMaxMats * kTMatBytes + 1024;
 constexpr uint32_t kTTmemCols = 128;   // 2 slots x 2 halves x 32 columns
-constexpr long kTSpin = 1L << 26;      // polls before a wait is given up
+constexpr long kTSpin = 1L << 24;      // try_wait polls before a wait is given up
 constexpr int kTNH = kTS >> 5;         // tile-index values of bits 5..11
 // Instruction descriptor: D f32, A and B tf32, both K-major, N = 32, M = 128.
 constexpr uint32_t kTIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
@@ -96,10 +99,14 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, 
       "l"(ad), "l"(bd), "r"(kTIdesc), "r"(acc));
 }
 
-__device__ __forceinline__ bool tc_test(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void tc_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool tc_try(uint32_t bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
-      "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
       "selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(done)
       : "r"(bar), "r"(parity)
@@ -107,15 +114,21 @@ __device__ __forceinline__ bool tc_test(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
-__device__ __forceinline__ void tc_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
-}
-
 // Bounded blocking wait (one thread); false when it ran out or *abort rose.
 __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
   for (long it = 0; it < kTSpin; ++it) {
-    if (tc_test(bar, parity)) return true;
-    if ((it & 1023) == 1023 && *abort) return false;
+    if (tc_try(bar, parity)) return true;
+    if ((it & 255) == 255 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+// The same for a whole warp, with a warp-uniform result.
+__device__ __forceinline__ bool tc_wait_warp(uint32_t bar, uint32_t parity, volatile int* abort) {
+  for (long it = 0; it < kTSpin; ++it) {
+    if (__all_sync(0xffffffffu, tc_try(bar, parity))) return true;
+    if ((it & 255) == 255 && __any_sync(0xffffffffu, *abort != 0)) return false;
   }
   *abort = 1;
   return false;
@@ -204,19 +217,20 @@ __global__ void __launch_bounds__(kTThreads, 1) k_tc_pass(const __grid_constant_
   __shared__ uint64_t hoff[kTNH];   // global offset of tile index (j << 5)
   __shared__ uint16_t lhigh[kTNH];  // first-op layout pair index of tile index (j << 5)
   __shared__ uint16_t nhigh[kTNH];  // natural layout pair index of tile index (j << 5)
-  __shared__ __align__(8) uint64_t bar_full[2], bar_ready[2], bar_done[2], bar_final[2], bar_drain;
+  __shared__ __align__(8) uint64_t bar_full[2], bar_ready[2], bar_done[2], bar_final[2], bar_drain[2];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
-  float2* Ahi[2] = {reinterpret_cast<float2*>(base), reinterpret_cast<float2*>(base + 2 * kTBytes)};
-  float2* Alo[2] = {reinterpret_cast<float2*>(base + kTBytes), reinterpret_cast<float2*>(base + 3 * kTBytes)};
   unsigned char* bmem = base + 4 * kTBytes;
   const int t = threadIdx.x;
   const int warp = __shfl_sync(0xffffffffu, t >> 5, 0), lane = t & 31;
   const TileInfo& ti = a.ti;
 
-  tile_tables_build(ti, ttab);
+  for (int e = t; e < 3 * kTileTab; e += kTThreads) {
+    const int part = e / kTileTab;
+    ttab[e] = tile_base(ti, (int64_t)(e % kTileTab) << (8 * part));
+  }
   for (int j = t; j < kTNH; j += kTThreads) {
     hoff[j] = lin_off<kTL>(ti, (uint32_t)j << 5);
     uint32_t lp = 0, np = 0;
@@ -254,11 +268,11 @@ __global__ void __launch_bounds__(kTThreads, 1) k_tc_pass(const __grid_constant_
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tsu32(&bar_ready[s])), "r"(32 * kTEpi));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(tsu32(&bar_done[s])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tsu32(&bar_final[s])), "r"(32 * kTEpi));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(tsu32(&bar_drain[s])));
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(tsu32(&bar_drain)));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == kTEpi) {
+  if (warp == kTMmaWarp0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tsu32(&tmem_base_sh)),
                  "r"(kTTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
@@ -272,179 +286,165 @@ __global__ void __launch_bounds__(kTThreads, 1) k_tc_pass(const __grid_constant_
   const int64_t step = gridDim.x;
   const int64_t count = blockIdx.x < ti.ntiles ? (ti.ntiles - 1 - blockIdx.x) / step + 1 : 0;
 
-  if (warp < kTEpi) {
-    // ---- epilogue warps: per slot, stage 0 = split of a loaded tile,
-    // stage o + 1 = read-back of op o
-    int64_t k[2] = {0, 1};
-    int stage[2] = {0, 0};
-    uint32_t nfull[2] = {0, 0}, ndone[2] = {0, 0};
-    long spin = 0;
-    int s = 0;
-    while (k[0] < count || k[1] < count) {
-      if (__any_sync(0xffffffffu, *abort != 0)) break;  // warp-uniform exit
-      if (k[s] >= count) {
-        s ^= 1;
-        continue;
-      }
-      const uint32_t bar = stage[s] == 0 ? tsu32(&bar_full[s]) : tsu32(&bar_done[s]);
-      const uint32_t par = stage[s] == 0 ? (nfull[s] & 1u) : (ndone[s] & 1u);
-      const bool ok = __all_sync(0xffffffffu, tc_test(bar, par));
-      if (!ok) {
-        if (++spin > kTSpin) *abort = 1;
-        s ^= 1;
-        continue;
-      }
-      spin = 0;
-      const int64_t tile = blockIdx.x + k[s] * step;
-      const uint64_t gbase = tile_base_fast(ttab, tile);
-      if (stage[s] == 0) {
-        ++nfull[s];
-        // three-term split of the loaded tile in place (16-byte chunks)
-        float4* h4 = reinterpret_cast<float4*>(Ahi[s]);
-        float4* l4 = reinterpret_cast<float4*>(Alo[s]);
+  // Two independent slot pipelines: slot s owns epilogue warps 4s..4s+3,
+  // MMA warp kTMmaWarp0 + s and producer warps kTProdWarp0 + kTProd * s ...,
+  // and processes this CTA's tiles k = s, s + 2, s + 4, ...
+  int s = 0, role = 0;
+  if (warp < 2 * kTEpi) {
+    s = warp / kTEpi;
+    role = 0;
+  } else if (warp < kTMmaWarp0 + 2) {
+    s = warp - kTMmaWarp0;
+    role = 1;
+  } else {
+    s = (warp - kTProdWarp0) / kTProd;
+    role = 2;
+  }
+  float2* Ahi = reinterpret_cast<float2*>(base + s * 2 * kTBytes);
+  float2* Alo = reinterpret_cast<float2*>(base + s * 2 * kTBytes + kTBytes);
+  const uint32_t full = tsu32(&bar_full[s]), ready = tsu32(&bar_ready[s]), done = tsu32(&bar_done[s]),
+                 fin = tsu32(&bar_final[s]);
+
+  if (role == 0) {
+    // ---- epilogue warps of slot s
+    const int w = warp & 3;
+    const int et = t - 32 * kTEpi * s;  // 0..127 within the slot's group
+    uint32_t ndone = 0;
+    for (int64_t k = s, it = 0; k < count; k += 2, ++it) {
+      if (!tc_wait_warp(full, (uint32_t)(it & 1), abort)) break;
+      const uint64_t gbase = tile_base_fast(ttab, blockIdx.x + k * step);
+      // three-term split of the loaded tile in place (16-byte chunks)
+      float4* h4 = reinterpret_cast<float4*>(Ahi);
+      float4* l4 = reinterpret_cast<float4*>(Alo);
 #pragma unroll 4
-        for (int f = t; f < kTS / 2; f += 32 * kTEpi) {
-          const float4 v = h4[f];
-          const float4 hv = make_float4(tc_tf32(v.x), tc_tf32(v.y), tc_tf32(v.z), tc_tf32(v.w));
-          h4[f] = hv;
-          l4[f] = make_float4(tc_tf32(v.x - hv.x), tc_tf32(v.y - hv.y), tc_tf32(v.z - hv.z), tc_tf32(v.w - hv.w));
-        }
-        tc_fence_async();
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        tc_arrive(tsu32(&bar_ready[s]));
-        stage[s] = 1;
-      } else {
-        ++ndone[s];
-        const int o = stage[s] - 1;
-        tc_epilogue_op(a, o, tmem + (uint32_t)(64 * s), warp, lane, gbase, Ahi[s], Alo[s]);
-        if (o + 1 < a.nops) {
-          tc_fence_async();
-          asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-          tc_arrive(tsu32(&bar_ready[s]));
-          stage[s] = o + 2;
-        } else {
-          asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-          tc_arrive(tsu32(&bar_final[s]));
-          stage[s] = 0;
-          k[s] += 2;
-        }
+      for (int f = et; f < kTS / 2; f += 32 * kTEpi) {
+        const float4 v = h4[f];
+        const float4 hv = make_float4(tc_tf32(v.x), tc_tf32(v.y), tc_tf32(v.z), tc_tf32(v.w));
+        h4[f] = hv;
+        l4[f] = make_float4(tc_tf32(v.x - hv.x), tc_tf32(v.y - hv.y), tc_tf32(v.z - hv.z), tc_tf32(v.w - hv.w));
       }
-      s ^= 1;
+      tc_fence_async();
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      tc_arrive(ready);
+      bool ok = true;
+      for (int o = 0; o < a.nops; ++o) {
+        if (!tc_wait_warp(done, ndone & 1u, abort)) {
+          ok = false;
+          break;
+        }
+        ++ndone;
+        tc_epilogue_op(a, o, tmem + (uint32_t)(64 * s), w, lane, gbase, Ahi, Alo);
+        if (o + 1 < a.nops) tc_fence_async();
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        tc_arrive(o + 1 < a.nops ? ready : fin);
+      }
+      if (!ok) break;
     }
-  } else if (warp == kTEpi) {
-    // ---- MMA issuer: one thread, the next op of whichever slot is ready
+  } else if (role == 1) {
+    // ---- MMA issuer of slot s: one thread
     if (lane == 0) {
-      int64_t k[2] = {0, 1};
-      int op_of[2] = {0, 0};
-      uint32_t nready[2] = {0, 0};
-      long spin = 0;
-      int s = 0;
+      uint32_t nready = 0;
       bool issued = false;
-      while ((k[0] < count || k[1] < count) && !*abort) {
-        if (k[s] >= count || !tc_test(tsu32(&bar_ready[s]), nready[s] & 1u)) {
-          if (++spin > kTSpin) *abort = 1;
-          s ^= 1;
-          continue;
-        }
-        spin = 0;
-        ++nready[s];
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const TcOpDev& op = a.ops[op_of[s]];
-        const uint64_t gbase = tile_base_fast(ttab, blockIdx.x + k[s] * step);
-        uint32_t sel = 0;
-        for (int q = 0; q < op.nsel; ++q) sel |= (uint32_t)((gbase >> op.selg[q]) & 1ull) << q;
-        const uint32_t bh = tsu32(bmem) + (uint32_t)(op.bslot + (int)sel) * kTMatBytes;
-        const uint32_t ah = tsu32(Ahi[s]), al = tsu32(Alo[s]);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const uint32_t d = tmem + (uint32_t)(64 * s + 32 * h);
-#pragma unroll
-          for (int p = 0; p < 3; ++p) {
-            const uint32_t A = (p == 2 ? al : ah) + (uint32_t)(h * kTHalfBytes);
-            const uint32_t B = p == 1 ? bh + 4096 : bh;
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) tc_mma(d, tc_desc(A + 32 * ks), tc_desc(B + 32 * ks), (p | ks) != 0);
+      for (int64_t k = s; k < count && !*abort; k += 2) {
+        const uint64_t gbase = tile_base_fast(ttab, blockIdx.x + k * step);
+        bool ok = true;
+        for (int o = 0; o < a.nops; ++o) {
+          if (!tc_wait(ready, nready & 1u, abort)) {
+            ok = false;
+            break;
           }
+          ++nready;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const TcOpDev& op = a.ops[o];
+          uint32_t sel = 0;
+          for (int q = 0; q < op.nsel; ++q) sel |= (uint32_t)((gbase >> op.selg[q]) & 1ull) << q;
+          const uint32_t bh = tsu32(bmem) + (uint32_t)(op.bslot + (int)sel) * kTMatBytes;
+          const uint32_t ah = tsu32(Ahi), al = tsu32(Alo);
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                // the two halves' accumulation chains interleave
+                const uint32_t A = (p == 2 ? al : ah) + (uint32_t)(h * kTHalfBytes);
+                const uint32_t B = p == 1 ? bh + 4096 : bh;
+                tc_mma(tmem + (uint32_t)(64 * s + 32 * h), tc_desc(A + 32 * ks), tc_desc(B + 32 * ks),
+                       (p | ks) != 0);
+              }
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(done)
+                       : "memory");
+          issued = true;
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                         tsu32(&bar_done[s]))
-                     : "memory");
-        issued = true;
-        if (++op_of[s] == a.nops) {
-          op_of[s] = 0;
-          k[s] += 2;
-        }
-        s ^= 1;
+        if (!ok) break;
       }
       if (issued) {
         // every MMA issued so far completes before tensor memory is freed
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                         tsu32(&bar_drain))
+                         tsu32(&bar_drain[s]))
                      : "memory");
         volatile int never = 0;
-        tc_wait(tsu32(&bar_drain), 0, &never);
+        tc_wait(tsu32(&bar_drain[s]), 0, &never);
       }
     }
   } else {
-    // ---- producers: loads into the first op's layout, natural-order stores
-    const int pt = t - 32 * (kTEpi + 1);
+    // ---- producers of slot s: loads into the first op's layout, natural-order stores
+    const int pt = t - 32 * (kTProdWarp0 + kTProd * s);  // 0..kTProdThreads-1
     const int pw = pt >> 5;
     const uint64_t lo_l = lin_off<kTL>(ti, (uint32_t)lane);
     uint32_t lp_l = 0;
 #pragma unroll
     for (int b = 0; b < 5; ++b)
       if ((lane >> b) & 1) lp_l ^= a.lcol[b];
-    // store geometry: pair index j = pt + kTProdThreads * i covers tile indices 2j, 2j + 1
-    auto load = [&](int64_t kk, int s) {
+    auto load = [&](int64_t kk) {
       const uint64_t gb = tile_base_fast(ttab, blockIdx.x + kk * step);
       const float2* g = a.psi + gb + lo_l;
-      float2* dst = Ahi[s];
 #pragma unroll 4
       for (int jj = pw; jj < kTNH; jj += kTProd) {
-        const uint32_t sa = tsu32(dst + (lp_l ^ lhigh[jj]));
+        const uint32_t sa = tsu32(Ahi + (lp_l ^ lhigh[jj]));
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g + hoff[jj]) : "memory");
       }
-      asm volatile("cp.async.mbarrier.arrive.noinc.shared.b64 [%0];\n" ::"r"(tsu32(&bar_full[s])) : "memory");
+      asm volatile("cp.async.mbarrier.arrive.noinc.shared.b64 [%0];\n" ::"r"(full) : "memory");
     };
-    for (int64_t kk = 0; kk < count && kk < 2; ++kk) load(kk, (int)kk);
-    for (int64_t kk = 0; kk < count; ++kk) {
-      const int s = (int)(kk & 1);
-      const bool ok = tc_wait(tsu32(&bar_final[s]), (uint32_t)((kk >> 1) & 1), abort);
-      // every producer leaves at the same iteration (they meet at bar 2 below)
+    if (s < count) load(s);
+    for (int64_t kk = s, it = 0; kk < count; kk += 2, ++it) {
+      const bool ok = tc_wait(fin, (uint32_t)(it & 1), abort);
+      // every producer of the slot leaves at the same iteration (they meet at a named barrier below)
       uint32_t any_fail;
       asm volatile(
-          "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, 3, %2, p;\n"
+          "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, %2, %3, p;\n"
           "selp.u32 %0, 1, 0, q;\n}\n"
           : "=r"(any_fail)
-          : "r"((uint32_t)!ok), "n"(kTProdThreads)
+          : "r"((uint32_t)!ok), "r"(4 + s), "n"(kTProdThreads)
           : "memory");
       if (any_fail) break;
       const uint64_t gb = tile_base_fast(ttab, blockIdx.x + kk * step);
-      const float2* src = Ahi[s];
 #pragma unroll 4
       for (int j = pt; j < kTS / 2; j += kTProdThreads) {
         const uint32_t i2 = (uint32_t)(2 * j);
         uint32_t np = nhigh[i2 >> 5];
-#pragma unroll
-        for (int b = 1; b < 5; ++b)
-          if ((i2 >> b) & 1) np ^= tc_nat_col(b);
-        const float4 v = *reinterpret_cast<const float4*>(src + np);
         uint64_t go = hoff[i2 >> 5];
 #pragma unroll
         for (int b = 1; b < 5; ++b)
-          if ((i2 >> b) & 1) go += ti.gw[b];
+          if ((i2 >> b) & 1) {
+            np ^= tc_nat_col(b);
+            go += ti.gw[b];
+          }
+        const float4 v = *reinterpret_cast<const float4*>(Ahi + np);
         __stcs(reinterpret_cast<float4*>(a.psi + gb + go), v);
       }
-      // every producer has read slot s before any refills it
-      asm volatile("bar.sync 2, %0;\n" ::"n"(kTProdThreads) : "memory");
-      if (kk + 2 < count) load(kk + 2, s);
+      // every producer has read the slot before any refills it
+      asm volatile("bar.sync %0, %1;\n" ::"r"(2 + s), "n"(kTProdThreads) : "memory");
+      if (kk + 2 < count) load(kk + 2);
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   if (t == 0 && *abort && a.abort) atomicExch(a.abort, 1);
-  if (warp == kTEpi) {
+  if (warp == kTMmaWarp0) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTTmemCols));
   }

@@ -72,6 +72,26 @@ def _plain_gates():
     return _PLAIN_GATES
 
 
+_CHANNEL_GATES = None
+
+
+def _channel_gates():
+    """The reference's channel gate families: each defines its own Kraus
+    operators or mixture (cirq-core/cirq/ops/common_channels.py,
+    kraus_channel.py, mixed_unitary_channel.py), so none needs the
+    decomposition fallback, and answering that from the type avoids building
+    their operators twice per simulation."""
+    global _CHANNEL_GATES
+    if _CHANNEL_GATES is None:
+        cirq = _cirq()
+        _CHANNEL_GATES = (
+            cirq.DepolarizingChannel, cirq.AsymmetricDepolarizingChannel, cirq.AmplitudeDampingChannel,
+            cirq.GeneralizedAmplitudeDampingChannel, cirq.PhaseDampingChannel, cirq.PhaseFlipChannel,
+            cirq.BitFlipChannel, cirq.ResetChannel, cirq.KrausChannel, cirq.MixedUnitaryChannel,
+        )
+    return _CHANNEL_GATES
+
+
 def _is_measurement(op) -> bool:
     return _cirq().is_measurement(op)
 
@@ -106,6 +126,7 @@ def flatten_ops(circuit) -> list:
     rejected by the compiler."""
     cirq = _cirq()
     plain, gate_op, meas = _plain_gates(), cirq.GateOperation, cirq.MeasurementGate
+    chans = _channel_gates()
     ops = []
     for moment in circuit:
         for op in moment:
@@ -113,6 +134,9 @@ def flatten_ops(circuit) -> list:
                 gate = op.gate
                 if isinstance(gate, meas) or (isinstance(gate, plain) and len(op.qubits) <= MAX_OP_QUBITS):
                     ops.append(op)
+                    continue
+                if isinstance(gate, chans) and len(op.qubits) <= MAX_OP_QUBITS:
+                    ops.append(op)  # a channel with operators of its own
                     continue
             if is_loop(op):
                 ops.append(op)  # repeats a data-dependent number of times: a trajectory event
@@ -156,6 +180,8 @@ def is_measurement_op(op) -> bool:
             return True
         if isinstance(gate, (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate, cirq.PhasedXPowGate)):
             return False
+        if isinstance(gate, _channel_gates()) and not isinstance(gate, (cirq.KrausChannel, cirq.MixedUnitaryChannel)):
+            return False  # channels without a measurement key
     return cirq.is_measurement(op) and not is_keyed_channel(op)
 
 
@@ -204,6 +230,8 @@ def _needs_decomposition(op) -> bool:
     if gate is not None and isinstance(gate, (cirq.EigenGate, cirq.PhasedXZGate, cirq.MatrixGate,
                                                cirq.MeasurementGate, cirq.PhasedXPowGate)):
         return False  # the common gate families: unitary (or a measurement) by construction
+    if gate is not None and isinstance(gate, _channel_gates()):
+        return False  # operators of their own
     if not op.qubits or cirq.is_parameterized(op) or cirq.is_measurement(op):
         return False
     if isinstance(op.untagged, cirq.ClassicallyControlledOperation):
