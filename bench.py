@@ -187,6 +187,7 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
     import cirq_gb300
 
     sim = cirq_gb300.Simulator(**planner_kwargs)
+    a0 = sim.engine.pinned.allocations
     for _ in range(warmup):
         r = sim.simulate(circuit)
         vec = r.final_state_vector
@@ -203,6 +204,7 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
         vec_bytes = vec.nbytes
         del r, vec
     compiled = next(iter(sim._cache.values()))
+    e2e_steps.pinned_allocations = sim.engine.pinned.allocations - a0
     return float(np.mean(times)), int(compiled.plan.pool.nbytes), int(vec_bytes)
 
 
@@ -246,13 +248,14 @@ def e2e_phases(circuit, planner_kwargs, repeats: int = 2):
         res = sim_mod._state_vector_result(cirq.ParamResolver({}), {}, qubits, vec)
         ph["assemble"] = time.perf_counter() - t
         ph["total"] = sum(ph.values())
+        ph["pinned_allocations_so_far"] = eng.pinned.allocations
         del res, vec
         if rep == 0:
             out["first"] = ph
         else:
             prev = out.get("cached")
             out["cached"] = ph if prev is None or ph["total"] < prev["total"] else prev
-    return {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in out.items()}
+    return {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()} for k, v in out.items()}
 
 
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
@@ -608,6 +611,33 @@ def width33_bench(depth: int = 40, steps: int = 2):
     }
 
 
+def tc_bench(n: int = 30, depth: int = 40, budgets=(3, 4, 6), steps: int = 2):
+    """The pipelined tensor-core pass (k_tc_pass: 12-bit tiles, 4-qubit blocks
+    as tcgen05 TF32 three-term MMAs) on the headline workload, against the
+    CUDA-core plan of the headline line: ms per step and per pass, passes,
+    and the HBM fraction per pass, for a few MMA-op budgets per pass."""
+    from cirq_gb300.engine import Engine
+    from cirq_gb300.planner import Planner
+
+    eng = Engine.get(0)
+    circuit, ngates = build_workload(n, depth, 0)
+    peak, _ = peaks()
+    out = {"workload": f"random-layer circuit {n}q depth {depth} ({ngates} gates), seed 0"}
+    for b in budgets:
+        ck = compile_plan(circuit, Planner(tensor=True, budget=b))
+        ms, pms, npass, _ = device_steps(eng, ck, steps, 1, pass_timing=True)
+        mma = int((ck.plan.ops["kind"] == 9).sum())
+        out[f"mma_ops_per_pass_{b}"] = {
+            "gate_updates_per_s": ngates / (ms / 1e3),
+            "ms_per_step": ms,
+            "passes": int(ck.plan.npasses),
+            "mma_ops": mma,
+            "mean_pass_ms": pms,
+            "hbm_frac": 16 * (1 << ck.nbits) / (pms / 1e3) / 1e9 / peak if pms else None,
+        }
+    return out
+
+
 def mma_bench(n: int = 30, reps: int = 3):
     """Tensor-core evaluation: one 11-bit-tile pass applying 1, 2 or 4
     random 4-qubit matrices with tcgen05 MMAs (GBQ_OP_MMA, TF32 three-term
@@ -740,7 +770,8 @@ def main():
             kw = dict(tensor_cores=True, mma_ops_per_pass=args.tensor_cores)
         e2e_s, h2d, d2h = e2e_steps(circuit, kw, steps=min(args.steps, 3), warmup=1)
         e2e = {"value": ngates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "s_per_step": e2e_s, "phases_s": e2e_phases(circuit, kw)}
+               "s_per_step": e2e_s, "pinned_host_allocations": getattr(e2e_steps, "pinned_allocations", None),
+               "phases_s": e2e_phases(circuit, kw)}
 
     sweep = None
     if not args.no_sweep and rank == 0:
@@ -769,7 +800,8 @@ def main():
     if not args.no_extra and rank == 0:
         for name, fn in (("c1_20q", c1_bench), ("adjoint", adjoint_bench), ("density_matrix", density_bench),
                          ("batch_sweep", batch_bench),
-                         ("width_33", width33_bench), ("tensor_core_pass", mma_bench)):
+                         ("width_33", width33_bench), ("tensor_core_pipelined", tc_bench),
+                         ("tensor_core_pass_11bit", mma_bench)):
             try:
                 extra[name] = fn()
             except Exception as e:  # reported, not hidden

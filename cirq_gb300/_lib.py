@@ -183,6 +183,7 @@ SIGNATURES = {
     "gbq_run": [_P, _P, _I, _P, _I, _P, _I, _P],
     "gbq_run_dual": [_P, _P, _P, _I, _P, _I, _P, _I, _P, _P],
     "gbq_reduce_slots": [_P, _P, _I, _I64, _P],
+    "gbq_adjoint": [_P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _I, _P, _I, _P, _I, _P, _P],
     "gbq_sv_norm2": [_P, _P, _I, _P],
     "gbq_sv_scale": [_P, _P, _I, _F],
     "gbq_sv_final_renormalize": [_P, _P, _I, _P, _P],

@@ -224,6 +224,42 @@ class AdjointProgram:
         lam.free()
         return E, g
 
+    def value_and_grad_native(self, values) -> tuple[float, np.ndarray]:
+        """The same (E, gradient) through one C-ABI call (gbq_adjoint): the
+        matrix pools of the forward and reverse programs are built here and
+        the engine runs the forward passes, lam = H psi, <psi|lam>, the
+        reverse sweep and the slot sums on its own."""
+        import ctypes
+
+        from cirq_gb300 import _lib
+
+        eng = self.engine
+        r = cirq.ParamResolver(dict(zip(self.symbols, [float(v) for v in values])))
+        fwd = self.forward
+        gates = fwd.gate_batch([r])
+        fpool = eng.upload(np.ascontiguousarray(fwd.pool_from_batch(gates, 1)[0]))
+        rpool = eng.upload(np.ascontiguousarray(self._reverse_pool(r, gates)))
+        slots = np.zeros(max(self.nslots, 1), dtype=np.float64)
+        value = ctypes.c_double()
+        fp, rp = fwd.plan, self.reverse
+        try:
+            _lib.check(
+                eng.lib.gbq_adjoint(
+                    eng.ctx, self.n, self.nbits, fp.passes.ctypes.data, len(fp.passes), fp.ops.ctypes.data,
+                    len(fp.ops), fpool.ptr, self._pauli.ctypes.data, len(self._pauli), rp.passes.ctypes.data,
+                    len(rp.passes), rp.ops.ctypes.data, len(rp.ops), rpool.ptr, self.nslots, ctypes.byref(value),
+                    slots.ctypes.data,
+                ),
+                "gbq_adjoint",
+            )
+        finally:
+            fpool.free()
+            rpool.free()
+        grad = np.zeros(len(self.symbols))
+        if self.nslots:
+            np.add.at(grad, np.array(self.slot_symbol), 2.0 * slots[: self.nslots])
+        return value.value, grad
+
     def value(self, values) -> float:
         psi, lam, E, _ = self.forward_state(values)
         psi.free()

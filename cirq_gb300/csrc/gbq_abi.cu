@@ -776,6 +776,80 @@ int gbq_run_dual(gbq_ctx* c, gbq_c64* psi, gbq_c64* lam, int nbits, const gbq_pa
                     passes, npasses, ops, nops, reinterpret_cast<const float2*>(mats), partial);
 }
 
+int gbq_adjoint(gbq_ctx* c, int nq, int nbits, const gbq_pass* fpasses, int nfpasses, const gbq_op* fops,
+                int nfops, const gbq_c64* fmats, const gbq_pauli* terms, int nterms, const gbq_pass* rpasses,
+                int nrpasses, const gbq_op* rops, int nrops, const gbq_c64* rmats, int nslots, double* value,
+                double* slot_values) {
+  CHECK_CTX(c);
+  if (nq < 1 || nbits < nq || nbits > 36 || !value || nslots < 0 || (nslots && !slot_values))
+    return arg_fail("gbq_adjoint: bad arguments");
+  if (nfpasses < 0 || (nfpasses && (!fpasses || !fops || !fmats))) return arg_fail("gbq_adjoint: null forward program");
+  if (nrpasses < 0 || (nrpasses && (!rpasses || !rops || !rmats))) return arg_fail("gbq_adjoint: null reverse program");
+  int rc = gbq_validate_program(nbits, fpasses, nfpasses, fops, nfops, 0);
+  if (rc) return rc;
+  rc = gbq_validate_program(nbits, rpasses, nrpasses, rops, nrops, 1);
+  if (rc) return rc;
+  int rl = 0;
+  for (int q = 0; q < nrpasses; ++q) {
+    if (rl && rpasses[q].L != rl) return arg_fail("gbq_adjoint: reverse passes must share one tile width");
+    rl = rpasses[q].L;
+  }
+  for (int q = 0; q < nrpasses; ++q)
+    for (int o = 0; o < rpasses[q].op_count; ++o) {
+      const gbq_op& op = rops[rpasses[q].op_begin + o];
+      const bool probe = op.kind == GBQ_OP_PROBE || op.kind == GBQ_OP_PROBE_DIAG || op.kind == GBQ_OP_RPROBE ||
+                         op.kind == GBQ_OP_RPROBE_DIAG;
+      if (probe && (op.slot < 0 || op.slot >= nslots)) return arg_fail("gbq_adjoint: probe slot out of range");
+    }
+  const int64_t ntiles = rl ? (int64_t)1 << (nbits - rl) : 1;
+  const size_t sbytes = (size_t)8 << nbits;
+  const size_t pbytes = (size_t)8 * (nslots ? nslots : 1) * ntiles;
+  float2 *psi = nullptr, *lam = nullptr;
+  double *partial = nullptr, *d_slots = nullptr;
+  auto release = [&]() {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(psi);
+    cudaFree(lam);
+    cudaFree(partial);
+    cudaFree(d_slots);
+  };
+  cudaError_t e = cudaMalloc(&psi, sbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&lam, sbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&partial, pbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&d_slots, 8 * (size_t)(nslots ? nslots : 1));
+  if (e != cudaSuccess) {
+    release();
+    return cuda_fail(e, "gbq_adjoint: cudaMalloc");
+  }
+  // forward: psi = U(theta)|0>, lam = H psi (padding amplitudes stay zero), E = <psi|lam>
+  rc = do_set_basis(c, psi, nbits, 0);
+  if (!rc && nfpasses)
+    rc = run_passes(c, psi, nullptr, nbits, fpasses, nfpasses, fops, nfops, reinterpret_cast<const float2*>(fmats),
+                    nullptr);
+  if (!rc) {
+    e = cudaMemsetAsync(lam, 0, sbytes, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "gbq_adjoint: cudaMemsetAsync");
+  }
+  if (!rc)
+    rc = gbq_sv_apply_paulisum(c, reinterpret_cast<const gbq_c64*>(psi), nq, terms, nterms,
+                               reinterpret_cast<gbq_c64*>(lam));
+  double ip[2] = {0.0, 0.0};
+  if (!rc) rc = gbq_sv_inner(c, reinterpret_cast<const gbq_c64*>(psi), reinterpret_cast<const gbq_c64*>(lam), nq, ip);
+  // reverse sweep: probes add Re<lam|D|psi> per slot
+  if (!rc && nrpasses)
+    rc = run_passes(c, psi, lam, nbits, rpasses, nrpasses, rops, nrops, reinterpret_cast<const float2*>(rmats),
+                    partial);
+  if (!rc && nslots) rc = do_reduce_slots(c, partial, nslots, ntiles, d_slots);
+  if (!rc && nslots) {
+    e = cudaMemcpyAsync(slot_values, d_slots, 8 * (size_t)nslots, cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "gbq_adjoint: cudaMemcpyAsync");
+  }
+  if (!rc) rc = sync(c, "gbq_adjoint");
+  release();
+  if (!rc) *value = ip[0];
+  return rc;
+}
+
 int gbq_reduce_slots(gbq_ctx* c, const double* partial, int nslots, int64_t ntiles, double* out) {
   CHECK_CTX(c);
   if (nslots <= 0) return GBQ_OK;

@@ -57,6 +57,7 @@ class PinnedArrayPool:
         self.lib = lib
         self.free: dict[int, list[int]] = {}
         self.lock = threading.Lock()
+        self.allocations = 0  # buffers pinned so far (each reuse avoids one)
 
     # pinning a large buffer costs far more than a garbage collection (0.5 s
     # for 8 GiB on a GB300 host, against tens of ms)
@@ -80,6 +81,7 @@ class PinnedArrayPool:
             hp = ctypes.c_void_p()
             check(self.lib.gbq_host_alloc(nbytes, ctypes.byref(hp)), "gbq_host_alloc")
             p = hp.value
+            self.allocations += 1
         raw = (ctypes.c_char * nbytes).from_address(p)
         arr = np.frombuffer(raw, dtype=dtype).reshape(shape)
         pool = self

@@ -837,7 +837,15 @@ class Simulator(
             return eng.new_state(n, basis=int(initial_state), nbits_dev=compiled.nbits_dev, into=into)
         if isinstance(initial_state, cirq.SimulationStateBase):
             raise NotImplementedError("unwrap SimulationState initial states first")
-        vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
+        if isinstance(initial_state, np.ndarray):
+            # taken as given, without the normalisation check, as the
+            # reference's _BufferedStateVector.create does
+            # (cirq-core/cirq/sim/state_vector_simulation_state.py:76-90)
+            vec = initial_state.reshape(-1).astype(np.complex64, copy=False)
+            if vec.size != 2**n:
+                raise ValueError(f"initial state has {vec.size} amplitudes, expected {2**n}")
+        else:
+            vec = cirq.to_valid_state_vector(initial_state, n, qid_shape=(2,) * n, dtype=np.complex64)
         return eng.new_state(n, initial=vec, nbits_dev=compiled.nbits_dev, into=into)
 
     def simulate_sweep_iter(

@@ -203,6 +203,22 @@ int gbq_run_dual(gbq_ctx* ctx, gbq_c64* psi, gbq_c64* lam, int nbits, const gbq_
                  int npasses, const gbq_op* ops, int nops, const gbq_c64* mats, double* partial);
 /* out[s] = sum_t partial[s * ntiles + t] for s < nslots (device arrays). */
 int gbq_reduce_slots(gbq_ctx* ctx, const double* partial, int nslots, int64_t ntiles, double* out);
+/* One-call adjoint gradient of <H> (no reference counterpart: the reference
+ * has no gradient code; its gradients come from parameter shift through
+ * Simulator.simulate_expectation_values, cirq-core/cirq/sim/sparse_simulator.py:193-218).
+ * Runs the forward program (fpasses/fops, matrices fmats on the device) on
+ * |0...0> of nbits bits (nq qubits; nbits > nq pads with |0> high bits),
+ * forms lam = H psi from the nterms Pauli terms (real coefficients) over the
+ * nq qubits, *value = <psi|H|psi>, then the two-state reverse program
+ * (rpasses/rops, device matrices rmats; every pass the same tile width),
+ * whose probe ops add Re<lam|D_s|psi> into slot s < nslots:
+ * slot_values[s] (host array) receives each slot's total.  A parameter's
+ * derivative is 2 x the sum of its slots.  Device buffers for psi, lam and
+ * the per-tile partial sums are allocated and freed by the call. */
+int gbq_adjoint(gbq_ctx* ctx, int nq, int nbits, const gbq_pass* fpasses, int nfpasses, const gbq_op* fops,
+                int nfops, const gbq_c64* fmats, const gbq_pauli* terms, int nterms, const gbq_pass* rpasses,
+                int nrpasses, const gbq_op* rops, int nrops, const gbq_c64* rmats, int nslots, double* value,
+                double* slot_values);
 
 /* Sum of |psi_i|^2 in double (host result).
  * Replaces np.linalg.norm in StateVectorTrialResult.final_state_vector

@@ -83,3 +83,22 @@ def test_parameter_shift_through_plain_simulator_matches():
     _, g = prog.value_and_grad(values)
     ps = adjoint.parameter_shift_gradient(cirq_gb300.Simulator(), circuit, ham, symbols, values, indices=range(8))
     np.testing.assert_allclose(g[:8], ps[:8], atol=TOL)
+
+
+def test_one_call_adjoint_entry_point_matches():
+    """gbq_adjoint (the whole gradient in one C-ABI call) against the
+    reference's parameter-shift gradient and the orchestrated path."""
+    circuit, symbols, _ = workloads.hea_circuit(5, 2, seed=9)
+    ham = workloads.random_pauli_hamiltonian(5, 12, seed=10)
+    values = GOLD["hea_n5_l2_values"]
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    E, g = prog.value_and_grad_native(values)
+    assert abs(E - float(GOLD["hea_n5_l2_energy"])) < TOL
+    np.testing.assert_allclose(g, GOLD["hea_n5_l2_grad_ps"], atol=TOL)
+    circuit, symbols, values = workloads.hea_circuit(14, 3, seed=14)
+    ham = workloads.random_pauli_hamiltonian(14, 40, seed=15)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    E1, g1 = prog.value_and_grad(values)
+    E2, g2 = prog.value_and_grad_native(values)
+    assert abs(E1 - E2) < 1e-6
+    np.testing.assert_allclose(g1, g2, atol=1e-6)

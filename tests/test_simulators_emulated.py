@@ -275,3 +275,19 @@ def test_simulate_of_untangled_circuits_beyond_the_device_state(emu):
     probs = np.abs(b0) ** 2
     i = int(np.argmax(probs))
     assert ((i >> 2) & 1) == m[0] and ((i >> 1) & 1) == m[0]
+
+
+def test_unnormalized_array_initial_state_is_taken_as_given(emu):
+    """An ndarray initial state is not validated (the reference's
+    _BufferedStateVector.create takes it as given); the final state keeps its
+    norm and simulate() warns, as the reference does, that it skips
+    renormalising."""
+    q = cirq.LineQubit.range(11)
+    c = workloads.random_layer_circuit(11, 3, seed=5)
+    init = np.zeros(2**11, dtype=np.complex64)
+    init[0] = 1.01
+    with pytest.warns(UserWarning, match="skipping renormalization"):
+        ref = cirq.Simulator(dtype=np.complex64).simulate(c, qubit_order=q, initial_state=init).final_state_vector
+    with pytest.warns(UserWarning, match="skipping renormalization"):
+        got = cirq_gb300.Simulator().simulate(c, qubit_order=q, initial_state=init).final_state_vector
+    np.testing.assert_allclose(got, ref, atol=1e-5)
