@@ -201,6 +201,7 @@ SIGNATURES = {
     "gbq_points_expect": [_P, _P, _I, _I, _P, _I, _P],
     "gbq_points_sample": [_P, _P, _I, _I, _P, _P],
     "gbq_points_rdm": [_P, _P, _I, _I, _I, _P, _P],
+    "gbq_points_dm_marginal": [_P, _P, _I, _I, _I, _I, _P, _P],
     "gbq_sv64_set_basis": [_P, _P, _I, _U64],
     "gbq_sv64_apply": [_P, _P, _I, _I, _P, _P],
     "gbq_sv64_compare": [_P, _P, _P, _I, _P],

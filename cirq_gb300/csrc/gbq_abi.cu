@@ -1112,6 +1112,25 @@ int gbq_points_rdm(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, in
   return sync(c, "gbq_points_rdm");
 }
 
+int gbq_points_dm_marginal(gbq_ctx* c, const gbq_c64* states, int nbits, int nq, int npoints, int m,
+                           const int* bits, double* out) {
+  CHECK_CTX(c);
+  if (!states || nq < 1 || 2 * nq > nbits || nbits > 34 || npoints < 1 || npoints > 65535 || m < 1 || m > 5 ||
+      !bits || !out)
+    return arg_fail("gbq_points_dm_marginal: bad arguments");
+  for (int j = 0; j < m; ++j)
+    if (bits[j] < 0 || bits[j] >= nq) return arg_fail("gbq_points_dm_marginal: bit out of range");
+  const size_t b = (size_t)npoints * (1u << m) * sizeof(double);
+  int rc = ensure_scratch(c, b);
+  if (rc) return rc;
+  double* d_out = reinterpret_cast<double*>(c->scratch);
+  rc = points_dm_marginal(c, reinterpret_cast<const float2*>(states), nbits, nq, npoints, m, bits, d_out);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(out, d_out, b, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(marginal)");
+  return sync(c, "gbq_points_dm_marginal");
+}
+
 int gbq_points_sample(gbq_ctx* c, const gbq_c64* states, int nbits, int npoints, const double* u,
                       uint64_t* out) {
   CHECK_CTX(c);

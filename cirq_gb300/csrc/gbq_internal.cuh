@@ -201,6 +201,8 @@ int build_tc_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInf
 int launch_tc_pass(Ctx* c, const TcArgs& a);
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
 int points_rdm(Ctx* c, const float2* states, int nbits, int npoints, int k, const int* g, double* d_out);
+int points_dm_marginal(Ctx* c, const float2* states, int nbits, int nq, int npoints, int m, const int* bits,
+                       double* d_out);
 int points_sample(Ctx* c, const float2* states, int nbits, int npoints, const double* d_u,
                   unsigned long long* d_out);
 int points_expect(Ctx* c, const float2* states, int nbits, int npoints, const gbq_pauli* d_terms, int nterms,

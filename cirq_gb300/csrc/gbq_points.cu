@@ -197,7 +197,52 @@ __global__ void __launch_bounds__(kPtThreads) k_points_rdm(const float2* __restr
     }
 }
 
+// Marginal distribution of m <= 5 measured qubits from the diagonal of every
+// point's density matrix: rho_p = the 2nq-bit vector of point p (stride
+// 2^nbits amplitudes; row index bits nq..2nq-1, column bits 0..nq-1), its
+// diagonal entries at i (2^nq + 1).  Block (chunk, point) bins Re rho_p[i, i]
+// of its share of the diagonal by the outcome sum_j bit(i, b_j) << j and adds
+// the bins to out[p * 2^m + outcome].
+__global__ void __launch_bounds__(kPtThreads) k_points_dm_marginal(const float2* __restrict__ states, int nbits,
+                                                                  int nq, int m, int4 b03, int b4, int chunk_bits,
+                                                                  double* __restrict__ out) {
+  __shared__ double bins[32];
+  const int p = blockIdx.y;
+  const int nb = 1 << m;
+  for (int j = threadIdx.x; j < nb; j += kPtThreads) bins[j] = 0.0;
+  __syncthreads();
+  const float2* rho = states + ((int64_t)p << nbits);
+  const uint64_t step = (1ull << nq) + 1ull;
+  const int bb[5] = {b03.x, b03.y, b03.z, b03.w, b4};
+  const uint64_t lo = (uint64_t)blockIdx.x << chunk_bits, hi = lo + (1ull << chunk_bits);
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kPtThreads) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      if (j < m) o |= (uint32_t)((i >> bb[j]) & 1ull) << j;
+    atomicAdd(&bins[o], (double)rho[i * step].x);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nb; j += kPtThreads) atomicAdd(out + (int64_t)p * nb + j, bins[j]);
+}
+
 }  // namespace
+
+int points_dm_marginal(Ctx* c, const float2* states, int nbits, int nq, int npoints, int m, const int* bits,
+                       double* d_out) {
+  cudaError_t e = cudaMemsetAsync(d_out, 0, (size_t)npoints * (1u << m) * sizeof(double), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(marginal out)");
+  const int chunk_bits = nq < 16 ? nq : 16;
+  dim3 grid((unsigned)(1u << (nq - chunk_bits)), (unsigned)npoints, 1);
+  int b[5] = {0, 0, 0, 0, 0};
+  for (int j = 0; j < m; ++j) b[j] = bits[j];
+  k_points_dm_marginal<<<grid, kPtThreads, 0, c->stream>>>(states, nbits, nq, m, make_int4(b[0], b[1], b[2], b[3]),
+                                                           b[4], chunk_bits, d_out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_points_dm_marginal launch");
+  c->launches += 1;
+  return GBQ_OK;
+}
 
 int points_rdm(Ctx* c, const float2* states, int nbits, int npoints, int k, const int* g, double* d_out) {
   const int D = 1 << k;

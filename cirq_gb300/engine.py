@@ -302,10 +302,19 @@ class Engine:
         return out
 
     def sample(self, state: DeviceBuffer, nbits: int, uniforms: np.ndarray, dm: bool = False) -> np.ndarray:
+        return self._sample_at(state.ptr, nbits, uniforms, dm)
+
+    def sample_point(self, states: DeviceBuffer, slot_bits: int, point: int, nbits: int, uniforms: np.ndarray,
+                     dm: bool = False) -> np.ndarray:
+        """sample() of point `point` of a batch of states in slots of
+        2^slot_bits amplitudes."""
+        return self._sample_at(states.ptr + point * (8 << slot_bits), nbits, uniforms, dm)
+
+    def _sample_at(self, ptr: int, nbits: int, uniforms: np.ndarray, dm: bool) -> np.ndarray:
         u = np.ascontiguousarray(uniforms, dtype=np.float64)
         out = np.empty(u.size, dtype=np.uint64)
         check(
-            self.lib.gbq_sample(self.ctx, state.ptr, nbits, int(dm), u.ctypes.data, u.size, out.ctypes.data),
+            self.lib.gbq_sample(self.ctx, ptr, nbits, int(dm), u.ctypes.data, u.size, out.ctypes.data),
             "gbq_sample",
         )
         return out
@@ -417,6 +426,17 @@ class Engine:
               "gbq_points_rdm")
         d = 1 << k
         return (out[0::2] + 1j * out[1::2]).reshape(npoints, d, d)
+
+    def points_dm_marginal(self, states, nbits: int, nq: int, npoints: int, bits) -> np.ndarray:
+        """(npoints, 2^m) outcome probabilities of the measured index bits
+        `bits` (bit j of the outcome <-> bits[j]) from the diagonals of npoints
+        density matrices of nq qubits (slots of 2^nbits amplitudes)."""
+        m = len(bits)
+        b = np.ascontiguousarray(bits, dtype=np.int32)
+        out = np.zeros(npoints << m, dtype=np.float64)
+        check(self.lib.gbq_points_dm_marginal(self.ctx, states.ptr, nbits, nq, npoints, m, b.ctypes.data,
+                                              out.ctypes.data), "gbq_points_dm_marginal")
+        return out.reshape(npoints, 1 << m)
 
     def points_sample(self, states: DeviceBuffer, nbits: int, npoints: int, uniforms: np.ndarray) -> np.ndarray:
         """One basis index per point, drawn from |psi_p|^2."""

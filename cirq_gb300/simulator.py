@@ -615,11 +615,13 @@ class _GpuSimulatorBase:
             if rec is not None:
                 return rec
         if self._traj_needed(circuit):
-            if not self._dm:
-                ops = _traj.circuit_ops(self, circuit, qubits, param_resolver)
+            ops = _traj.circuit_ops(self, circuit, qubits, param_resolver)
+            if self._dm:
+                rec = _traj.run_batched_dm(self, ops, qubits, param_resolver, repetitions)
+            else:
                 rec = _traj.run_batched(self, ops, qubits, param_resolver, repetitions)
-                if rec is not None:
-                    return rec
+            if rec is not None:
+                return rec
             per_rep = []
             for _, state, rec in self._traj_states(circuit, qubits, param_resolver, 0, repetitions,
                                                    records_only=True):

@@ -570,8 +570,8 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
     from cirq_gb300.engine import Engine
     from cirq_gb300.simulator import _recorded_in_place
 
-    if reps < 1:
-        return None
+    if reps < 1 or getattr(sim.planner, "tensor", False):
+        return None  # batched points run on the CUDA-core passes only
     ops = records_relevant(ops)
     items, _ = build_items(ops, dm=False)
     last_unitary = max((i for i, it in enumerate(items) if not isinstance(it, Measure)), default=-1)
@@ -710,6 +710,155 @@ def run_batched(sim, ops, qubits, resolver, reps: int):
             for key, v in term.items():
                 v8 = v.astype(np.uint8)
                 # a key measured mid-circuit and again at the end: more instances
+                out[key] = np.concatenate([out[key], v8], axis=1) if key in out else v8
+        return out
+    finally:
+        runner.close()
+
+
+def _dm_projector_program(sim, op_qubits, qubits):
+    """A one-slot program on the 2n-bit vector of a density matrix whose
+    matrix each trajectory supplies: it acts on the row bits and the column
+    bits of `op_qubits` (virtual qubit p <-> row bit of qubit p, virtual
+    qubit n + p <-> its column bit, so that position p owns index bit
+    2n-1-p).  Cached per simulator like slot_program."""
+    cache = sim.__dict__.setdefault("_slot_programs", {})
+    key = ("dm", tuple(op_qubits), tuple(qubits))
+    c = cache.get(key)
+    if c is None:
+        if len(cache) >= _MAX_SLOT_PROGRAMS:
+            cache.clear()
+        from cirq_gb300.planner import Planner
+        from cirq_gb300.program import CompiledCircuit
+
+        n = len(qubits)
+        vq = [cirq.NamedQubit(f"__dm_index_{i:04d}") for i in range(2 * n)]
+        pos = {q: i for i, q in enumerate(qubits)}
+        targets = [vq[pos[q]] for q in op_qubits] + [vq[n + pos[q]] for q in op_qubits]
+        op = cirq.IdentityGate(len(targets)).on(*targets)
+        c = CompiledCircuit([Slot(op, 0)], vq, dm=False, planner=Planner(tile_bits=12, kmax=4, budget=25.0),
+                            resolvers=[cirq.ParamResolver({})])
+        cache[key] = c
+    return c
+
+
+def run_batched_dm(sim, ops, qubits, resolver, reps: int):
+    """run() of a density-matrix circuit with mid-circuit measurements, all
+    repetitions at once: the repetitions' density matrices lie back to back as
+    batched points, each segment of channels and unitaries is one launch per
+    pass over all of them (gbq_run_points, the same matrices for every
+    point), and each mid-circuit measurement reads every point's outcome
+    distribution from the diagonal (gbq_points_dm_marginal), draws an outcome
+    per repetition on the host and applies P rho P / p as a one-slot pass with
+    per-repetition projectors -- the procedure of the reference's
+    measure_density_matrix (cirq-core/cirq/sim/density_matrix_utils.py:97-183)
+    in each trajectory of SimulatorBase._run
+    (cirq-core/cirq/sim/simulator_base.py:248-264).  Returns run() records, or
+    None when the circuit needs the one-at-a-time runner (classical control,
+    loops, a mid-circuit measurement of more than 2 qubits, tensor-core
+    plans)."""
+    from cirq_gb300.simulator import _recorded_in_place
+
+    if reps < 1 or getattr(sim.planner, "tensor", False):
+        return None
+    ops = records_relevant(ops)
+    items, _ = build_items(ops, dm=True)
+    last_unitary = max((i for i, it in enumerate(items) if not isinstance(it, Measure)), default=-1)
+    body = items[: last_unitary + 1]
+    terminal = [it.op for it in items[last_unitary + 1 :]]
+    for it in body:
+        if not isinstance(it, (Segment, Measure)):
+            return None
+        if isinstance(it, Measure) and (len(it.op.qubits) > 2 or any(q.dimension != 2 for q in it.op.qubits)):
+            return None
+    if not any(isinstance(it, Measure) for it in body):
+        return None  # nothing mid-circuit: the caller samples one final state
+    runner = TrajectoryRunner(sim, ops, qubits, resolver)
+    eng = sim.engine
+    prng = sim._prng
+    try:
+        n = runner.n
+        nb = runner.empty.nbits_dev  # bits of one density-matrix slot (2n, padded to >= 10)
+        _, free, _ = eng.device_info()
+        budget = max(1 << 28, min(int(free) // 2, 32 << 30))
+        chunk = max(1, min(reps, 65535, budget // (8 << nb), (1 << 24) >> max(nb - 10, 0)))
+        proj = {i: _dm_projector_program(sim, it.op.qubits, runner.qubits)
+                for i, it in enumerate(body) if isinstance(it, Measure)}
+        states = eng.alloc((8 << nb) * chunk)
+        records: list = [dict() for _ in range(reps)]
+        samples = np.zeros(reps, dtype=np.int64)
+        term_qubits = []
+        for op in terminal:
+            for q in op.qubits:
+                if q not in term_qubits:
+                    term_qubits.append(q)
+        try:
+            for start in range(0, reps, chunk):
+                k = min(chunk, reps - start)
+                eng.points_set_zero(states, nb, k)
+                for j, it in enumerate(body):
+                    if isinstance(it, Segment):
+                        c = runner.compiled[j]
+                        if not c.plan.npasses:
+                            continue
+                        pool_dev = eng.upload(np.ascontiguousarray(c.plan.pool, dtype=np.complex64))
+                        eng.run_points(states, nb, k, c.plan, pool_dev, 0)  # one pool for every point
+                        eng.sync()
+                        pool_dev.free()
+                        continue
+                    op = it.op
+                    qm = list(op.qubits)
+                    m = len(qm)
+                    bits = [n - 1 - runner.index[q] for q in qm]  # outcome bit j <-> qm[j]
+                    probs = np.clip(eng.points_dm_marginal(states, nb, n, k, bits), 0.0, None)
+                    cum = np.cumsum(probs, axis=1)
+                    u = prng.random_sample(k) * cum[:, -1]
+                    outcome = np.minimum((u[:, None] >= cum).sum(axis=1), (1 << m) - 1)
+                    p = np.maximum(probs[np.arange(k), outcome], 1e-30)
+                    d = 1 << m
+                    mats = np.zeros((k, d * d, d * d), dtype=np.complex128)
+                    for r in range(k):
+                        be = 0  # the outcome with qm[0] most significant, as the slot's matrix order
+                        for jq in range(m):
+                            be |= ((int(outcome[r]) >> jq) & 1) << (m - 1 - jq)
+                        mats[r, be * d + be, be * d + be] = 1.0 / p[r]
+                    c = proj[j]
+                    pool = np.ascontiguousarray(c.pool_from_batch({0: mats}, k), dtype=np.complex64)
+                    plen = pool.shape[1]
+                    if plen & 1:
+                        pool = np.concatenate([pool, np.zeros((k, 1), np.complex64)], axis=1)
+                        plen += 1
+                    pool_dev = eng.upload(pool.reshape(-1))
+                    eng.run_points(states, nb, k, c.plan, pool_dev, plen)
+                    eng.sync()
+                    pool_dev.free()
+                    key = cirq.measurement_key_name(op)
+                    raw = ((outcome[:, None] >> np.arange(m)[None, :]) & 1).astype(np.int8)
+                    rec = _recorded_in_place(raw, op, prng)
+                    for r in range(k):
+                        records[start + r].setdefault(key, []).append([int(b) for b in rec[r]])
+                if term_qubits:
+                    if len(term_qubits) <= 5:
+                        tb = [n - 1 - runner.index[q] for q in term_qubits]
+                        probs = np.clip(eng.points_dm_marginal(states, nb, n, k, tb), 0.0, None)
+                        cum = np.cumsum(probs, axis=1)
+                        u = prng.random_sample(k) * cum[:, -1]
+                        o = np.minimum((u[:, None] >= cum).sum(axis=1), (1 << len(tb)) - 1)
+                        idx = np.zeros(k, dtype=np.int64)
+                        for jq, b in enumerate(tb):
+                            idx |= ((o >> jq) & 1) << b
+                        samples[start : start + k] = idx
+                    else:
+                        for r in range(k):
+                            samples[start + r] = int(eng.sample_point(states, nb, r, n, prng.random_sample(1),
+                                                                      dm=True)[0])
+        finally:
+            states.free()
+        out = pad_records(records) if any(records) else {}
+        if terminal:
+            term = sim._records_from_samples(samples, runner.empty, terminal)
+            for key, v in term.items():
+                v8 = v.astype(np.uint8)
                 out[key] = np.concatenate([out[key], v8], axis=1) if key in out else v8
         return out
     finally:

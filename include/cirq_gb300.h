@@ -364,6 +364,17 @@ int gbq_points_sample(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoint
  * ||K psi||^2 of cirq-core/cirq/sim/state_vector_simulation_state.py:206-257). */
 int gbq_points_rdm(gbq_ctx* ctx, const gbq_c64* states, int nbits, int npoints, int k, const int* bits,
                    double* out);
+/* Marginal distribution of m <= 5 measured qubits for every point's density
+ * matrix: the states are npoints density matrices of nq qubits, each the
+ * 2nq-bit vector of the reference's (2,)*2nq tensor (index row * 2^nq + col)
+ * in a 2^nbits slot (nbits >= 2 nq).  out[p * 2^m + o] (host array) =
+ * sum of rho_p[i, i] over the row indices i whose bit bits[j] is bit j of o
+ * (bits[j] < nq: qubit position nq-1-bits[j]).  The outcome probabilities of
+ * a measurement in the reference's measure_density_matrix
+ * (cirq-core/cirq/sim/density_matrix_utils.py:97-183), for all trajectories
+ * of a batch at once; npoints <= 65535. */
+int gbq_points_dm_marginal(gbq_ctx* ctx, const gbq_c64* states, int nbits, int nq, int npoints, int m,
+                           const int* bits, double* out);
 
 #ifdef __cplusplus
 }

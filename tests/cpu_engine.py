@@ -122,7 +122,10 @@ class EmuEngine:
     def run_points(self, states, nbits, npoints, plan, pool_dev, pool_stride) -> None:
         size = 1 << nbits
         for p in range(npoints):
-            pool = _buf(pool_dev).arr[p * pool_stride : (p + 1) * pool_stride]
+            if pool_stride == 0:  # one pool for every point
+                pool = _buf(pool_dev).arr
+            else:
+                pool = _buf(pool_dev).arr[p * pool_stride : (p + 1) * pool_stride]
             _buf(states).arr[p * size : (p + 1) * size] = run_program(
                 _buf(states).arr[p * size : (p + 1) * size], nbits, plan.passes, plan.ops, pool
             )
@@ -212,6 +215,26 @@ class EmuEngine:
             sign = 1.0 - 2.0 * (np.bitwise_count(m & zy) & 1)
             out[t] = (1j**ny) * np.sum(sign * rho[m, m ^ x])  # Tr(P rho), P|m> = i^ny (-1)^{m.zy} |m^x>
         return out * coefs
+
+    def points_dm_marginal(self, states, nbits, nq, npoints, bits) -> np.ndarray:
+        """gbq_points_dm_marginal: outcome probabilities of the index bits
+        `bits` from the diagonals of npoints density matrices."""
+        size = 1 << nbits
+        i = np.arange(1 << nq, dtype=np.int64)
+        o = np.zeros_like(i)
+        for j, b in enumerate(bits):
+            o |= ((i >> b) & 1) << j
+        out = np.zeros((npoints, 1 << len(bits)))
+        for p in range(npoints):
+            diag = np.real(_buf(states).arr[p * size : (p + 1) * size][i * ((1 << nq) + 1)])
+            np.add.at(out[p], o, diag)
+        self._launches += 1
+        return out
+
+    def sample_point(self, states, slot_bits, point, nbits, uniforms, dm=False) -> np.ndarray:
+        size = 1 << slot_bits
+        view = EmuBuffer(8 * size, _buf(states).arr[point * size : (point + 1) * size])
+        return self.sample(view, nbits, uniforms, dm)
 
     def points_sample(self, states, nbits, npoints, uniforms) -> np.ndarray:
         from oracle.statevector import sample_from_probs

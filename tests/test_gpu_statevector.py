@@ -86,6 +86,22 @@ def test_cuda_graph_sweep_matches_plain_path():
     for a, b, d in zip(plain, graphed, again):
         np.testing.assert_allclose(a.final_state_vector, b.final_state_vector, atol=1e-6)
         np.testing.assert_allclose(a.final_state_vector, d.final_state_vector, atol=1e-6)
+    # and against the complex128 oracle, point by point
+    for r, b in zip(cirq.to_resolvers(pts), again):
+        assert np.max(np.abs(b.final_state_vector - simulate_state_vector(c, r))) < TOL
+
+
+def test_cuda_graph_sweep_vs_reference_golden():
+    """Graph replay over the reference's QAOA sweep (golden expectation values)."""
+    circuit, gammas, betas, obs, _ = workloads.qaoa_circuit(8, 4, seed=7)
+    pts = GOLD["qaoa_n8_p4_points"]
+    res = [cirq.ParamResolver({**dict(zip(gammas, p[:4])), **dict(zip(betas, p[4:]))}) for p in pts]
+    sim = cirq_gb300.Simulator(use_cuda_graphs=True)
+    for _ in range(2):  # capture, then replay
+        vals = sim.simulate_expectation_values_sweep(circuit, obs, res)
+        np.testing.assert_allclose(np.array([v[0] for v in vals]), GOLD["qaoa_n8_p4_expect"], atol=1e-4)
+    for r, tr in zip(res[:4], sim.simulate_sweep(circuit, res[:4])):
+        assert np.max(np.abs(tr.final_state_vector - simulate_state_vector(circuit, r))) < TOL
 
 
 def test_autotuned_simulator_matches_oracle(tmp_path, monkeypatch):

@@ -410,3 +410,39 @@ def test_repeat_until_loops_and_pauli_measurements(dm):
     bell = cirq.Circuit(cirq.H(q0), cirq.CNOT(q0, q1), pm("XZ", q0, q1))
     p = sim.run(bell, repetitions=4000).records["XZ"].mean()
     assert abs(p - 0.5) < 0.03
+
+
+def test_batched_density_matrix_trajectories_vs_reference_samples():
+    """run() of a density-matrix circuit with mid-circuit measurements: every
+    repetition's density matrix evolves as a batched point
+    (trajectories.run_batched_dm); records match the reference's in
+    distribution."""
+    import scipy.stats
+
+    from cirq_gb300 import trajectories as traj
+
+    q = cirq.LineQubit.range(5)
+    c = cirq.Circuit(
+        cirq.H(q[0]), cirq.CNOT(q[0], q[1]), cirq.ry(0.8).on(q[2]),
+        cirq.amplitude_damp(0.3).on(q[1]), cirq.depolarize(0.1).on(q[2]),
+        cirq.measure(q[1], key="a"),
+        cirq.CNOT(q[1], q[3]), cirq.H(q[2]), cirq.CZ(q[2], q[3]), cirq.CNOT(q[3], q[4]),
+        cirq.measure(q[2], q[3], key="b", invert_mask=(True, False)),
+        cirq.X(q[0]) ** 0.3, cirq.phase_damp(0.2).on(q[0]),
+        cirq.measure(*q, key="all"),
+    )
+    reps = 4000
+    sim = cirq_gb300.DensityMatrixSimulator(seed=3)
+    ops = traj.circuit_ops(sim, c, tuple(sorted(c.all_qubits())), cirq.ParamResolver({}))
+    assert traj.run_batched_dm(sim, ops, tuple(sorted(c.all_qubits())), cirq.ParamResolver({}), 4) is not None
+    ours = sim.run(c, repetitions=reps).records
+    ref = cirq.DensityMatrixSimulator(seed=4).run(c, repetitions=reps).records
+
+    def keys(rec):
+        flat = np.concatenate([rec[k][:, 0, :] for k in ("a", "b", "all")], axis=1).astype(np.int64)
+        return flat @ (1 << np.arange(flat.shape[1] - 1, -1, -1))
+
+    h1 = np.bincount(keys(ours), minlength=1 << 8)
+    h2 = np.bincount(keys(ref), minlength=1 << 8)
+    keep = (h1 + h2) > 0
+    assert scipy.stats.chi2_contingency(np.stack([h1[keep], h2[keep]]))[1] > 1e-4
