@@ -163,15 +163,21 @@ def device_steps(eng, compiled, steps: int, warmup: int, pass_timing: bool):
     for _ in range(warmup):
         one()
     eng.sync()
+    # steady state: the pass-specialised kernels queued by the first run are built
+    eng.jit_wait()
+    one()
+    eng.sync()
     if pass_timing:
         eng.set_pass_timing(True)
     l0 = eng.launches()
+    j0 = eng.jit_launches()
     eng.event(0)
     for _ in range(steps):
         one()
     eng.event(1)
     ms = eng.elapsed_ms(0, 1)
     launches = (eng.launches() - l0) / steps
+    device_steps.jit_launches_per_step = (eng.jit_launches() - j0) / steps
     pass_ms, pass_n = (0.0, 0)
     if pass_timing:
         pass_ms, pass_n = eng.pass_timing()
@@ -194,6 +200,7 @@ def e2e_steps(circuit, planner_kwargs, steps: int, warmup: int):
         # drop the result so that its pinned host buffer returns to the pool
         # (a user's loop that keeps no result reuses one buffer per call)
         del r, vec
+    sim.engine.jit_wait()
     times = []
     vec_bytes = 0
     for _ in range(steps):
@@ -215,8 +222,13 @@ def e2e_phases(circuit, planner_kwargs, repeats: int = 2):
     the compile cache), pool (the fused matrices of the point), passes (pool
     upload, basis state and every tile pass), renormalise (the final-state
     rule: a norm pass, and a scale pass when it applies), d2h (the state into
-    pinned host memory) and assemble (the cirq result object).  Returns
-    {"first": {...}, "cached": {...}} in seconds."""
+    pinned host memory; d2h_gc and d2h_pin are the parts of it spent in a
+    garbage collection that returned a buffer and in pinning a new one) and
+    assemble (the cirq result object).  Returns
+    {"first": {...}, "cached": {...}, "specialised_kernels_ready_s": T} in
+    seconds: the first call runs the interpreter while the pass-specialised
+    kernels of the circuit compile in the background (T after its start they
+    are all built); the cached calls run them."""
     cirq = _cirq()
     import cirq_gb300
     from cirq_gb300 import simulator as sim_mod
@@ -224,6 +236,7 @@ def e2e_phases(circuit, planner_kwargs, repeats: int = 2):
     sim = cirq_gb300.Simulator(**planner_kwargs)
     eng = sim.engine
     out = {}
+    t_first = time.perf_counter()
     for rep in range(repeats + 1):
         ph = {}
         t = time.perf_counter()
@@ -240,22 +253,29 @@ def e2e_phases(circuit, planner_kwargs, repeats: int = 2):
         sim_mod._final_renormalize(eng, state, compiled.n)
         eng.sync()
         ph["renormalise"] = time.perf_counter() - t
+        g0, p0 = eng.pinned.gc_seconds, eng.pinned.pin_seconds
         t = time.perf_counter()
         vec = eng.download_state(state, compiled.n)
         ph["d2h"] = time.perf_counter() - t
+        ph["d2h_gc"] = eng.pinned.gc_seconds - g0
+        ph["d2h_pin"] = eng.pinned.pin_seconds - p0
         state.free()
         t = time.perf_counter()
         res = sim_mod._state_vector_result(cirq.ParamResolver({}), {}, qubits, vec)
         ph["assemble"] = time.perf_counter() - t
-        ph["total"] = sum(ph.values())
+        ph["total"] = sum(v for k, v in ph.items() if k not in ("d2h_gc", "d2h_pin"))
         ph["pinned_allocations_so_far"] = eng.pinned.allocations
         del res, vec
         if rep == 0:
             out["first"] = ph
+            eng.jit_wait()
+            ready = time.perf_counter() - t_first
         else:
             prev = out.get("cached")
             out["cached"] = ph if prev is None or ph["total"] < prev["total"] else prev
-    return {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()} for k, v in out.items()}
+    res = {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()} for k, v in out.items()}
+    res["specialised_kernels_ready_s"] = round(ready, 3)
+    return res
 
 
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
@@ -703,6 +723,7 @@ def main():
     ap.add_argument("--kmax", type=int, default=4)
     ap.add_argument("--budget", type=float, default=25.0)
     ap.add_argument("--tensor-cores", type=int, default=0, help="plan tensor-core passes with this many MMA ops per pass")
+    ap.add_argument("--jit", type=int, default=None, help="pass-specialised kernels: 1 on, 0 off (default: library default)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -730,6 +751,8 @@ def main():
     from cirq_gb300.planner import Planner
 
     eng = Engine.get(local)
+    if args.jit is not None:
+        eng.set_jit(bool(args.jit))
     circuit, ngates = build_workload(args.n, args.depth, args.seed)
     if args.tensor_cores:
         planner = Planner(tensor=True, budget=args.tensor_cores)
@@ -742,6 +765,13 @@ def main():
     def barrier():
         if dist is not None:
             dist.barrier()
+
+    kw = dict(tile_bits=args.tile_bits, fusion_max_qubits=args.kmax, pass_budget=args.budget)
+    if args.tensor_cores:
+        kw = dict(tensor_cores=True, mma_ops_per_pass=args.tensor_cores)
+    # first: the per-phase breakdown, whose first call is the process's first
+    # sight of this circuit structure (no specialised kernel cached yet)
+    phases = e2e_phases(circuit, kw) if not args.no_e2e and rank == 0 else None
 
     barrier()
     with ClockSampler(local) as clocks:
@@ -756,7 +786,9 @@ def main():
     alg_bytes = 16 * (1 << compiled.nbits)
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9 if pass_ms else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "tile_ws_traffic.json")
+    jit_per_step = getattr(device_steps, "jit_launches_per_step", 0)
+    kernel = "k_jit (pass-specialised k_tile_ws)" if jit_per_step >= 0.5 * passes_per_step else "k_tile_ws"
+    tpath = os.path.join(ROOT, "profiles", "jit_pass_traffic.json" if kernel.startswith("k_jit") else "tile_ws_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
@@ -765,13 +797,10 @@ def main():
 
     e2e = None
     if not args.no_e2e and rank == 0:
-        kw = dict(tile_bits=args.tile_bits, fusion_max_qubits=args.kmax, pass_budget=args.budget)
-        if args.tensor_cores:
-            kw = dict(tensor_cores=True, mma_ops_per_pass=args.tensor_cores)
         e2e_s, h2d, d2h = e2e_steps(circuit, kw, steps=min(args.steps, 3), warmup=1)
         e2e = {"value": ngates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "s_per_step": e2e_s, "pinned_host_allocations": getattr(e2e_steps, "pinned_allocations", None),
-               "phases_s": e2e_phases(circuit, kw)}
+               "phases_s": phases}
 
     sweep = None
     if not args.no_sweep and rank == 0:
@@ -835,7 +864,7 @@ def main():
             },
             "hbm_frac": (achieved / peak) if achieved else None,
             "roofline": {
-                "kernel": "k_tile_ws",
+                "kernel": kernel,
                 "bound": "hbm",
                 "achieved": achieved,
                 "peak": peak,
@@ -848,6 +877,8 @@ def main():
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             },
             "gpu_launches": int(round(launches * args.steps)),
+            "specialised_passes": {"launches_per_step": jit_per_step, "kernels_compiled": eng.jit_compiles(),
+                                   "mode": 0 if args.jit == 0 else (args.jit or 2)},
             "clocks": clocks.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,

@@ -132,7 +132,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(sources())) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = out + ".tmp"
-    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
@@ -163,6 +163,10 @@ SIGNATURES = {
     "gbq_ctx_sync": [_P],
     "gbq_device_info": [_P, _P, _P, _P],
     "gbq_set_graphs": [_P, _I],
+    "gbq_set_jit": [_P, _I],
+    "gbq_jit_stats": [_P, _P, _P],
+    "gbq_jit_source": [_I, _P, _P, _I, _P, _SZ, _P],
+    "gbq_jit_compile_check": [ctypes.c_char_p, _P],
     "gbq_device_name": [_P, _P, _I],
     "gbq_launch_count": [_P, _P],
     "gbq_event_record": [_P, _I],

@@ -8,6 +8,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -397,6 +398,24 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
   PassArgs a;
   MmaArgs ma;
   TcArgs ta;
+  // pass-specialised kernels: queue the new ones of this program (compiled
+  // in parallel by worker threads); mode 1 waits for them
+  // background mode only for states of >= kJitAutoMinBits bits: below, a
+  // pass takes microseconds and the interpreter is as fast
+  const bool jit = !dual && jit_enabled(c) && (c->jit == 1 || nbits >= kJitAutoMinBits);
+  if (jit) {
+    std::vector<std::pair<std::string, PassArgs*>> todo;
+    int rc = GBQ_OK;
+    for (int q = 0; q < npasses && !rc; ++q) {
+      int mma = 0;
+      rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, ta, mma);
+      if (rc || mma || !jit_eligible(a)) continue;
+      todo.emplace_back(jit_key(a, c), new PassArgs(a));
+    }
+    if (!rc) jit_prepare(c, todo, c->jit == 1);
+    for (auto& t : todo) delete t.second;
+    if (rc) return rc;
+  }
   for (int q = 0; q < npasses; ++q) {
     int mma = 0;
     int rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, ta, mma);
@@ -424,7 +443,9 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
       ma.abort = c->d_abort;
       rc = launch_mma_pass(c, ma);
     } else {
-      rc = launch_pass(c, a, dual);
+      bool launched = false;
+      if (jit && jit_eligible(a)) rc = jit_launch(c, a, jit_key(a, c), launched);
+      if (!rc && !launched) rc = launch_pass(c, a, dual);
     }
     if (rc) return rc;
     if (c->pass_timing) {
@@ -543,6 +564,46 @@ int gbq_set_graphs(gbq_ctx* c, int enable) {
   return GBQ_OK;
 }
 
+int gbq_set_jit(gbq_ctx* c, int mode) {
+  if (!c) return arg_fail("null context");
+  if (mode < 0 || mode > 2) return arg_fail("gbq_set_jit: mode must be 0, 1 or 2");
+  c->jit = mode;
+  return GBQ_OK;
+}
+
+int gbq_jit_stats(int64_t* compiles, int64_t* pending, int64_t* launches) {
+  if (!compiles) return arg_fail("null argument");
+  *compiles = jit_compile_count();
+  if (pending) *pending = jit_pending();
+  if (launches) *launches = jit_launch_count();
+  return GBQ_OK;
+}
+
+int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, char* buf, size_t len,
+                   size_t* needed) {
+  if (!pass || !ops || !needed) return arg_fail("gbq_jit_source: null argument");
+  PassArgs* a = new PassArgs();
+  MmaArgs* ma = new MmaArgs();
+  TcArgs* ta = new TcArgs();
+  int mma = 0;
+  int rc = convert_pass(*pass, ops, nops, nbits, false, *a, *ma, *ta, mma);
+  if (!rc && (mma || !jit_eligible(*a))) rc = GBQ_ERR_UNSUPPORTED;
+  if (rc == GBQ_ERR_UNSUPPORTED) set_error("gbq_jit_source: the pass has no specialised form");
+  if (!rc) {
+    const std::string src = jit_source(*a);
+    *needed = src.size() + 1;
+    if (buf && len) {
+      const size_t n = std::min(len - 1, src.size());
+      memcpy(buf, src.data(), n);
+      buf[n] = '\0';
+    }
+  }
+  delete a;
+  delete ma;
+  delete ta;
+  return rc;
+}
+
 int gbq_launch_count(gbq_ctx* c, int64_t* out) {
   if (!c || !out) return arg_fail("null argument");
   *out = c->launches;
@@ -623,7 +684,8 @@ int gbq_free(gbq_ctx* c, void* dptr) {
 
 int gbq_host_alloc(size_t bytes, void** hptr) {
   if (!hptr) return arg_fail("null output pointer");
-  cudaError_t e = cudaMallocHost(hptr, bytes ? bytes : 16);
+  const size_t n = bytes ? bytes : 16;
+  cudaError_t e = cudaMallocHost(hptr, n);
   if (e != cudaSuccess) {
     *hptr = nullptr;
     return cuda_fail(e, "cudaMallocHost");

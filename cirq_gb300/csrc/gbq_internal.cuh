@@ -178,6 +178,10 @@ struct Ctx {
   int64_t timed_launches = 0;
   int* d_abort = nullptr;  // device flag set by a pass that gave up a bounded wait
   bool abort_armed = false;  // a kernel that can set d_abort has been launched
+  // pass-specialised kernels: 0 off, 1 compiled before a program's first
+  // launch, 2 compiled in the background (the interpreter runs passes whose
+  // kernel is not ready); -1 not decided yet (environment variable GBQ_JIT)
+  int jit = -1;
 };
 
 int ensure_scratch(Ctx* c, size_t bytes);
@@ -200,6 +204,17 @@ int build_tc_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInf
                   TcArgs& A);
 int launch_tc_pass(Ctx* c, const TcArgs& a);
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
+// Pass-specialised kernels (gbq_jit.cu).
+constexpr int kJitAutoMinBits = 20;
+bool jit_enabled(Ctx* c);
+bool jit_eligible(const PassArgs& a);
+std::string jit_key(const PassArgs& a, const Ctx* c);
+std::string jit_source(const PassArgs& a);
+void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes, bool wait);
+int jit_launch(Ctx* c, const PassArgs& a, const std::string& key, bool& launched);
+int64_t jit_compile_count();
+int64_t jit_launch_count();
+int64_t jit_pending();
 int points_rdm(Ctx* c, const float2* states, int nbits, int npoints, int k, const int* g, double* d_out);
 int points_dm_marginal(Ctx* c, const float2* states, int nbits, int nq, int npoints, int m, const int* bits,
                        double* d_out);

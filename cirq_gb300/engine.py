@@ -11,6 +11,7 @@ import ctypes
 import gc
 import os
 import threading
+import time
 import weakref
 
 import numpy as np
@@ -58,6 +59,8 @@ class PinnedArrayPool:
         self.free: dict[int, list[int]] = {}
         self.lock = threading.Lock()
         self.allocations = 0  # buffers pinned so far (each reuse avoids one)
+        self.gc_seconds = 0.0  # spent in collections that returned a buffer
+        self.pin_seconds = 0.0  # spent pinning new buffers
 
     # pinning a large buffer costs far more than a garbage collection (0.5 s
     # for 8 GiB on a GB300 host, against tens of ms)
@@ -75,13 +78,17 @@ class PinnedArrayPool:
         if p is None and nbytes >= self.GC_BYTES:
             # results that the caller dropped but that still sit in reference
             # cycles (cirq result objects) return their buffers here
+            t = time.perf_counter()
             gc.collect()
+            self.gc_seconds += time.perf_counter() - t
             p = self._take(nbytes)
         if p is None:
+            t = time.perf_counter()
             hp = ctypes.c_void_p()
             check(self.lib.gbq_host_alloc(nbytes, ctypes.byref(hp)), "gbq_host_alloc")
             p = hp.value
             self.allocations += 1
+            self.pin_seconds += time.perf_counter() - t
         raw = (ctypes.c_char * nbytes).from_address(p)
         arr = np.frombuffer(raw, dtype=dtype).reshape(shape)
         pool = self
@@ -179,6 +186,41 @@ class Engine:
         v = ctypes.c_float()
         check(self.lib.gbq_event_elapsed(self.ctx, a, b, ctypes.byref(v)), "gbq_event_elapsed")
         return v.value
+
+    def set_jit(self, mode: int | bool) -> None:
+        """Pass-specialised kernels for this engine's passes: 0 (or False)
+        off, 1 (or True) compiled before a program's first launch, 2 compiled
+        in the background while the interpreter runs."""
+        check(self.lib.gbq_set_jit(self.ctx, int(mode)), "gbq_set_jit")
+
+    def jit_compiles(self) -> int:
+        """Specialised kernels compiled by this process so far."""
+        v = ctypes.c_int64()
+        check(self.lib.gbq_jit_stats(ctypes.byref(v), None, None), "gbq_jit_stats")
+        return v.value
+
+    def jit_launches(self) -> int:
+        """Launches of specialised kernels by this process so far."""
+        v, n = ctypes.c_int64(), ctypes.c_int64()
+        check(self.lib.gbq_jit_stats(ctypes.byref(v), None, ctypes.byref(n)), "gbq_jit_stats")
+        return n.value
+
+    def jit_pending(self) -> int:
+        """Specialised kernels queued or being compiled now."""
+        v, p = ctypes.c_int64(), ctypes.c_int64()
+        check(self.lib.gbq_jit_stats(ctypes.byref(v), ctypes.byref(p), None), "gbq_jit_stats")
+        return p.value
+
+    def jit_wait(self, timeout_s: float = 300.0) -> bool:
+        """Waits until no specialised kernel is being compiled; False on timeout."""
+        import time
+
+        end = time.monotonic() + timeout_s
+        while self.jit_pending():
+            if time.monotonic() > end:
+                return False
+            time.sleep(0.01)
+        return True
 
     def set_pass_timing(self, enable: bool) -> None:
         check(self.lib.gbq_set_pass_timing(self.ctx, int(enable)), "gbq_set_pass_timing")

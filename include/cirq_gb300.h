@@ -139,6 +139,32 @@ int gbq_set_graphs(gbq_ctx* ctx, int enable);
 int gbq_device_name(gbq_ctx* ctx, char* buf, int len);
 /* Number of kernels this context has launched (for launch accounting). */
 int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
+
+/* Pass-specialised kernels.  Every single-state pass of 12-bit tiles whose
+ * ops are register layouts, register dense ops of width <= 2 and register
+ * diagonals can run a kernel generated for its op records and compiled at
+ * run time with NVRTC (cached per op-record sequence and device; worker
+ * threads compile the new passes of a program in parallel).  The generated
+ * kernel computes exactly what the interpreter computes, in the same order,
+ * so results are bit-identical whichever kernel runs a pass.
+ * mode 0: off.  mode 1: a program's new kernels are compiled before its
+ * first launch.  mode 2: they are compiled in the background and the
+ * interpreter runs each pass until its kernel is ready (states of 20 or
+ * more bits only; smaller passes take microseconds).  Default: the value of
+ * the environment variable GBQ_JIT, else 2. */
+int gbq_set_jit(gbq_ctx* ctx, int mode);
+/* Specialised kernels compiled by this process so far and (optional) those
+ * queued or being compiled now, and the launches of specialised kernels. */
+int gbq_jit_stats(int64_t* compiles, int64_t* pending, int64_t* launches);
+/* The generated CUDA source of one pass (test and inspection hook; no GPU
+ * needed).  *needed receives the size including the terminating zero;
+ * GBQ_ERR_UNSUPPORTED if the pass has no specialised form. */
+int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, char* buf, size_t len,
+                   size_t* needed);
+/* Compiles a source with NVRTC for sm_103a (no GPU needed); *cubin_bytes
+ * receives the size of the result.  GBQ_ERR_UNSUPPORTED with the compiler
+ * log as the error message if it does not compile or NVRTC is absent. */
+int gbq_jit_compile_check(const char* src, size_t* cubin_bytes);
 /* Stream-ordered timing: records CUDA event `slot` (0..15) on the context's
  * stream; gbq_event_elapsed waits for event b and returns the ms from a to b. */
 int gbq_event_record(gbq_ctx* ctx, int slot);

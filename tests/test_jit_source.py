@@ -1,0 +1,63 @@
+"""Generated sources of pass-specialised kernels compile for sm_103a (NVRTC,
+no GPU needed) and passes without a specialised form are refused."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from cirq_gb300 import _lib, workloads
+from cirq_gb300.planner import Planner
+from cirq_gb300.program import CompiledCircuit, split_measurements
+
+import cirq
+
+
+def _plan(n, depth):
+    c = workloads.random_layer_circuit(n, depth, 1)
+    body, _ = split_measurements(c)
+    cc = CompiledCircuit(body, sorted(c.all_qubits()), dm=False, planner=Planner(budget=25.0),
+                         resolvers=[cirq.ParamResolver({})])
+    return cc.nbits_dev, cc.plan
+
+
+def _source(lib, nbits, plan, q):
+    passes = np.ascontiguousarray(plan.passes)
+    ops = np.ascontiguousarray(plan.ops)
+    need = ctypes.c_size_t(0)
+    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), None, 0,
+                            ctypes.byref(need))
+    if rc:
+        return rc, None
+    buf = ctypes.create_string_buffer(need.value)
+    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), buf, need.value,
+                            ctypes.byref(need))
+    return rc, buf.value
+
+
+def test_generated_pass_compiles():
+    lib = _lib.load()
+    nbits, plan = _plan(18, 8)
+    rc, src = _source(lib, nbits, plan, 0)
+    assert rc == 0
+    assert b"k_jit" in src and b"rdense<" in src
+    size = ctypes.c_size_t(0)
+    rc = lib.gbq_jit_compile_check(src, ctypes.byref(size))
+    if rc == _lib.ERR_UNSUPPORTED and b"not found" in lib.gbq_last_error():
+        pytest.skip("NVRTC is not installed")
+    assert rc == 0, lib.gbq_last_error().decode()[:2000]
+    assert size.value > 1000
+
+
+def test_pass_without_specialised_form_is_refused():
+    lib = _lib.load()
+    # a shared-memory dense op (width 3) has no specialised form
+    passes = np.zeros(1, dtype=_lib.PASS_DTYPE)
+    passes[0]["L"], passes[0]["m"], passes[0]["op_begin"], passes[0]["op_count"] = 12, 5, 0, 1
+    passes[0]["hi"][:7] = np.arange(5, 12)
+    ops = np.zeros(1, dtype=_lib.OP_DTYPE)
+    ops[0]["kind"], ops[0]["k"] = _lib.OP_DENSE, 3
+    ops[0]["bits"][:3] = [0, 1, 2]
+    need = ctypes.c_size_t(0)
+    rc = lib.gbq_jit_source(12, passes.ctypes.data, ops.ctypes.data, 1, None, 0, ctypes.byref(need))
+    assert rc == _lib.ERR_UNSUPPORTED
