@@ -559,6 +559,79 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
     }
 
 
+def clifford_bench(n: int = 500, depth: int = 100, shots: int = 1_000_000, ref_shots: int = 3):
+    """Clifford sampling: a random Clifford circuit of n qubits and depth
+    layers with a mid-circuit measurement and reset every layer, depolarizing
+    noise and a final measurement of every qubit, sampled `shots` times by
+    Pauli frames on the GPU; the reference's cirq.StabilizerSampler (one
+    tableau run per repetition) is timed on `ref_shots` repetitions.
+    Frame-kernel bytes: per op and 32 shots, the frame and record words it
+    reads and writes (4 B each)."""
+    cirq = _cirq()
+    from cirq_gb300 import clifford as C, workloads
+    from cirq_gb300.engine import Engine
+    from cirq_gb300 import _lib as L
+
+    eng = Engine.get(0)
+    c = workloads.random_clifford_circuit(n, depth, 0, mid_measure=1.0, resets=True, p=1e-3)
+    q = sorted(c.all_qubits())
+    t = time.perf_counter()
+    prog = C.CliffordProgram(c, q)
+    compile_s = time.perf_counter() - t
+    t = time.perf_counter()
+    prog.reference(eng)
+    reference_s = time.perf_counter() - t
+    nw = (shots + 31) // 32
+    words = 2 * n  # frame initialisation
+    for op in prog.ops:
+        kind, k = int(op["kind"]), int(op["k"])
+        words += {L.CLIFF_UNITARY: 4 * k, L.CLIFF_MEASURE: 4, L.CLIFF_RESET: 2, L.CLIFF_NOISE: 4,
+                  L.CLIFF_COND_PAULI: 2 * k + int(op["cond_count"])}[kind]
+    alg_bytes = words * 4 * nw
+    prog.sample_records(eng, 4096, 1)  # warm-up
+    dev = []
+    wall = []
+    for rep in range(3):
+        eng.set_pass_timing(True)
+        t = time.perf_counter()
+        prog.sample_records(eng, shots, 100 + rep)
+        wall.append(time.perf_counter() - t)
+        ms, nlaunch = eng.pass_timing()
+        eng.set_pass_timing(False)
+        dev.append(ms)
+    t = time.perf_counter()
+    res = C.StabilizerSampler(seed=5).run(c, repetitions=shots)
+    api_s = time.perf_counter() - t
+    t = time.perf_counter()
+    cirq.StabilizerSampler(seed=5).run(c, repetitions=ref_shots)
+    ref_s = (time.perf_counter() - t) / ref_shots
+    peak, _ = peaks()
+    dev_s = min(dev) / 1e3
+    return {
+        "workload": f"random Clifford circuit {n}q depth {depth}, a measurement + reset per layer, "
+                    f"depolarize(1e-3), {prog.nrec} records, {len(prog.ops)} ops",
+        "shots": shots,
+        "shots_per_s_device": shots / dev_s,
+        "shots_per_s_api": shots / api_s,
+        "api_s": api_s,
+        "device_ms": min(dev),
+        "device_ms_note": "the frame kernel alone (CUDA events around its launch)",
+        "wall_s_sample_records": min(wall),
+        "wall_note": "one gbq_cliff_sample call: uploads, reference records, frame kernel, on-device transpose "
+                     "to shot-major bytes and their download",
+        "compile_s": compile_s,
+        "reference_run_s": reference_s,
+        "frame_bytes": alg_bytes,
+        "frame_gbs_of_device_time": alg_bytes / dev_s / 1e9,
+        "frame_hbm_frac": alg_bytes / dev_s / 1e9 / peak,
+        "frame_note": "frames + records are 2*n*nw + nrec*nw words; at these sizes much of the traffic stays in L2",
+        "reference_shots_per_s": 1.0 / ref_s,
+        "reference_sample": f"cirq.StabilizerSampler, {ref_shots} repetitions",
+        "speedup_api_vs_reference": (shots / api_s) * ref_s,
+        "result_shape": list(res.measurements["m"].shape),
+    }
+
+
 def c1_bench(n: int = 20, depth: int = 20, reps: int = 10_000, calls: int = 5):
     """The CPU-runnable configuration: 20 qubits, depth 20 (590 gates).
     simulate() latency (first call, with planning, and cached) and
@@ -828,7 +901,7 @@ def main():
     extra = {}
     if not args.no_extra and rank == 0:
         for name, fn in (("c1_20q", c1_bench), ("adjoint", adjoint_bench), ("density_matrix", density_bench),
-                         ("batch_sweep", batch_bench),
+                         ("batch_sweep", batch_bench), ("clifford_sampling", clifford_bench),
                          ("width_33", width33_bench), ("tensor_core_pipelined", tc_bench),
                          ("tensor_core_pass_11bit", mma_bench)):
             try:

@@ -48,6 +48,21 @@ PASS_DTYPE = np.dtype(
     [("L", "i4"), ("m", "i4"), ("op_begin", "i4"), ("op_count", "i4"), ("hi", "i1", (16,))],
     align=True,
 )
+CLIFF_OP_DTYPE = np.dtype(
+    [
+        ("kind", "i1"),
+        ("k", "i1"),
+        ("lin", "i1", (6,)),
+        ("q", "i4", (3,)),
+        ("tab", "i4"),
+        ("rec", "i4"),
+        ("cond_begin", "i4"),
+        ("cond_count", "i4"),
+        ("p", "f4", (3,)),
+    ],
+    align=True,
+)
+CLIFF_UNITARY, CLIFF_MEASURE, CLIFF_RESET, CLIFF_NOISE, CLIFF_COND_PAULI = 0, 1, 2, 3, 4
 PAULI_DTYPE = np.dtype(
     [("x", "u8"), ("zy", "u8"), ("ny", "i4"), ("pad", "i4"), ("coef", "f8")], align=True
 )
@@ -164,6 +179,9 @@ SIGNATURES = {
     "gbq_device_info": [_P, _P, _P, _P],
     "gbq_set_graphs": [_P, _I],
     "gbq_set_jit": [_P, _I],
+    "gbq_cliff_validate": [_I, _P, _I, _I, _I, _I],
+    "gbq_cliff_reference": [_P, _I, _P, _I, _P, _I, _P, _I, _I, _P],
+    "gbq_cliff_sample": [_P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _I64, _U64, _P, _P, _I, _I],
     "gbq_jit_stats": [_P, _P, _P],
     "gbq_jit_source": [_I, _P, _P, _I, _P, _SZ, _P],
     "gbq_jit_compile_check": [ctypes.c_char_p, _P],

@@ -564,6 +564,60 @@ int gbq_set_graphs(gbq_ctx* c, int enable) {
   return GBQ_OK;
 }
 
+int gbq_cliff_validate(int nq, const gbq_cliff_op* ops, int nops, int ntables, int nconds, int nrec) {
+  if (nq < 1 || nq > (1 << 20) || nops < 0 || (nops && !ops) || ntables < 0 || nconds < 0 || nrec < 0)
+    return arg_fail("gbq_cliff_validate: bad sizes");
+  if (cliff_check(nq, ops, nops, ntables, nconds, nrec)) return arg_fail("gbq_cliff_validate: invalid op");
+  return GBQ_OK;
+}
+
+int gbq_cliff_reference(gbq_ctx* c, int nq, const gbq_cliff_op* ops, int nops, const uint32_t* tables,
+                        int ntables, const int32_t* conds, int nconds, int nrec, uint8_t* ref_out) {
+  CHECK_CTX(c);
+  int rc = gbq_cliff_validate(nq, ops, nops, ntables, nconds, nrec);
+  if (rc) return rc;
+  if ((ntables && !tables) || (nconds && !conds) || (nrec && !ref_out)) return arg_fail("gbq_cliff_reference: null array");
+  for (int i = 0; i < nconds; ++i)
+    if (conds[i] < 0 || conds[i] >= nrec) return arg_fail("gbq_cliff_reference: condition record out of range");
+  return cliff_reference(c, nq, ops, nops, tables, ntables, conds, nconds, nrec, ref_out);
+}
+
+int gbq_cliff_sample(gbq_ctx* c, int nq, const gbq_cliff_op* ops, int nops, const uint32_t* tables, int ntables,
+                     const int32_t* conds, int nconds, const uint8_t* ref, int nrec, int64_t shots, uint64_t seed,
+                     void* out, const int32_t* layers, int nlayers, int out_bytes) {
+  CHECK_CTX(c);
+  int rc = gbq_cliff_validate(nq, ops, nops, ntables, nconds, nrec);
+  if (rc) return rc;
+  if (shots < 1 || shots > ((int64_t)1 << 40)) return arg_fail("gbq_cliff_sample: shots out of range");
+  if (out_bytes && nrec > (1 << 21)) return arg_fail("gbq_cliff_sample: byte output takes at most 2^21 records");
+  if ((nconds && !conds) || (nrec && (!ref || !out))) return arg_fail("gbq_cliff_sample: null array");
+  for (int i = 0; i < nconds; ++i)
+    if (conds[i] < 0 || conds[i] >= nrec) return arg_fail("gbq_cliff_sample: condition record out of range");
+  (void)tables;
+  if (layers) {
+    if (nlayers < 0 || layers[0] != 0 || layers[nlayers] != nops) return arg_fail("gbq_cliff_sample: bad layers");
+    std::vector<int> last(nq, -1), rec_layer(nrec, INT32_MAX);
+    for (int L = 0; L < nlayers; ++L) {
+      if (layers[L + 1] < layers[L]) return arg_fail("gbq_cliff_sample: layers must not decrease");
+      for (int o = layers[L]; o < layers[L + 1]; ++o) {
+        const gbq_cliff_op& op = ops[o];
+        if (op.kind == GBQ_CLIFF_MEASURE) rec_layer[op.rec] = L;
+        if (op.kind == GBQ_CLIFF_COND_PAULI)
+          for (int i = 0; i < op.cond_count; ++i)
+            if (rec_layer[conds[op.cond_begin + i]] >= L)
+              return arg_fail("gbq_cliff_sample: a condition must come after its measurement's layer");
+        const int k = (op.kind == GBQ_CLIFF_UNITARY || op.kind == GBQ_CLIFF_COND_PAULI) ? op.k : 1;
+        for (int j = 0; j < k; ++j) {
+          if (last[op.q[j]] == L) return arg_fail("gbq_cliff_sample: a layer acts twice on one qubit");
+          last[op.q[j]] = L;
+        }
+      }
+    }
+  }
+  return cliff_sample(c, nq, ops, nops, conds, nconds, ref, nrec, shots, seed, out, layers, layers ? nlayers : 0,
+                      out_bytes != 0);
+}
+
 int gbq_set_jit(gbq_ctx* c, int mode) {
   if (!c) return arg_fail("null context");
   if (mode < 0 || mode > 2) return arg_fail("gbq_set_jit: mode must be 0, 1 or 2");

@@ -204,6 +204,14 @@ int build_tc_args(const gbq_pass& p, const gbq_op* ops, int nbits, const TileInf
                   TcArgs& A);
 int launch_tc_pass(Ctx* c, const TcArgs& a);
 int points_set_zero(Ctx* c, float2* states, int nbits, int npoints);
+// Clifford circuits (gbq_clifford.cu).
+int cliff_reference(Ctx* c, int nq, const gbq_cliff_op* ops, int nops, const uint32_t* tables, int ntables,
+                    const int32_t* conds, int nconds, int nrec, uint8_t* ref_out);
+int cliff_sample(Ctx* c, int nq, const gbq_cliff_op* ops, int nops, const int32_t* conds, int nconds,
+                 const uint8_t* ref, int nrec, int64_t shots, uint64_t seed, void* out,
+                 const int32_t* layers, int nlayers, int out_bytes);
+int cliff_check(int nq, const gbq_cliff_op* ops, int nops, int ntables, int nconds, int nrec);
+
 // Pass-specialised kernels (gbq_jit.cu).
 constexpr int kJitAutoMinBits = 20;
 bool jit_enabled(Ctx* c);

@@ -7,10 +7,12 @@ functions here keep their signatures, argument checks and error messages and
 run on :class:`cirq_gb300.Simulator` / :class:`cirq_gb300.DensityMatrixSimulator`
 instead.  Choices of simulator:
 
-* ``sample``: a noiseless circuit runs on the state-vector simulator
-  (mid-circuit measurements as trajectories); the reference sends Clifford
-  circuits to its tableau simulator and other measured circuits to the
-  density-matrix simulator.  The sample distribution is the same.
+* ``sample``: a noiseless Clifford circuit samples by Pauli frames on the GPU
+  (:class:`cirq_gb300.clifford.CliffordSimulator`), as the reference sends it
+  to its tableau simulator; another noiseless circuit runs on the
+  state-vector simulator (mid-circuit measurements as trajectories) where the
+  reference uses the density-matrix simulator.  The sample distribution is
+  the same.
   A noisy circuit runs on the density-matrix simulator up to
   ``DM_MAX_QUBITS`` qubits, as in the reference, and above that (where a
   density matrix does not fit) as state-vector trajectories of the circuit
@@ -57,6 +59,11 @@ def _dm_sim(dtype, seed, noise=None):
     return DensityMatrixSimulator(dtype=dtype, seed=seed, noise=noise)
 
 
+def _is_clifford_circuit(program) -> bool:
+    """mux.py:336-339: every non-measurement operation has a stabilizer effect."""
+    return all(cirq.has_stabilizer_effect(op) for op in program.all_operations() if not cirq.is_measurement(op))
+
+
 def _to_circuit(program) -> cirq.Circuit:
     """Circuit, gate or OP_TREE -> Circuit (mux.py:97-106)."""
     if isinstance(program, cirq.Circuit):
@@ -78,6 +85,12 @@ def sample(
     """Samples the circuit's measurements (``cirq.sample``, mux.py:53-94)."""
     noise_model = cirq.NoiseModel.from_noise_model_like(noise)
     if noise_model == cirq.NO_NOISE:
+        if _is_clifford_circuit(program):
+            # as the reference (mux.py:81-86): Clifford circuits sample on the
+            # stabilizer path, here Pauli frames on the GPU
+            from cirq_gb300.clifford import CliffordSimulator
+
+            return CliffordSimulator(seed=seed).run(program, param_resolver=param_resolver, repetitions=repetitions)
         return _sv_sim(dtype, seed).run(program, param_resolver=param_resolver, repetitions=repetitions)
     dm = _dm_sim(dtype, seed, noise_model)
     if _state_bits(program.all_qubits()) <= DM_MAX_QUBITS:

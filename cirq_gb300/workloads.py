@@ -15,6 +15,14 @@ All generators are deterministic in ``seed`` (``numpy.random.RandomState``).
 * ``hea_circuit`` -- hardware-efficient ansatz: per layer ``rx(theta)``,
   ``rz(theta)`` on every qubit then a CZ ladder; Hamiltonian of random Pauli
   strings of weight 2..4 with N(0, 1) coefficients.
+* ``random_clifford_circuit`` -- n qubits, depth d: each layer a random
+  single-qubit Clifford (one of the 24, as a ``SingleQubitCliffordGate``) on
+  every qubit, then two-qubit Cliffords (CNOT, CZ, SWAP or ISWAP, chosen at
+  random) on a brickwork of neighbouring pairs; optionally measurements of
+  random qubits into fresh keys after some layers (``mid_measure``),
+  resets, a Pauli X conditioned on the previous key (``feedback``),
+  ``depolarize(p)`` on every qubit after each layer, and a final measurement
+  of every qubit into key "m".
 """
 
 from __future__ import annotations
@@ -132,3 +140,35 @@ def random_pauli_hamiltonian(n: int, terms: int, seed: int = 0, min_w: int = 2, 
         ps = cirq.PauliString({q[int(i)]: paulis[rs.randint(3)] for i in qs}, coefficient=rs.normal())
         total += ps
     return total
+
+
+def random_clifford_circuit(n: int, depth: int, seed: int = 0, *, mid_measure: float = 0.0,
+                            resets: bool = False, feedback: bool = False, p: float = 0.0,
+                            final_measure: bool = True):
+    cirq = _cirq()
+    rs = np.random.RandomState(seed)
+    q = cirq.LineQubit.range(n)
+    cliffords = cirq.SingleQubitCliffordGate.all_single_qubit_cliffords
+    two = [cirq.CNOT, cirq.CZ, cirq.SWAP, cirq.ISWAP]
+    moments = []
+    nkeys = 0
+    for d in range(depth):
+        moments.append(cirq.Moment(cliffords[rs.randint(24)].on(x) for x in q))
+        pairs = [two[rs.randint(len(two))].on(q[i], q[i + 1]) for i in range(d % 2, n - 1, 2)]
+        if pairs:
+            moments.append(cirq.Moment(pairs))
+        if p > 0:
+            moments.append(cirq.Moment(cirq.depolarize(p).on(x) for x in q))
+        if mid_measure and rs.uniform() < mid_measure:
+            a = int(rs.randint(n))
+            key = f"k{nkeys}"
+            moments.append(cirq.Moment(cirq.measure(q[a], key=key)))
+            if feedback and nkeys > 0:
+                b = int(rs.randint(n))
+                moments.append(cirq.Moment(cirq.X(q[b]).with_classical_controls(f"k{nkeys - 1}")))
+            if resets:
+                moments.append(cirq.Moment(cirq.reset(q[a])))
+            nkeys += 1
+    if final_measure:
+        moments.append(cirq.Moment(cirq.measure(*q, key="m")))
+    return cirq.Circuit(moments)

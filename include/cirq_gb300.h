@@ -140,6 +140,63 @@ int gbq_device_name(gbq_ctx* ctx, char* buf, int len);
 /* Number of kernels this context has launched (for launch accounting). */
 int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
 
+/* ---- Clifford circuits: reference tableau run + Pauli-frame shots ---------
+ * Replaces the reference's per-repetition stabilizer simulation
+ * (StabilizerSampler._run, cirq-core/cirq/sim/clifford/stabilizer_sampler.py:52-70;
+ * CliffordSimulator.run through SimulatorBase._run,
+ * cirq-core/cirq/sim/simulator_base.py:225-273).
+ * Program: ops in circuit order; qubits 0..nq-1; measurement records
+ * 0..nrec-1 (one per measured qubit and measurement).
+ *   UNITARY (k = 1..3 qubits q[0..k)): tables[tab + idx] for idx = x bits |
+ *     z bits << k of a Pauli on those qubits gives its image x' | z' << k |
+ *     sign << 2k; lin[o] (o < 2k) gives output bit o of the frame map as an
+ *     XOR of input bits (x_0..x_{k-1}, z_0..z_{k-1}).
+ *   MEASURE (q[0] in the Z basis into record rec; lin[0] = 1 inverts).
+ *   RESET (q[0] to |0>).
+ *   NOISE (q[0]): Pauli X, Y, Z with probabilities p[0], p[1], p[2].
+ *   COND_PAULI (k qubits): the Pauli of tables[tab ...] (lin[j]: bit 0 = X,
+ *     bit 1 = Z part on q[j]) applied when any of the records
+ *     conds[cond_begin .. cond_begin + cond_count) is 1. */
+#define GBQ_CLIFF_UNITARY 0
+#define GBQ_CLIFF_MEASURE 1
+#define GBQ_CLIFF_RESET 2
+#define GBQ_CLIFF_NOISE 3
+#define GBQ_CLIFF_COND_PAULI 4
+typedef struct gbq_cliff_op {
+  int8_t kind;
+  int8_t k;
+  int8_t lin[6];
+  int32_t q[3];
+  int32_t tab;
+  int32_t rec;
+  int32_t cond_begin;
+  int32_t cond_count;
+  float p[3];
+} gbq_cliff_op;
+
+/* Runs the program once on a stabilizer tableau on the GPU (one CTA): every
+ * random measurement takes outcome 0, noise is skipped.  ref_out[nrec]
+ * receives the records.  Host arrays. */
+int gbq_cliff_reference(gbq_ctx* ctx, int nq, const gbq_cliff_op* ops, int nops, const uint32_t* tables,
+                        int ntables, const int32_t* conds, int nconds, int nrec, uint8_t* ref_out);
+/* Samples `shots` runs by Pauli frames relative to the reference records
+ * `ref` (from gbq_cliff_reference).  out (host): with out_bytes = 0, nrec *
+ * ceil(shots/32) words, record r's bit of shot j at
+ * out[r * ceil(shots/32) + j / 32] bit j % 32; with out_bytes != 0, shots *
+ * nrec bytes, out[j * nrec + r] (transposed on the device).  The same seed
+ * gives the same samples.
+ * layers (optional, nlayers + 1 entries): the ops in layers of ops on
+ * disjoint qubits, layer L = ops layers[L] .. layers[L + 1] - 1
+ * (layers[0] = 0, layers[nlayers] = nops).  With layers, each CTA keeps the
+ * frames of up to 1024 shots in shared memory and applies a layer's ops in
+ * parallel (when 2 * nq words per 32 shots fit; otherwise the frames stay
+ * in device memory and every thread walks the ops in order). */
+int gbq_cliff_sample(gbq_ctx* ctx, int nq, const gbq_cliff_op* ops, int nops, const uint32_t* tables, int ntables,
+                     const int32_t* conds, int nconds, const uint8_t* ref, int nrec, int64_t shots, uint64_t seed,
+                     void* out, const int32_t* layers, int nlayers, int out_bytes);
+/* Checks a Clifford program without a GPU (GBQ_ERR_ARG if invalid). */
+int gbq_cliff_validate(int nq, const gbq_cliff_op* ops, int nops, int ntables, int nconds, int nrec);
+
 /* Pass-specialised kernels.  Every single-state pass of 12-bit tiles whose
  * ops are register layouts, register dense ops of width <= 2 and register
  * diagonals can run a kernel generated for its op records and compiled at
