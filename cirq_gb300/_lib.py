@@ -185,6 +185,7 @@ SIGNATURES = {
     "gbq_jit_stats": [_P, _P, _P],
     "gbq_jit_source": [_I, _P, _P, _I, _P, _SZ, _P],
     "gbq_jit_compile_check": [ctypes.c_char_p, _P],
+    "gbq_jit_shutdown": [_D],
     "gbq_device_name": [_P, _P, _I],
     "gbq_launch_count": [_P, _P],
     "gbq_event_record": [_P, _I],
@@ -265,7 +266,36 @@ def load(path: str | None = None, build_if_missing: bool = True) -> ctypes.CDLL:
         if tuple(sizes) != want:
             raise RuntimeError(f"C struct sizes {tuple(sizes)} != numpy mirrors {want}")
         _lib = lib
+        _register_shutdown(lib)
         return lib
+
+
+class _Sentinel:
+    pass
+
+
+_SENTINEL = _Sentinel()
+
+
+def _register_shutdown(lib) -> None:
+    """At interpreter exit, stop the background compilation of specialised
+    kernels before anything is torn down: Python runs atexit handlers in
+    reverse order of registration, so this one (registered after the
+    weakref module's own exit hook, which the dummy finalizer below forces)
+    runs before the finalizers that free device buffers and graphs, and all
+    of them run before the C runtime's exit handlers."""
+    import atexit
+    import weakref
+
+    weakref.finalize(_SENTINEL, int)
+
+    def _stop():
+        try:
+            lib.gbq_jit_shutdown(30.0)
+        except Exception:  # noqa: BLE001  (exit path: never raise)
+            pass
+
+    atexit.register(_stop)
 
 
 def check(rc: int, what: str = "") -> None:

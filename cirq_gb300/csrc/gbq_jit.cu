@@ -611,15 +611,19 @@ static void jit_worker() {
 // being compiled, so no worker is inside NVRTC or the CUDA runtime while
 // they shut down.  Registered when the first worker starts, i.e. after the
 // CUDA runtime, so it runs before the runtime's own exit handlers.
-static void jit_at_exit() {
+// Stops the compile workers: drops the queued jobs and waits (bounded) for
+// the ones being compiled.  Returns true if none is left running.
+static bool jit_stop(double timeout_s) {
   JitState& S = jst();
   std::unique_lock<std::mutex> lk(S.mu);
   S.stopping = true;
   for (auto& j : S.queue) S.cache.erase(j.key);
   S.queue.clear();
   S.work_cv.notify_all();
-  S.cv.wait_for(lk, std::chrono::seconds(30), [&] { return S.busy == 0; });
+  return S.cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] { return S.busy == 0; });
 }
+
+static void jit_at_exit() { jit_stop(30.0); }
 
 bool jit_enabled(Ctx* c) {
   if (c->jit < 0) {
@@ -723,6 +727,14 @@ int64_t jit_pending() {
 using namespace gbq;
 
 extern "C" {
+
+// Stops background compilation for good (the process is about to exit):
+// queued passes are dropped and running compiles are awaited, at most
+// timeout_s seconds.  Passes whose kernel is not built keep running on the
+// interpreter.
+int gbq_jit_shutdown(double timeout_s) {
+  return jit_stop(timeout_s > 0 ? timeout_s : 0.0) ? GBQ_OK : GBQ_ERR_UNSUPPORTED;
+}
 
 // Test hook: compiles a source with NVRTC for sm_103a (no GPU needed).
 // Returns 0 and the CUBIN size, or an error with the compiler log.

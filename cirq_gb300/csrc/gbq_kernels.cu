@@ -57,11 +57,21 @@ __global__ void k_set_basis(float2* s, uint64_t n, uint64_t index) {
     s[i] = make_float2(i == index ? 1.f : 0.f, 0.f);
 }
 
-// sum |s_i * scale|^2 with every scaled value rounded to float first
-__global__ void k_norm2(const float2* s, uint64_t n, float scale, int use_scale, double* out) {
-  float acc = 0.f;
+// sum |s_i * scale|^2 with every scaled value rounded to float first.
+// Pairs of amplitudes as 16-byte loads, four loads in flight per thread;
+// float partial sums of at most 64 values go into a double.
+__device__ __forceinline__ float norm_pair(float4 v, float scale, int use_scale) {
+  if (use_scale) {
+    v.x *= scale;
+    v.y *= scale;
+    v.z *= scale;
+    v.w *= scale;
+  }
+  return fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w)));
+}
+// Scalar form for states that do not start on a 16-byte boundary.
+__global__ void k_norm2_scalar(const float2* s, uint64_t n, float scale, int use_scale, double* out) {
   double accd = 0.0;
-  int cnt = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     float2 v = s[i];
@@ -69,14 +79,36 @@ __global__ void k_norm2(const float2* s, uint64_t n, float scale, int use_scale,
       v.x *= scale;
       v.y *= scale;
     }
-    acc = fmaf(v.x, v.x, fmaf(v.y, v.y, acc));
-    if (++cnt == 64) {
-      accd += acc;
-      acc = 0.f;
-      cnt = 0;
+    accd += fmaf(v.x, v.x, v.y * v.y);
+  }
+  const double r = block_sum(accd);
+  if (threadIdx.x == 0) atomicAdd(out, r);
+}
+
+__global__ void k_norm2(const float2* s, uint64_t n, float scale, int use_scale, double* out) {
+  const float4* s4 = reinterpret_cast<const float4*>(s);
+  const uint64_t n4 = n / 2;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  double accd = 0.0;
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n4; i += 4 * stride) {
+    const float4 a = __ldcs(s4 + i), b = __ldcs(s4 + i + stride), c = __ldcs(s4 + i + 2 * stride),
+                 d = __ldcs(s4 + i + 3 * stride);
+    const float acc = norm_pair(a, scale, use_scale) + norm_pair(b, scale, use_scale) +
+                      norm_pair(c, scale, use_scale) + norm_pair(d, scale, use_scale);
+    accd += acc;
+  }
+  for (; i < n4; i += stride) accd += norm_pair(__ldcs(s4 + i), scale, use_scale);
+  if (n & 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      float2 v = s[n - 1];
+      if (use_scale) {
+        v.x *= scale;
+        v.y *= scale;
+      }
+      accd += fmaf(v.x, v.x, v.y * v.y);
     }
   }
-  accd += acc;
   const double r = block_sum(accd);
   if (threadIdx.x == 0) atomicAdd(out, r);
 }
@@ -90,11 +122,34 @@ __global__ void k_project(float2* s, uint64_t n, uint64_t mask, uint64_t value, 
   }
 }
 
-__global__ void k_scale(float2* s, uint64_t n, float scale) {
+__global__ void k_scale_scalar(float2* s, uint64_t n, float scale) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     float2 v = s[i];
     s[i] = make_float2(v.x * scale, v.y * scale);
+  }
+}
+
+__global__ void k_scale(float2* s, uint64_t n, float scale) {
+  float4* s4 = reinterpret_cast<float4*>(s);
+  const uint64_t n4 = n / 2;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (; i + stride < n4; i += 2 * stride) {
+    float4 a = __ldcs(s4 + i), b = __ldcs(s4 + i + stride);
+    a.x *= scale; a.y *= scale; a.z *= scale; a.w *= scale;
+    b.x *= scale; b.y *= scale; b.z *= scale; b.w *= scale;
+    __stcs(s4 + i, a);
+    __stcs(s4 + i + stride, b);
+  }
+  for (; i < n4; i += stride) {
+    float4 a = __ldcs(s4 + i);
+    a.x *= scale; a.y *= scale; a.z *= scale; a.w *= scale;
+    __stcs(s4 + i, a);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const float2 v = s[n - 1];
+    s[n - 1] = make_float2(v.x * scale, v.y * scale);
   }
 }
 
@@ -382,13 +437,19 @@ int do_norm2(Ctx* c, const float2* s, int nbits, float scale, int use_scale, dou
   const uint64_t n = 1ull << nbits;
   cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(double), c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "memset");
-  k_norm2<<<grid_for(c, n, kRedThreads), kRedThreads, 0, c->stream>>>(s, n, scale, use_scale, d_out);
+  if (reinterpret_cast<uintptr_t>(s) & 15)
+    k_norm2_scalar<<<grid_for(c, n, kRedThreads), kRedThreads, 0, c->stream>>>(s, n, scale, use_scale, d_out);
+  else
+    k_norm2<<<grid_for(c, n, kRedThreads), kRedThreads, 0, c->stream>>>(s, n, scale, use_scale, d_out);
   return check_launch(c, "k_norm2");
 }
 
 int do_scale(Ctx* c, float2* s, int nbits, float scale) {
   const uint64_t n = 1ull << nbits;
-  k_scale<<<grid_for(c, n, 256), 256, 0, c->stream>>>(s, n, scale);
+  if (reinterpret_cast<uintptr_t>(s) & 15)
+    k_scale_scalar<<<grid_for(c, n, 256), 256, 0, c->stream>>>(s, n, scale);
+  else
+    k_scale<<<grid_for(c, n, 256), 256, 0, c->stream>>>(s, n, scale);
   return check_launch(c, "k_scale");
 }
 

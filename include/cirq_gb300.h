@@ -213,6 +213,12 @@ int gbq_set_jit(gbq_ctx* ctx, int mode);
 /* Specialised kernels compiled by this process so far and (optional) those
  * queued or being compiled now, and the launches of specialised kernels. */
 int gbq_jit_stats(int64_t* compiles, int64_t* pending, int64_t* launches);
+/* Stops background compilation for good: queued passes are dropped and
+ * running compiles awaited (at most timeout_s seconds; GBQ_ERR_UNSUPPORTED
+ * if some are still running then).  A host calls it before it exits (the
+ * Python package does so from its atexit handler); passes whose kernel is
+ * not built run on the interpreter. */
+int gbq_jit_shutdown(double timeout_s);
 /* The generated CUDA source of one pass (test and inspection hook; no GPU
  * needed).  *needed receives the size including the terminating zero;
  * GBQ_ERR_UNSUPPORTED if the pass has no specialised form. */
