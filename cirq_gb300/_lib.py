@@ -183,7 +183,7 @@ SIGNATURES = {
     "gbq_cliff_reference": [_P, _I, _P, _I, _P, _I, _P, _I, _I, _P],
     "gbq_cliff_sample": [_P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _I64, _U64, _P, _P, _I, _I],
     "gbq_jit_stats": [_P, _P, _P],
-    "gbq_jit_source": [_I, _P, _P, _I, _P, _SZ, _P],
+    "gbq_jit_source": [_I, _P, _P, _I, _I, _P, _SZ, _P],
     "gbq_jit_compile_check": [ctypes.c_char_p, _P],
     "gbq_jit_shutdown": [_D],
     "gbq_device_name": [_P, _P, _I],

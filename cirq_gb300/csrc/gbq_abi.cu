@@ -402,17 +402,19 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
   // in parallel by worker threads); mode 1 waits for them
   // background mode only for states of >= kJitAutoMinBits bits: below, a
   // pass takes microseconds and the interpreter is as fast
-  const bool jit = !dual && jit_enabled(c) && (c->jit == 1 || nbits >= kJitAutoMinBits);
+  const bool jit = jit_enabled(c) && (c->jit == 1 || nbits >= kJitAutoMinBits);
   if (jit) {
     std::vector<std::pair<std::string, PassArgs*>> todo;
     int rc = GBQ_OK;
     for (int q = 0; q < npasses && !rc; ++q) {
       int mma = 0;
       rc = convert_pass(passes[q], ops, nops, nbits, dual, a, ma, ta, mma);
-      if (rc || mma || !jit_eligible(a)) continue;
-      todo.emplace_back(jit_key(a, c), new PassArgs(a));
+      if (rc || mma) continue;
+      a.ti.partial = partial;
+      if (!jit_eligible(a, dual)) continue;
+      todo.emplace_back(jit_key(a, c, dual), new PassArgs(a));
     }
-    if (!rc) jit_prepare(c, todo, c->jit == 1);
+    if (!rc) jit_prepare(c, todo, dual, c->jit == 1);
     for (auto& t : todo) delete t.second;
     if (rc) return rc;
   }
@@ -444,7 +446,7 @@ static int run_passes(Ctx* c, float2* psi, float2* lam, int nbits, const gbq_pas
       rc = launch_mma_pass(c, ma);
     } else {
       bool launched = false;
-      if (jit && jit_eligible(a)) rc = jit_launch(c, a, jit_key(a, c), launched);
+      if (jit && jit_eligible(a, dual)) rc = jit_launch(c, a, jit_key(a, c, dual), launched);
       if (!rc && !launched) rc = launch_pass(c, a, dual);
     }
     if (rc) return rc;
@@ -633,18 +635,20 @@ int gbq_jit_stats(int64_t* compiles, int64_t* pending, int64_t* launches) {
   return GBQ_OK;
 }
 
-int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, char* buf, size_t len,
+int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, int dual, char* buf, size_t len,
                    size_t* needed) {
   if (!pass || !ops || !needed) return arg_fail("gbq_jit_source: null argument");
   PassArgs* a = new PassArgs();
   MmaArgs* ma = new MmaArgs();
   TcArgs* ta = new TcArgs();
   int mma = 0;
-  int rc = convert_pass(*pass, ops, nops, nbits, false, *a, *ma, *ta, mma);
-  if (!rc && (mma || !jit_eligible(*a))) rc = GBQ_ERR_UNSUPPORTED;
+  int rc = convert_pass(*pass, ops, nops, nbits, dual != 0, *a, *ma, *ta, mma);
+  static double probe_sink;  // probes need a partial buffer to be eligible; only its presence is checked
+  a->ti.partial = dual ? &probe_sink : nullptr;
+  if (!rc && (mma || !jit_eligible(*a, dual != 0))) rc = GBQ_ERR_UNSUPPORTED;
   if (rc == GBQ_ERR_UNSUPPORTED) set_error("gbq_jit_source: the pass has no specialised form");
   if (!rc) {
-    const std::string src = jit_source(*a);
+    const std::string src = jit_source(*a, dual != 0);
     *needed = src.size() + 1;
     if (buf && len) {
       const size_t n = std::min(len - 1, src.size());
@@ -1154,7 +1158,12 @@ int gbq_sv_apply_paulisum(gbq_ctx* c, const gbq_c64* psi, int nbits, const gbq_p
   if (rc) return rc;
   gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(c->scratch);
   if (nterms) {
-    cudaError_t e = cudaMemcpyAsync(d_terms, terms, tbytes, cudaMemcpyHostToDevice, c->stream);
+    // terms with the same X mask read the same amplitude: the kernel
+    // reads it once per run of equal masks
+    std::vector<gbq_pauli> sorted(terms, terms + nterms);
+    std::stable_sort(sorted.begin(), sorted.end(), [](const gbq_pauli& a, const gbq_pauli& b) { return a.x < b.x; });
+    cudaError_t e = cudaMemcpyAsync(d_terms, sorted.data(), tbytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // `sorted` is pageable and local
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
   }
   rc = do_apply_paulisum(c, reinterpret_cast<const float2*>(psi), nbits, d_terms, nterms,

@@ -215,10 +215,10 @@ int cliff_check(int nq, const gbq_cliff_op* ops, int nops, int ntables, int ncon
 // Pass-specialised kernels (gbq_jit.cu).
 constexpr int kJitAutoMinBits = 20;
 bool jit_enabled(Ctx* c);
-bool jit_eligible(const PassArgs& a);
-std::string jit_key(const PassArgs& a, const Ctx* c);
-std::string jit_source(const PassArgs& a);
-void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes, bool wait);
+bool jit_eligible(const PassArgs& a, bool dual);
+std::string jit_key(const PassArgs& a, const Ctx* c, bool dual);
+std::string jit_source(const PassArgs& a, bool dual);
+void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes, bool dual, bool wait);
 int jit_launch(Ctx* c, const PassArgs& a, const std::string& key, bool& launched);
 int64_t jit_compile_count();
 int64_t jit_launch_count();

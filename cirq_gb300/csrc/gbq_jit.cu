@@ -55,14 +55,20 @@ typedef unsigned short u16;
 
 struct JitArgs {
   float2* psi;
+  float2* lam;
   const float2* mats;
+  double* partial;
   int* abort;
   i64 ntiles;
   int nbits;
   int L;
-  u64 gw[12];
+  u64 gw[13];
   signed char nt[64];
 };
+
+#define LT @LT@
+#define DUAL @DUAL@
+#define NSL (1 << (LT - 8))
 
 __device__ __forceinline__ u32 phys_dev(u32 i) {
   u32 s = (__popc(i & @SWZ0@u) & 1) | ((__popc(i & @SWZ1@u) & 1) << 1) |
@@ -73,7 +79,7 @@ __device__ __forceinline__ u32 su32(const void* p) { return (u32)__cvta_generic_
 __device__ __forceinline__ u64 lin_off(const JitArgs& a, u32 i) {
   u64 r = 0;
 #pragma unroll
-  for (int b = 0; b < 12; ++b)
+  for (int b = 0; b < LT; ++b)
     if ((i >> b) & 1u) r ^= a.gw[b];
   return r;
 }
@@ -119,6 +125,23 @@ __device__ __forceinline__ void ops_barrier() { asm volatile("bar.sync 1, 256;\n
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
+__device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// A probe's per-thread total over the CTA's tiles into its accumulator
+// (once per CTA: the per-tile parts are added in double per thread).
+__device__ __forceinline__ void probe_flush(double v, int pidx, double* red) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) atomicAdd(red + pidx, v);
+}
 __host__ __device__ constexpr int popc_c(int x) { return x ? (x & 1) + popc_c(x >> 1) : 0; }
 __host__ __device__ constexpr int dep_c(int x, int mask) {
   int r = 0, i = 0;
@@ -129,19 +152,23 @@ __host__ __device__ constexpr int dep_c(int x, int mask) {
     }
   return r;
 }
-// Dense op on the register positions in MASK (width <= 2): packed form
+template <bool SH>
+__device__ __forceinline__ float4 mload(const float2* mp, int e) {
+  return SH ? *reinterpret_cast<const float4*>(mp + e) : __ldg(reinterpret_cast<const float4*>(mp + e));
+}
+// Dense op on the register positions in MASK (width <= 2) of v (and, in
+// two-state passes, of w with the same matrix): packed form
 // acc += m * (a.x, a.x) + (i m) * (a.y, a.y), the interpreter's order.
 template <int MASK, bool SH>
-__device__ __forceinline__ void rdense(float2 (&v)[16], const float2* __restrict__ mp) {
+__device__ __forceinline__ void rdense(float2 (&v)[NSL], float2 (&w)[NSL], const float2* __restrict__ mp) {
   constexpr int K = popc_c(MASK);
   constexpr int D = 1 << K;
-  constexpr int NG = 16 / D;
-  constexpr int REST = 15 & ~MASK;
+  constexpr int NG = NSL / D;
+  constexpr int REST = (NSL - 1) & ~MASK;
   float2 m[D * D], im[D * D];
 #pragma unroll
   for (int e = 0; e < D * D; e += 2) {
-    // SH: staged in shared memory, else the pool through the read-only cache
-    const float4 mm = SH ? *reinterpret_cast<const float4*>(mp + e) : __ldg(reinterpret_cast<const float4*>(mp + e));
+    const float4 mm = mload<SH>(mp, e);
     m[e] = make_float2(mm.x, mm.y);
     m[e + 1] = make_float2(mm.z, mm.w);
     im[e] = make_float2(-mm.y, mm.x);
@@ -150,12 +177,17 @@ __device__ __forceinline__ void rdense(float2 (&v)[16], const float2* __restrict
 #pragma unroll
   for (int g = 0; g < NG; ++g) {
     const int s0 = dep_c(g, REST);
-    float2 ax[D], ay[D];
+    float2 ax[D], ay[D], bx[DUAL ? D : 1], by[DUAL ? D : 1];
 #pragma unroll
     for (int j = 0; j < D; ++j) {
       const float2 a = v[s0 | dep_c(j, MASK)];
       ax[j] = make_float2(a.x, a.x);
       ay[j] = make_float2(a.y, a.y);
+      if (DUAL) {
+        const float2 b = w[s0 | dep_c(j, MASK)];
+        bx[j % (DUAL ? D : 1)] = make_float2(b.x, b.x);
+        by[j % (DUAL ? D : 1)] = make_float2(b.y, b.y);
+      }
     }
 #pragma unroll
     for (int r = 0; r < D; ++r) {
@@ -166,14 +198,79 @@ __device__ __forceinline__ void rdense(float2 (&v)[16], const float2* __restrict
         acc = __ffma2_rn(im[r * D + c], ay[c], acc);
       }
       v[s0 | dep_c(r, MASK)] = acc;
+      if (DUAL) {
+        float2 accb = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          accb = __ffma2_rn(m[r * D + c], bx[c % (DUAL ? D : 1)], accb);
+          accb = __ffma2_rn(im[r * D + c], by[c % (DUAL ? D : 1)], accb);
+        }
+        w[s0 | dep_c(r, MASK)] = accb;
+      }
     }
   }
 }
+// Dense probe on the register positions in MASK: the thread's part of
+// Re <w | M v> (the interpreter's scalar order; width 3 reads M row by row).
+template <int MASK, bool SH>
+__device__ __forceinline__ float rprobe(const float2 (&v)[NSL], const float2 (&w)[NSL], const float2* __restrict__ mp) {
+  constexpr int K = popc_c(MASK);
+  constexpr int D = 1 << K;
+  constexpr int NG = NSL / D;
+  constexpr int REST = (NSL - 1) & ~MASK;
+  float part = 0.f;
+  if (K <= 2) {
+    float2 m[D * D];
+#pragma unroll
+    for (int e = 0; e < D * D; e += 2) {
+      const float4 mm = mload<SH>(mp, e);
+      m[e] = make_float2(mm.x, mm.y);
+      m[e + 1] = make_float2(mm.z, mm.w);
+    }
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_c(g, REST);
+      float2 in[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) in[j] = v[s0 | dep_c(j, MASK)];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; ++c) cfma(acc, m[r * D + c], in[c]);
+        const float2 l = w[s0 | dep_c(r, MASK)];
+        part = fmaf(l.x, acc.x, fmaf(l.y, acc.y, part));
+      }
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int s0 = dep_c(g, REST);
+      float2 in[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) in[j] = v[s0 | dep_c(j, MASK)];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < D; c += 2) {
+          const float4 mm = mload<SH>(mp, r * D + c);
+          cfma(acc, make_float2(mm.x, mm.y), in[c]);
+          cfma(acc, make_float2(mm.z, mm.w), in[c + 1]);
+        }
+        const float2 l = w[s0 | dep_c(r, MASK)];
+        part = fmaf(l.x, acc.x, fmaf(l.y, acc.y, part));
+      }
+    }
+  }
+  return part;
+}
 
 extern "C" __global__ void __launch_bounds__(320, 2) k_jit(const __grid_constant__ JitArgs a) {
-  constexpr int TS = 4096;
+  constexpr int TS = 1 << LT;
   constexpr int S = 3;
   constexpr int NH = TS >> 5;
+  constexpr int NST = DUAL ? 2 : 1;  // states per tile buffer
   extern __shared__ float4 smraw[];
   __shared__ u64 ttab[768];
   __shared__ u64 hoff[NH];
@@ -182,7 +279,8 @@ extern "C" __global__ void __launch_bounds__(320, 2) k_jit(const __grid_constant
   __shared__ int abort_flag;
   __shared__ u32 lent[@NL@ * 256];  // consumers' shared offsets of slot 0, per layout
   __shared__ __align__(16) float2 mtab[@NM@];  // the pass's dense matrices, staged once per CTA
-  float2* buf = reinterpret_cast<float2*>(smraw);
+  __shared__ double red[@NP@];  // probe accumulators of this CTA
+  float2* buf = reinterpret_cast<float2*>(smraw);  // [S][NST][TS]
   const int t = threadIdx.x;
   for (int e = t; e < 768; e += 320) {
     const int part = e / 256;
@@ -192,6 +290,7 @@ extern "C" __global__ void __launch_bounds__(320, 2) k_jit(const __grid_constant
     hoff[j] = lin_off(a, (u32)j << 5);
     hphys[j] = (u16)phys_dev((u32)j << 5);
   }
+  for (int j = t; j < @NP@; j += 320) red[j] = 0.0;
 @STAGE@
   if (t == 0) {
     abort_flag = 0;
@@ -215,26 +314,34 @@ extern "C" __global__ void __launch_bounds__(320, 2) k_jit(const __grid_constant
     const int shalf = (2 * lane) >> 5;
     for (i64 i = 0; i < count + S; ++i) {
       const int b = (int)(i % S);
-      float2* sb = buf + (size_t)b * TS;
+      float2* sb = buf + (size_t)b * NST * TS;
       if (i >= S) {
         if (!ws_wait(&empty[b], (u32)(((i - S) / S) & 1), abort)) break;
         const u64 gb = tile_base_fast(ttab, blockIdx.x + (i - S) * step);
-        float2* g = a.psi + gb + so_l;
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          float2* g = (st ? a.lam : a.psi) + gb + so_l;
+          const float2* sbs = sb + st * TS;
 #pragma unroll 4
-        for (int j = pw; j < NH / 2; j += 2) {
-          const int h = 2 * j + shalf;
-          const u32 p = sp_l ^ hphys[h];
-          const float2 x = sb[p], y = sb[p ^ 1u];
-          __stcs(reinterpret_cast<float4*>(g + hoff[h]), make_float4(x.x, x.y, y.x, y.y));
+          for (int j = pw; j < NH / 2; j += 2) {
+            const int h = 2 * j + shalf;
+            const u32 p = sp_l ^ hphys[h];
+            const float2 x = sbs[p], y = sbs[p ^ 1u];
+            __stcs(reinterpret_cast<float4*>(g + hoff[h]), make_float4(x.x, x.y, y.x, y.y));
+          }
         }
       }
       if (i < count) {
         const u64 gb = tile_base_fast(ttab, blockIdx.x + i * step);
-        const float2* g = a.psi + gb + lo_l;
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          const float2* g = (st ? a.lam : a.psi) + gb + lo_l;
+          float2* sbs = sb + st * TS;
 #pragma unroll 4
-        for (int jj = pw; jj < NH / 2; jj += 2) {
-          cp_async8(sb + (lp_l ^ hphys[2 * jj]), g + hoff[2 * jj]);
-          cp_async8(sb + (lp_l ^ hphys[2 * jj + 1]), g + hoff[2 * jj + 1]);
+          for (int jj = pw; jj < NH / 2; jj += 2) {
+            cp_async8(sbs + (lp_l ^ hphys[2 * jj]), g + hoff[2 * jj]);
+            cp_async8(sbs + (lp_l ^ hphys[2 * jj + 1]), g + hoff[2 * jj + 1]);
+          }
         }
         asm volatile("cp.async.mbarrier.arrive.noinc.shared.b64 [%0];\n" ::"r"(su32(&full[b])) : "memory");
       }
@@ -246,28 +353,36 @@ extern "C" __global__ void __launch_bounds__(320, 2) k_jit(const __grid_constant
       const int b = (int)(i % S);
       const bool ok = ws_wait(&full[b], (u32)((i / S) & 1), abort);
       if (consumers_any(!ok)) break;
-      char* sbb = reinterpret_cast<char*>(buf + (size_t)b * TS);
+      char* sbb = reinterpret_cast<char*>(buf + (size_t)b * NST * TS);
+      char* sbw = sbb + (size_t)TS * 8;
       const u64 gb = tile_base_fast(ttab, blockIdx.x + i * step);
       const float2* __restrict__ M = a.mats;
-      float2 v[16];
+      float2 v[NSL];
+      float2 w[NSL];
+      (void)sbw;
+      (void)w;
 @BODY@
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(su32(&empty[b])) : "memory");
     }
+@FLUSH@
   }
   if (t == 0 || t == 256) {
     if (*abort && a.abort) atomicExch(a.abort, 1);
   }
+@EPILOGUE@
 }
 )GBQJIT";
 
 struct JitArgs {
   float2* psi;
+  float2* lam;
   const float2* mats;
+  double* partial;
   int* abort;
   int64_t ntiles;
   int nbits;
   int L;
-  uint64_t gw[12];
+  uint64_t gw[13];
   int8_t nt[64];
 };
 
@@ -351,25 +466,35 @@ static std::string nvrtc_compile(const std::string& src, std::string* log) {
 // ---- source generation ----------------------------------------------------------
 constexpr int kJitMaxLayouts = 8;  // per-thread layout table: 1 KB per layout
 // Static shared memory per CTA that keeps two CTAs of three 32 KB tile
-// buffers on an SM (228 KB per SM, 1 KB reserved per CTA), and the part of
-// it taken by the fixed tables (tile bases, producer offsets, barriers).
+// buffers on an SM (228 KB per SM, 1 KB reserved per CTA).
 constexpr int64_t kJitStaticSmem = 17 * 1024 - 256;
-constexpr int64_t kJitFixedSmem = 768 * 8 + 128 * 8 + 128 * 2 + 6 * 8 + 16;
 
-static bool jit_op_ok(const OpDev& op) {
-  if (op.kind == GBQ_OP_LAYOUT) return op.k == 4;
+// Tile width of the specialised kernels: 12 bits for one state (16
+// amplitudes per consumer thread), 11 bits for two states (8 + 8).
+static int jit_tile_bits(bool dual) { return dual ? 11 : 12; }
+
+static bool jit_op_ok(const OpDev& op, bool dual, int R) {
+  if (op.kind == GBQ_OP_LAYOUT) return op.k == R;
   if (op.kind == GBQ_OP_RDENSE) return op.k >= 1 && op.k <= 2 && op.nsel <= 3;
   if (op.kind == GBQ_OP_RDIAG) return op.k >= 1 && op.k <= 8;
+  if (!dual) return false;
+  if (op.kind == GBQ_OP_RPROBE) return op.k >= 1 && op.k <= 3 && op.nsel <= 3;
+  if (op.kind == GBQ_OP_RPROBE_DIAG) return op.k >= 1 && op.k <= 8;
   return false;
 }
 
-bool jit_eligible(const PassArgs& a) {
+bool jit_eligible(const PassArgs& a, bool dual) {
   const TileInfo& ti = a.ti;
-  if (ti.L != 12 || ti.m < 5 || ti.pstride != 0 || ti.nops < 1 || ti.nbits - ti.L > 24) return false;
+  if (ti.L != jit_tile_bits(dual) || ti.m < 5 || ti.pstride != 0 || ti.nops < 1 || ti.nbits - ti.L > 24)
+    return false;
+  if (dual && !ti.partial) {
+    for (int o = 0; o < ti.nops; ++o)
+      if (a.ops[o].kind == GBQ_OP_RPROBE || a.ops[o].kind == GBQ_OP_RPROBE_DIAG) return false;
+  }
   if (a.ops[0].kind != GBQ_OP_LAYOUT) return false;
   int nl = 0;
   for (int o = 0; o < ti.nops; ++o) {
-    if (!jit_op_ok(a.ops[o])) return false;
+    if (!jit_op_ok(a.ops[o], dual, ti.L - 8)) return false;
     nl += a.ops[o].kind == GBQ_OP_LAYOUT;
   }
   return nl <= kJitMaxLayouts;
@@ -382,29 +507,34 @@ static std::string hex(uint32_t v) {
 }
 
 // Shared byte offset (relative to the thread's slot 0) of register slot s.
-static uint32_t slot_off(const OpDev& lay, int s) {
+static uint32_t slot_off(const OpDev& lay, int s, int R) {
   uint32_t p = 0;
-  for (int b = 0; b < 4; ++b)
+  for (int b = 0; b < R; ++b)
     if ((s >> b) & 1) p ^= lay.pcol[b];
   return p * 8u;
 }
 
-std::string jit_source(const PassArgs& a) {
+std::string jit_source(const PassArgs& a, bool dual) {
   const TileInfo& ti = a.ti;
-  std::ostringstream setup, body, stage;
+  const int L = ti.L, R = L - 8, NS = 1 << R;
+  std::ostringstream setup, body, stage, epi;
+  int nl = 0, np = 0;
+  for (int o = 0; o < ti.nops; ++o) {
+    nl += a.ops[o].kind == GBQ_OP_LAYOUT;
+    if (a.ops[o].kind == GBQ_OP_RPROBE || a.ops[o].kind == GBQ_OP_RPROBE_DIAG) np = std::max(np, a.ops[o].pidx + 1);
+  }
   // dense matrices staged in shared memory (as many ops as fit; the rest
-  // are read through the read-only cache)
-  int nl = 0;
-  for (int o = 0; o < ti.nops; ++o) nl += a.ops[o].kind == GBQ_OP_LAYOUT;
-  const int64_t budget = (kJitStaticSmem - kJitFixedSmem - 1024 * (int64_t)nl) / 8;  // float2 entries
-  // A family of 2^nsel selected matrices is stored with a stride of
-  // dd + 2 entries, so the matrices that the lanes of a quarter-warp select
-  // start in different banks.
+  // are read through the read-only cache).  A family of 2^nsel selected
+  // matrices is stored with a stride of dd + 2 entries, so the matrices
+  // that the lanes of a quarter-warp select start in different banks.
+  const int64_t nh = (int64_t)1 << (L - 5);
+  const int64_t fixed = 768 * 8 + nh * 8 + nh * 2 + 6 * 8 + 16 + 8 * std::max(np, 1);
+  const int64_t budget = (kJitStaticSmem - fixed - 1024 * (int64_t)nl) / 8;  // float2 entries
   int64_t staged = 0;
   std::vector<int64_t> soff(ti.nops, -1);
   for (int o = 0; o < ti.nops; ++o) {
     const OpDev& op = a.ops[o];
-    if (op.kind != GBQ_OP_RDENSE) continue;
+    if (op.kind != GBQ_OP_RDENSE && op.kind != GBQ_OP_RPROBE) continue;
     const int lg = 2 * op.k;
     const int64_t dd = (int64_t)1 << lg, stride = op.nsel ? dd + 2 : dd;
     const int64_t cnt = dd << op.nsel;
@@ -414,14 +544,36 @@ std::string jit_source(const PassArgs& a) {
           << " + (e & " << dd - 1 << ")] = a.mats[" << (long long)op.mat << "ll + e];\n";
     staged += stride << op.nsel;
   }
-  int q = -1;            // current layout index
+  int q = -1;  // current layout index
   const OpDev* lay = nullptr;
-  int tbit[12];          // thread bit carrying tile bit c in the current layout, or -1
+  int tbit[13];  // thread bit carrying tile bit c in the current layout, or -1
   auto exit_layout = [&]() {
-    for (int s = 0; s < 16; ++s)
-      body << "      *reinterpret_cast<float2*>(sbb + (P" << q << " ^ " << hex(slot_off(*lay, s))
-           << ")) = v[" << s << "];\n";
+    for (int s = 0; s < NS; ++s) {
+      body << "      *reinterpret_cast<float2*>(sbb + (P" << q << " ^ " << hex(slot_off(*lay, s, R)) << ")) = v[" << s
+           << "];\n";
+      if (dual)
+        body << "      *reinterpret_cast<float2*>(sbw + (P" << q << " ^ " << hex(slot_off(*lay, s, R)) << ")) = w["
+             << s << "];\n";
+    }
     body << "      ops_barrier();\n";
+  };
+  auto matrix_ptr = [&](int o, const OpDev& op) {
+    const int dd = 1 << (2 * op.k);
+    const int stride = soff[o] >= 0 && op.nsel ? dd + 2 : dd;
+    std::ostringstream sel;
+    for (int s = 0; s < op.nsel; ++s) {
+      const int c = op.selg[s];
+      if (c >= 0)
+        sel << " + (((u32)t >> " << tbit[c] << ") & 1u) * " << (stride << s) << "u";
+      else
+        sel << " + ((u32)(gb >> " << (-c - 1) << ") & 1u) * " << (stride << s) << "u";
+    }
+    std::ostringstream out;
+    if (soff[o] >= 0)
+      out << "true>(v, w, mtab + (" << soff[o] << sel.str() << "))";
+    else
+      out << "false>(v, w, M + (" << (long long)op.mat << "ll" << sel.str() << "))";
+    return out.str();
   };
   for (int o = 0; o < ti.nops; ++o) {
     const OpDev& op = a.ops[o];
@@ -429,9 +581,9 @@ std::string jit_source(const PassArgs& a) {
       if (lay) exit_layout();
       ++q;
       lay = &op;
-      for (int c = 0; c < 12; ++c) tbit[c] = -1;
+      for (int c = 0; c < 13; ++c) tbit[c] = -1;
       for (int j = 0; j < 8; ++j)
-        for (int c = 0; c < 12; ++c)
+        for (int c = 0; c < L; ++c)
           if (op.tcol[j] == (1u << c)) tbit[c] = j;
       // per-thread shared byte offset of slot 0, kept in shared memory
       setup << "    {\n      u32 p = 0u;\n";
@@ -439,63 +591,89 @@ std::string jit_source(const PassArgs& a) {
         setup << "      if ((t >> " << j << ") & 1) p ^= " << hex(op.gcol[j] * 8u) << ";\n";
       setup << "      lent[" << q * 256 << " + t] = p;\n    }\n";
       body << "      const u32 P" << q << " = lent[" << q * 256 << " + t];\n";
-      for (int s = 0; s < 16; ++s)
+      for (int s = 0; s < NS; ++s) {
         body << "      v[" << s << "] = *reinterpret_cast<const float2*>(sbb + (P" << q << " ^ "
-             << hex(slot_off(op, s)) << "));\n";
+             << hex(slot_off(op, s, R)) << "));\n";
+        if (dual)
+          body << "      w[" << s << "] = *reinterpret_cast<const float2*>(sbw + (P" << q << " ^ "
+               << hex(slot_off(op, s, R)) << "));\n";
+      }
       continue;
     }
     if (op.kind == GBQ_OP_RDENSE) {
-      // matrix index: selector s = tile bit (a thread bit of the layout) or global bit
-      const int dd = 1 << (2 * op.k);
-      const int stride = soff[o] >= 0 && op.nsel ? dd + 2 : dd;
-      std::ostringstream sel;
-      for (int s = 0; s < op.nsel; ++s) {
-        const int c = op.selg[s];
-        if (c >= 0)
-          sel << " + (((u32)t >> " << tbit[c] << ") & 1u) * " << (stride << s) << "u";
-        else
-          sel << " + ((u32)(gb >> " << (-c - 1) << ") & 1u) * " << (stride << s) << "u";
-      }
-      if (soff[o] >= 0)
-        body << "      rdense<" << (int)op.rmask << ", true>(v, mtab + (" << soff[o] << sel.str() << "));\n";
-      else
-        body << "      rdense<" << (int)op.rmask << ", false>(v, M + (" << (long long)op.mat << "ll" << sel.str()
-             << "));\n";
+      body << "      rdense<" << (int)op.rmask << ", " << matrix_ptr(o, op) << ";\n";
       continue;
     }
-    // RDIAG: table index = thread part ^ global part ^ register-slot part
+    if (op.kind == GBQ_OP_RPROBE) {
+      body << "      pacc" << op.pidx << " += (double)rprobe<" << (int)op.rmask << ", " << matrix_ptr(o, op) << ";\n";
+      continue;
+    }
+    // RDIAG / RPROBE_DIAG: table index = thread part ^ global part ^ register-slot part
+    const bool probe = op.kind == GBQ_OP_RPROBE_DIAG;
     body << "      {\n        u32 base = 0u;\n";
-    for (int c = 0; c < 12; ++c)
+    for (int c = 0; c < L; ++c)
       if (op.dcol[c] && tbit[c] >= 0)
         body << "        if ((t >> " << tbit[c] << ") & 1) base ^= " << hex(op.dcol[c]) << ";\n";
     for (int j = 0; j < op.k && j < 8; ++j)
       if (op.dext[j] >= 0) body << "        base |= ((u32)(gb >> " << (int)op.dext[j] << ") & 1u) << " << j << ";\n";
     body << "        const float2* __restrict__ tab = M + " << (long long)op.mat << "ll;\n";
-    uint32_t rc[4];
-    for (int p = 0; p < 4; ++p) rc[p] = op.dcol[lay->rbits[p]];
-    for (int s = 0; s < 16; ++s) {
+    if (probe) body << "        float part = 0.f;\n";
+    uint32_t rc[5];
+    for (int p = 0; p < R; ++p) rc[p] = op.dcol[lay->rbits[p]];
+    for (int s = 0; s < NS; ++s) {
       uint32_t x = 0;
-      for (int p = 0; p < 4; ++p)
+      for (int p = 0; p < R; ++p)
         if ((s >> p) & 1) x ^= rc[p];
-      body << "        v[" << s << "] = cmul(__ldg(tab + (base ^ " << hex(x) << ")), v[" << s << "]);\n";
+      if (probe) {
+        body << "        {\n          const float2 y = cmul(__ldg(tab + (base ^ " << hex(x) << ")), v[" << s
+             << "]);\n          part = fmaf(w[" << s << "].x, y.x, fmaf(w[" << s << "].y, y.y, part));\n        }\n";
+      } else {
+        body << "        {\n          const float2 d = __ldg(tab + (base ^ " << hex(x) << "));\n          v[" << s
+             << "] = cmul(d, v[" << s << "]);\n";
+        if (dual) body << "          w[" << s << "] = cmul(d, w[" << s << "]);\n";
+        body << "        }\n";
+      }
     }
+    if (probe) body << "        pacc" << op.pidx << " += (double)part;\n";
     body << "      }\n";
   }
   if (lay) exit_layout();
+  std::ostringstream flush;
+  for (int i = 0; i < np; ++i) {
+    setup << "    double pacc" << i << " = 0.0;\n";
+    flush << "    probe_flush(pacc" << i << ", " << i << ", red);\n";
+  }
+  if (np) {
+    // probe totals of this CTA: into the partial of its first tile, zeros into
+    // those of its other tiles (the host sums over all tiles)
+    epi << "  __syncthreads();\n";
+    for (int o = 0; o < ti.nops; ++o) {
+      const OpDev& op = a.ops[o];
+      if (op.kind != GBQ_OP_RPROBE && op.kind != GBQ_OP_RPROBE_DIAG) continue;
+      epi << "  for (i64 tile = blockIdx.x + (i64)t * step; tile < a.ntiles; tile += 320 * step)\n"
+          << "    a.partial[(i64)" << op.slot << " * a.ntiles + tile] = tile == (i64)blockIdx.x ? red[" << op.pidx
+          << "] : 0.0;\n";
+    }
+  }
   std::string src(kJitSkeleton);
   auto put = [&](const char* key, const std::string& val) {
-    const size_t at = src.find(key);
-    if (at != std::string::npos) src.replace(at, strlen(key), val);
+    size_t at;
+    while ((at = src.find(key)) != std::string::npos) src.replace(at, strlen(key), val);
   };
   put("@SWZ0@", std::to_string(kSwzRow0));
   put("@SWZ1@", std::to_string(kSwzRow1));
   put("@SWZ2@", std::to_string(kSwzRow2));
   put("@SWZ3@", std::to_string(kSwzRow3));
+  put("@LT@", std::to_string(L));
+  put("@DUAL@", dual ? "1" : "0");
   put("@NL@", std::to_string(q + 1));
   put("@NM@", std::to_string(std::max<int64_t>(staged, 2)));
+  put("@NP@", std::to_string(std::max(np, 1)));
   put("@STAGE@", stage.str());
   put("@SETUP@", setup.str());
   put("@BODY@", body.str());
+  put("@EPILOGUE@", epi.str());
+  put("@FLUSH@", flush.str());
   return src;
 }
 
@@ -514,6 +692,7 @@ struct JitJob {
   std::string key;
   std::unique_ptr<PassArgs> args;
   int device;
+  bool dual;
 };
 struct JitState {
   std::mutex mu;
@@ -560,8 +739,9 @@ static void jit_load(JitKernel& k, const std::string& cubin) {
 
 // Cache key of a pass: its converted op records (zero-padded by
 // convert_op), which fix the generated source completely, and the device.
-std::string jit_key(const PassArgs& a, const Ctx* c) {
+std::string jit_key(const PassArgs& a, const Ctx* c, bool dual) {
   std::string k(reinterpret_cast<const char*>(&c->device), sizeof(c->device));
+  k.push_back(dual ? 'D' : 'S');
   k.append(reinterpret_cast<const char*>(a.ops), (size_t)a.ti.nops * sizeof(OpDev));
   return k;
 }
@@ -570,7 +750,7 @@ std::string jit_key(const PassArgs& a, const Ctx* c) {
 static void jit_build(JitJob& job) {
   JitState& S = jst();
   std::string log;
-  const std::string cubin = nvrtc_compile(jit_source(*job.args), &log);
+  const std::string cubin = nvrtc_compile(jit_source(*job.args, job.dual), &log);
   S.compiles.fetch_add(1);
   JitKernel k;
   k.log = log;
@@ -636,7 +816,7 @@ bool jit_enabled(Ctx* c) {
 // Queues the passes whose kernels are not cached (entry state 0 until a
 // worker has built them).  With wait, returns once every kernel of `passes`
 // is ready or has failed.
-void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes, bool wait) {
+void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes, bool dual, bool wait) {
   JitState& S = jst();
   std::unique_lock<std::mutex> lk(S.mu);
   if (S.stopping) return;
@@ -648,6 +828,7 @@ void jit_prepare(Ctx* c, std::vector<std::pair<std::string, PassArgs*>>& passes,
     job.key = p.first;
     job.args.reset(new PassArgs(*p.second));
     job.device = c->device;
+    job.dual = dual;
     S.queue.push_back(std::move(job));
     ++queued;
   }
@@ -686,18 +867,21 @@ static JitKernel* jit_ready(const std::string& key) {
 // Launches the specialised kernel of a pass; launched = false when the pass
 // is not eligible or its kernel is unavailable (the interpreter then runs).
 int jit_launch(Ctx* c, const PassArgs& a, const std::string& key, bool& launched) {
+  // the kernel's own state count is part of its key
   launched = false;
   JitKernel* k = jit_ready(key);
   if (!k) return GBQ_OK;
   JitArgs j;
   memset(&j, 0, sizeof(j));
   j.psi = a.psi;
+  j.lam = a.lam;
+  j.partial = a.ti.partial;
   j.mats = a.ti.mats;
   j.abort = a.abort;
   j.ntiles = a.ti.ntiles;
   j.nbits = a.ti.nbits;
   j.L = a.ti.L;
-  for (int b = 0; b < 12; ++b) j.gw[b] = a.ti.gw[b];
+  for (int b = 0; b < 13; ++b) j.gw[b] = a.ti.gw[b];
   memcpy(j.nt, a.ti.nt, sizeof(j.nt));
   int64_t grid = (int64_t)c->sm_count * k->blocks_per_sm;
   if (grid > a.ti.ntiles) grid = a.ti.ntiles;

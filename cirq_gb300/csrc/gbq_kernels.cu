@@ -339,6 +339,7 @@ __global__ void k_dm_expect_partial(const float2* rho, int nq, const gbq_pauli* 
 }
 
 // out_i = sum_t c_t * sign_t(i ^ x_t) * psi_{i ^ x_t},  c_t = coef_t * i^ny_t
+// (terms sorted by x_t by the caller)
 __global__ void k_apply_paulisum(const float2* psi, int nbits, const gbq_pauli* terms, int nterms,
                                  float2* out) {
   extern __shared__ float4 sterm[];  // per term: (x lo/hi bits packed), zy, c.re, c.im
@@ -355,19 +356,33 @@ __global__ void k_apply_paulisum(const float2* psi, int nbits, const gbq_pauli* 
   }
   __syncthreads();
   const uint64_t n = 1ull << nbits;
+  // terms come sorted by X mask: the coefficients of a run of equal masks
+  // are summed (with their signs at this index) and the amplitude is read
+  // once per run
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     float2 acc = make_float2(0.f, 0.f);
+    float2 cf = make_float2(0.f, 0.f);
+    uint64_t xcur = 0;
     for (int t = 0; t < nterms; ++t) {
       const float4 a = sterm[2 * t], c = sterm[2 * t + 1];
       const uint64_t x = (uint64_t)__float_as_uint(a.x) | ((uint64_t)__float_as_uint(a.y) << 32);
       const uint64_t zy = (uint64_t)__float_as_uint(a.z) | ((uint64_t)__float_as_uint(a.w) << 32);
-      const uint64_t k = i ^ x;
-      const float2 v = __ldg(psi + k);
-      const float sg = (__popcll(k & zy) & 1) ? -1.f : 1.f;
-      const float vr = sg * v.x, vi = sg * v.y;
-      acc.x = fmaf(c.x, vr, fmaf(-c.y, vi, acc.x));
-      acc.y = fmaf(c.x, vi, fmaf(c.y, vr, acc.y));
+      if (t > 0 && x != xcur) {
+        const float2 v = __ldg(psi + (i ^ xcur));
+        acc.x = fmaf(cf.x, v.x, fmaf(-cf.y, v.y, acc.x));
+        acc.y = fmaf(cf.x, v.y, fmaf(cf.y, v.x, acc.y));
+        cf = make_float2(0.f, 0.f);
+      }
+      xcur = x;
+      const float sg = (__popcll((i ^ x) & zy) & 1) ? -1.f : 1.f;
+      cf.x = fmaf(sg, c.x, cf.x);
+      cf.y = fmaf(sg, c.y, cf.y);
+    }
+    if (nterms > 0) {
+      const float2 v = __ldg(psi + (i ^ xcur));
+      acc.x = fmaf(cf.x, v.x, fmaf(-cf.y, v.y, acc.x));
+      acc.y = fmaf(cf.x, v.y, fmaf(cf.y, v.x, acc.y));
     }
     out[i] = acc;
   }

@@ -199,11 +199,14 @@ int gbq_cliff_validate(int nq, const gbq_cliff_op* ops, int nops, int ntables, i
 
 /* Pass-specialised kernels.  Every single-state pass of 12-bit tiles whose
  * ops are register layouts, register dense ops of width <= 2 and register
- * diagonals can run a kernel generated for its op records and compiled at
- * run time with NVRTC (cached per op-record sequence and device; worker
- * threads compile the new passes of a program in parallel).  The generated
- * kernel computes exactly what the interpreter computes, in the same order,
- * so results are bit-identical whichever kernel runs a pass.
+ * diagonals, and every two-state pass (gbq_run_dual) of 11-bit tiles whose
+ * ops are those and register probes, can run a kernel generated for its op
+ * records and compiled at run time with NVRTC (cached per op-record
+ * sequence and device; worker threads compile the new passes of a program
+ * in parallel).  The generated kernel computes exactly what the interpreter
+ * computes, in the same order, so states are bit-identical whichever kernel
+ * runs a pass (probe sums are reduced with atomics in either kernel, so
+ * they agree to rounding).
  * mode 0: off.  mode 1: a program's new kernels are compiled before its
  * first launch.  mode 2: they are compiled in the background and the
  * interpreter runs each pass until its kernel is ready (states of 20 or
@@ -220,9 +223,10 @@ int gbq_jit_stats(int64_t* compiles, int64_t* pending, int64_t* launches);
  * not built run on the interpreter. */
 int gbq_jit_shutdown(double timeout_s);
 /* The generated CUDA source of one pass (test and inspection hook; no GPU
- * needed).  *needed receives the size including the terminating zero;
- * GBQ_ERR_UNSUPPORTED if the pass has no specialised form. */
-int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, char* buf, size_t len,
+ * needed); dual != 0 for a two-state pass as gbq_run_dual runs it.  *needed
+ * receives the size including the terminating zero; GBQ_ERR_UNSUPPORTED if
+ * the pass has no specialised form. */
+int gbq_jit_source(int nbits, const gbq_pass* pass, const gbq_op* ops, int nops, int dual, char* buf, size_t len,
                    size_t* needed);
 /* Compiles a source with NVRTC for sm_103a (no GPU needed); *cubin_bytes
  * receives the size of the result.  GBQ_ERR_UNSUPPORTED with the compiler

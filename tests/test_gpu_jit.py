@@ -93,3 +93,27 @@ def test_background_compilation_switches_kernels_without_changing_results():
         sim.engine.set_jit(0)
     assert np.array_equal(first, plain)
     assert np.array_equal(second, plain)
+
+
+def test_specialised_two_state_passes_match_interpreter():
+    # adjoint gradient: forward passes (one state) and reverse passes (two
+    # states with probes) on the generated kernels against the interpreter;
+    # probe sums are reduced with atomics, so they agree to rounding
+    from cirq_gb300 import adjoint
+
+    circuit, symbols, values = workloads.hea_circuit(20, 4, seed=2)
+    ham = workloads.random_pauli_hamiltonian(20, 40, seed=3)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    eng = prog.engine
+    eng.set_jit(0)
+    e0, g0 = prog.value_and_grad(values)
+    before = eng.jit_launches()
+    eng.set_jit(1)
+    try:
+        e1, g1 = prog.value_and_grad(values)
+    finally:
+        eng.set_jit(0)
+    assert eng.jit_launches() - before > prog.reverse.npasses // 2
+    # the forward state is bit-identical; <psi|H|psi> is reduced with atomics
+    assert abs(e1 - e0) < 1e-12 * max(1.0, abs(e0))
+    assert np.allclose(g1, g0, rtol=1e-5, atol=1e-6), np.max(np.abs(g1 - g0))

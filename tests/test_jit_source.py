@@ -21,16 +21,16 @@ def _plan(n, depth):
     return cc.nbits_dev, cc.plan
 
 
-def _source(lib, nbits, plan, q):
+def _source(lib, nbits, plan, q, dual=0):
     passes = np.ascontiguousarray(plan.passes)
     ops = np.ascontiguousarray(plan.ops)
     need = ctypes.c_size_t(0)
-    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), None, 0,
+    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), dual, None, 0,
                             ctypes.byref(need))
     if rc:
         return rc, None
     buf = ctypes.create_string_buffer(need.value)
-    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), buf, need.value,
+    rc = lib.gbq_jit_source(nbits, passes[q:q + 1].ctypes.data, ops.ctypes.data, len(ops), dual, buf, need.value,
                             ctypes.byref(need))
     return rc, buf.value
 
@@ -59,5 +59,28 @@ def test_pass_without_specialised_form_is_refused():
     ops[0]["kind"], ops[0]["k"] = _lib.OP_DENSE, 3
     ops[0]["bits"][:3] = [0, 1, 2]
     need = ctypes.c_size_t(0)
-    rc = lib.gbq_jit_source(12, passes.ctypes.data, ops.ctypes.data, 1, None, 0, ctypes.byref(need))
+    rc = lib.gbq_jit_source(12, passes.ctypes.data, ops.ctypes.data, 1, 0, None, 0, ctypes.byref(need))
     assert rc == _lib.ERR_UNSUPPORTED
+
+
+def test_generated_two_state_pass_compiles():
+    # a reverse (two-state) pass of an adjoint program: probes and both states
+    from cirq_gb300 import adjoint
+
+    lib = _lib.load()
+    circuit, symbols, _ = workloads.hea_circuit(14, 2, seed=0)
+    ham = workloads.random_pauli_hamiltonian(14, 10, seed=1)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    plan = prog.reverse
+    for q in range(len(plan.passes)):
+        rc, src = _source(lib, prog.nbits, plan, q, dual=1)
+        if rc == 0 and b"rprobe<" in src:
+            break
+    else:
+        pytest.fail("no two-state pass with a probe has a specialised form")
+    assert b"probe_add" in src and b"a.partial" in src
+    size = ctypes.c_size_t(0)
+    rc = lib.gbq_jit_compile_check(src, ctypes.byref(size))
+    if rc == _lib.ERR_UNSUPPORTED and b"not found" in lib.gbq_last_error():
+        pytest.skip("NVRTC is not installed")
+    assert rc == 0, lib.gbq_last_error().decode()[:2000]
