@@ -78,7 +78,7 @@ def test_generated_two_state_pass_compiles():
             break
     else:
         pytest.fail("no two-state pass with a probe has a specialised form")
-    assert b"probe_add" in src and b"a.partial" in src
+    assert b"probe_flush" in src and b"a.partial" in src
     size = ctypes.c_size_t(0)
     rc = lib.gbq_jit_compile_check(src, ctypes.byref(size))
     if rc == _lib.ERR_UNSUPPORTED and b"not found" in lib.gbq_last_error():
