@@ -62,12 +62,23 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Probe accumulation: warp sums of v are added to the CTA's accumulator
-// acc[pidx] in shared memory (no barrier); the pass kernel writes the
-// accumulators once per CTA when its tiles are done.
-__device__ __forceinline__ void probe_add(double v, int pidx, double* acc) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc + pidx, v);
+// Probe accumulation: the warp's float sum of v is added (in double) to the
+// warp's own accumulator acc[pidx * kProbeWarps + warp] in shared memory (no
+// atomics, no barrier); the pass kernel sums the warps' accumulators and
+// writes them once per CTA when its tiles are done.
+constexpr int kProbeWarps = kThreads / 32;
+__device__ __forceinline__ void probe_add(float v, int pidx, double* acc) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) acc[pidx * kProbeWarps + (threadIdx.x >> 5)] += (double)v;
+}
+
+// A probe's CTA total: the sum of its warps' accumulators.
+__device__ __forceinline__ double probe_total(const double* acc, int pidx) {
+  double v = 0.0;
+#pragma unroll
+  for (int w = 0; w < kProbeWarps; ++w) v += acc[pidx * kProbeWarps + w];
+  return v;
 }
 
 // Block sum of v stored to *out by thread 0 (all threads must call).
@@ -213,7 +224,7 @@ __device__ __forceinline__ void op_dense(const TileInfo& ti, const OpDev& op, fl
         }
       }
     }
-    probe_add((double)part, op.pidx, red);
+    probe_add(part, op.pidx, red);
   } else {
     if constexpr (R > 1) __syncthreads();  // other threads still read this group
     if (!active) return;
@@ -314,7 +325,7 @@ __device__ __forceinline__ void op_diag(const TileInfo& ti, const OpDev& op, flo
     }
   }
   if constexpr (PROBE)
-    probe_add((double)part, op.pidx, red);
+    probe_add(part, op.pidx, red);
 }
 
 // KMAX: widest shared-memory dense op the kernel variant contains (0 or 5);
@@ -661,7 +672,7 @@ __device__ __forceinline__ void reg_dense(const TileInfo& ti, const OpDev& op,
     }
   }
   if constexpr (PROBE)
-    probe_add((double)part, op.pidx, red);
+    probe_add(part, op.pidx, red);
   (void)R;
 }
 
@@ -703,7 +714,7 @@ __device__ __forceinline__ void reg_diag(const TileInfo& ti, const OpDev& op,
     }
   }
   if constexpr (PROBE)
-    probe_add((double)part, op.pidx, red);
+    probe_add(part, op.pidx, red);
 }
 
 template <int LT, bool DUAL, bool PROBE, int RK, int M>
@@ -809,7 +820,7 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
   extern __shared__ float4 smraw[];
   __shared__ OpDev sops_sh[kParamOps ? 1 : GBQ_MAX_OPS_PER_PASS];
   __shared__ uint64_t ttab[3 * kTileTab];
-  __shared__ double red[GBQ_MAX_OPS_PER_PASS];  // probe accumulators (two-state passes)
+  __shared__ double red[DUAL ? GBQ_MAX_OPS_PER_PASS * kProbeWarps : 1];  // per-warp probe accumulators
   constexpr int TS = 1 << LT;
   constexpr int NS = DUAL ? 2 : 1;
   float2* buf = reinterpret_cast<float2*>(smraw);  // [kStages][NS][TS]
@@ -823,7 +834,7 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
   tile_tables_build(a.ti, ttab);
   const TileSetup ts = tile_setup<LT>(a.ti);
   if constexpr (DUAL) {
-    for (int i = threadIdx.x; i < GBQ_MAX_OPS_PER_PASS; i += kThreads) red[i] = 0.0;
+    for (int i = threadIdx.x; i < GBQ_MAX_OPS_PER_PASS * kProbeWarps; i += kThreads) red[i] = 0.0;
   }
   __syncthreads();
   const int64_t step = gridDim.x;
@@ -875,7 +886,7 @@ __global__ void __launch_bounds__(kThreads, (KMAX == 0 && RK <= 2 && !DUAL) ? 3 
       double* dst = a.ti.partial + (int64_t)op.slot * a.ti.ntiles;
       for (int64_t tile = blockIdx.x + (int64_t)threadIdx.x * step; tile < a.ti.ntiles;
            tile += (int64_t)kThreads * step)
-        dst[tile] = tile == (int64_t)blockIdx.x ? red[op.pidx] : 0.0;
+        dst[tile] = tile == (int64_t)blockIdx.x ? probe_total(red, op.pidx) : 0.0;
     }
   }
 }
