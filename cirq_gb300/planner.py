@@ -224,6 +224,9 @@ _F32_1E12 = int(np.array(1e-12, dtype=np.float32).view(np.int32))
 # recipe step kinds that read a gate matrix (gate index at step[1]) and the
 # kinds that only reshape; anything else disables point grouping for an op
 _GATE_STEPS = ("mul", "dmul", "dd", "init_diag", "init_dense", "probe")
+#: pools of one point are built by gbq_pool_build (the numpy replay stays
+#: for batches of points and as the checked reference of the native one)
+NATIVE_POOLS = True
 _GATE_FREE_STEPS = ("tx", "sx", "s2t", "dx")
 
 
@@ -273,6 +276,107 @@ class Plan:
                 tot += op.cost(0.0)
         return tot
 
+    def _native_program(self) -> np.ndarray:
+        """The layout's recipes as the int32 program of gbq_pool_build
+        (csrc/gbq_pool.cu), built once per plan."""
+        prog = self.__dict__.get("_native_prog")
+        if prog is not None:
+            return prog
+        words: list[int] = []
+
+        def dense_steps(recipe):
+            for st in recipe:
+                k = st[0]
+                if k == "init_dense":
+                    words.extend((1, st[1]))
+                elif k == "tx":
+                    words.extend((2, st[1]))
+                elif k == "sx":
+                    words.extend((3, st[1]))
+                elif k == "s2t":
+                    words.extend((4, st[1]))
+                elif k == "mul":
+                    words.extend((5, st[1], len(st[2]), *st[2]))
+                elif k == "dmul":
+                    _, gi, tpos, spos = st
+                    words.extend((6, gi, len(tpos)))
+                    words.extend(-1 if t is None else int(t) for t in tpos)
+                    words.extend(-1 if x is None else int(x) for x in spos)
+                elif k == "diag_as_dense":
+                    _, sub, bits, tg, sl = st
+                    words.extend((7, len(sub)))
+                    diag_steps(sub)
+                    words.extend((len(bits), *bits, len(tg), *tg, len(sl), *sl))
+                else:
+                    raise ValueError(k)
+
+        def diag_steps(recipe):
+            for st in recipe:
+                k = st[0]
+                if k == "init_diag":
+                    words.extend((8, st[1]))
+                elif k == "dx":
+                    words.extend((9, st[1]))
+                elif k == "dd":
+                    words.extend((10, st[1], len(st[2]), *st[2]))
+                else:
+                    raise ValueError(k)
+
+        for kind, recipe, off, shape, perm in self.layout:
+            code = {"dense": 0, "diag": 1, "probe": 2, "probe_diag": 3}[kind]
+            words.extend((code, off & 0xFFFFFFFF, off >> 32))
+            if kind == "dense":
+                ns, d = shape
+                words.extend((ns, d, int(perm is not None)))
+                if perm is not None:
+                    words.extend(int(x) for x in perm)
+                words.append(len(recipe))
+                dense_steps(recipe)
+            elif kind == "diag":
+                words.append(len(recipe))
+                diag_steps(recipe)
+            elif kind == "probe":
+                d = 1 << shape[0]
+                words.extend((recipe[0][1], d, int(perm is not None)))
+                if perm is not None:
+                    words.extend(int(x) for x in perm)
+            else:
+                words.append(recipe[0][1])
+        prog = np.asarray(words, dtype=np.int64).astype(np.int32)
+        self.__dict__["_native_prog"] = prog
+        return prog
+
+    def _native_pool(self, gates: dict) -> np.ndarray | None:
+        """The pool of one point through gbq_pool_build (None if the library
+        cannot be loaded)."""
+        try:
+            lib = _lib.load()
+        except Exception:  # noqa: BLE001  (no engine: the numpy replay runs)
+            return None
+        prog = self._native_program()
+        ng = (max(gates) + 1) if gates else 0
+        dims = np.zeros(max(ng, 1), dtype=np.int32)
+        offs = np.zeros(max(ng, 1), dtype=np.int64)
+        # one stacked block per matrix size
+        by_dim: dict = {}
+        for gi, g in gates.items():
+            by_dim.setdefault(g.shape[-1], []).append(gi)
+        blocks = []
+        at = 0
+        for d, gis in by_dim.items():
+            blocks.append(np.stack([gates[gi][0] for gi in gis]).astype(np.complex128, copy=False).reshape(-1))
+            idx = np.asarray(gis)
+            dims[idx] = d
+            offs[idx] = at + np.arange(len(gis), dtype=np.int64) * (d * d)
+            at += len(gis) * d * d
+        flat = np.ascontiguousarray(np.concatenate(blocks)) if blocks else np.zeros(1, np.complex128)
+        out = np.zeros((1, self.pool_len), dtype=np.complex64)
+        rc = lib.gbq_pool_build(prog.ctypes.data, len(prog), flat.ctypes.data, offs.ctypes.data, dims.ctypes.data,
+                                ng, out.ctypes.data, self.pool_len)
+        if rc != 0:
+            raise ValueError("gbq_pool_build rejected the plan's recipes")
+        return _snap(out)
+
     def pool_for(self, gates: dict, npoints: int, codes: dict | None = None) -> np.ndarray:
         """Recomputes the matrix pool for a batch: gates[gi] is (P, d, d).
 
@@ -282,8 +386,13 @@ class Plan:
         count as equal everywhere.  Each op is then built once per distinct
         combination of its gates and gathered to the points.
 
-        Returns complex64 (P, pool_len).
+        Returns complex64 (P, pool_len).  One point runs natively
+        (gbq_pool_build): the same steps as plain loops.
         """
+        if npoints == 1 and NATIVE_POOLS:
+            pool = self._native_pool(gates)
+            if pool is not None:
+                return pool
         out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
         dedupe = npoints > 1 and (codes is not None or any(
             np.asarray(g).ndim and np.asarray(g).strides[0] == 0 for g in gates.values()))

@@ -140,6 +140,17 @@ int gbq_device_name(gbq_ctx* ctx, char* buf, int len);
 /* Number of kernels this context has launched (for launch accounting). */
 int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
 
+/* Matrix pool of one parameter point from a plan's fused-op recipes (host
+ * only, no GPU): `prog` is the plan's int32 recipe program (layout of
+ * cirq_gb300/csrc/gbq_pool.cu), `gates` the point's gate matrices as
+ * complex128 (gate g at element gate_off[g], gate_dim[g] x gate_dim[g],
+ * row-major).  out receives pool_len complex64 entries (zero where no op
+ * writes).  Replaces the per-point replay of the planner's fusion recipes;
+ * the fused ops themselves replace the reference's per-gate
+ * apply_unitary calls (cirq-core/cirq/protocols/apply_unitary_protocol.py:306-418). */
+int gbq_pool_build(const int32_t* prog, int64_t prog_len, const double* gates, const int64_t* gate_off,
+                   const int32_t* gate_dim, int ngates, gbq_c64* out, int64_t pool_len);
+
 /* ---- Clifford circuits: reference tableau run + Pauli-frame shots ---------
  * Replaces the reference's per-repetition stabilizer simulation
  * (StabilizerSampler._run, cirq-core/cirq/sim/clifford/stabilizer_sampler.py:52-70;
