@@ -444,6 +444,7 @@ def adjoint_bench(n: int = 24, layers: int = 10, terms: int = 300, reps: int = 3
     ham = workloads.random_pauli_hamiltonian(n, terms, seed=1)
     prog = adjoint.AdjointProgram(circuit, ham, symbols)
     prog.value_and_grad(values)  # warm-up
+    prog.engine.jit_wait()  # steady state: the specialised kernels are built
     t = time.perf_counter()
     for _ in range(reps):
         e, g = prog.value_and_grad(values)
@@ -492,10 +493,16 @@ def density_bench(n: int = 13, depth: int = 16):
     r = sim.simulate(c)
     rho = r.final_density_matrix
     del r, rho  # its pinned host buffer returns to the pool for the timed call
-    t = time.perf_counter()
-    r = sim.simulate(c)
-    rho = r.final_density_matrix
-    dt = time.perf_counter() - t
+    sim.engine.jit_wait()  # steady state: the passes' specialised kernels are built
+    times = []
+    for _ in range(3):
+        t = time.perf_counter()
+        r = sim.simulate(c)
+        rho = r.final_density_matrix
+        times.append(time.perf_counter() - t)
+        if len(times) < 3:
+            del r, rho
+    dt = min(times)
     compiled = next(iter(sim._cache.values()))
     # the same passes with rho resident in HBM (the C3 roofline figure)
     ms, pass_ms, npass, _ = device_steps(sim.engine, compiled, 3, 2, True)
@@ -660,8 +667,10 @@ def c1_bench(n: int = 20, depth: int = 20, reps: int = 10_000, calls: int = 5):
     t = time.perf_counter()
     sim.simulate(circuit).final_state_vector
     first = time.perf_counter() - t
+    sim.engine.jit_wait()  # steady state: the specialised kernels are built
     ours_sim = timed(lambda: sim.simulate(circuit).final_state_vector, calls)
     sim.run(measured, repetitions=reps)
+    sim.engine.jit_wait()
     ours_run = timed(lambda: sim.run(measured, repetitions=reps), calls)
     ref = cirq.Simulator(dtype=np.complex64)
     ref_sim = timed(lambda: ref.simulate(circuit).final_state_vector, 1)
