@@ -456,19 +456,25 @@ def adjoint_bench(n: int = 24, layers: int = 10, terms: int = 300, reps: int = 3
     ps = adjoint.parameter_shift_gradient(sim, circuit, ham, symbols, values, indices=idx)
     t_ps = (time.perf_counter() - t) * len(symbols) / len(idx)
     # algorithmic HBM bytes of one gradient: forward passes (one read + one
-    # write of psi), lam = H psi (one read of psi per group of terms with the
-    # same X mask, one write of lam), <lam|psi> (two reads) and the reverse
-    # two-state passes (read + write of psi and lam)
+    # write of psi), lam = H psi (per tiled pass: a read of psi and a write
+    # of lam, plus a read of lam after the first; per group of wide terms
+    # with the same X mask: a read of psi, a read and a write of lam),
+    # <lam|psi> (two reads) and the reverse two-state passes (read + write
+    # of psi and lam)
     amp = 8 * (1 << prog.nbits)
     xgroups = len({t[0] for t in prog.terms})
-    alg_bytes = (2 * prog.forward.plan.npasses + xgroups + 1 + 2 + 4 * prog.reverse.npasses) * amp
+    hp_passes, hp_wide = prog.engine.paulisum_cover(prog.n, prog.terms)
+    # wide terms: more than nine X/Y factors on qubits 4 and up
+    wide_groups = len({t[0] for t in prog.terms if bin(t[0] >> 4).count("1") > 9}) if hp_wide else 0
+    hpsi = max(0, 3 * hp_passes - 1) + (wide_groups + 2 if hp_wide else 0)
+    alg_bytes = (2 * prog.forward.plan.npasses + hpsi + 2 + 4 * prog.reverse.npasses) * amp
     peak, peak_kind = peaks()
     return {
         "workload": f"HEA {n}q x {layers} layers ({len(symbols)} params), H = {terms} Pauli strings",
         "grads_per_s": 1.0 / t_adj,
         "hbm_bytes_per_grad": alg_bytes,
         "passes": {"forward": int(prog.forward.plan.npasses), "reverse_two_state": int(prog.reverse.npasses),
-                   "h_psi_x_groups": xgroups},
+                   "h_psi_x_groups": xgroups, "h_psi_tiled_passes": hp_passes, "h_psi_wide_terms": hp_wide},
         "hbm_frac_of_wall_time": alg_bytes / t_adj / 1e9 / peak,
         "hbm_frac_note": f"algorithmic bytes / wall time per gradient (host work included) / {peak_kind} hbm_gbs",
         "s_per_grad": t_adj,

@@ -217,6 +217,7 @@ SIGNATURES = {
     "gbq_dm_expect_paulis": [_P, _P, _I, _P, _I, _P],
     "gbq_sv_expect_paulis_noalloc": [_P, _P, _I, _P, _I, _P],
     "gbq_sv_apply_paulisum": [_P, _P, _I, _P, _I, _P],
+    "gbq_paulisum_cover": [_P, _I, _I, _P, _P, _P, _I],
     "gbq_sv_inner": [_P, _P, _P, _I, _P],
     "gbq_batch_expect": [_P, _P, _I, _P, _I, _P, _I, _P, _P, _I, _I, _P],
     "gbq_sv_project": [_P, _P, _I, _U64, _U64, _F],

@@ -30,8 +30,6 @@ int expect_chunk_bits(int nbits);
 int dm_expect_chunks(Ctx* c, int nq);
 int do_dm_expect(Ctx* c, const float2* rho, int nq, const gbq_pauli* d_terms, int nterms,
                  double* d_partial, double* d_out);
-int do_apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* d_terms, int nterms,
-                      float2* out);
 int do_inner(Ctx* c, const float2* a, const float2* b, int nbits, double* d_out);
 int do_reduce_slots(Ctx* c, const double* partial, int nslots, int64_t ntiles, double* out);
 
@@ -1153,24 +1151,19 @@ int gbq_sv_apply_paulisum(gbq_ctx* c, const gbq_c64* psi, int nbits, const gbq_p
     return arg_fail("gbq_sv_apply_paulisum: bad arguments (out must differ from psi)");
   int rc = validate_terms(terms, nterms, nbits);
   if (rc) return rc;
-  const size_t tbytes = (size_t)(nterms ? nterms : 1) * sizeof(gbq_pauli);
-  rc = ensure_scratch(c, tbytes);
+  rc = apply_paulisum(c, reinterpret_cast<const float2*>(psi), nbits, terms, nterms, reinterpret_cast<float2*>(out));
   if (rc) return rc;
-  gbq_pauli* d_terms = reinterpret_cast<gbq_pauli*>(c->scratch);
-  if (nterms) {
-    // terms with the same X mask read the same amplitude: the kernel
-    // reads it once per run of equal masks
-    std::vector<gbq_pauli> sorted(terms, terms + nterms);
-    std::stable_sort(sorted.begin(), sorted.end(), [](const gbq_pauli& a, const gbq_pauli& b) { return a.x < b.x; });
-    cudaError_t e = cudaMemcpyAsync(d_terms, sorted.data(), tbytes, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // `sorted` is pageable and local
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(terms)");
-  }
-  rc = do_apply_paulisum(c, reinterpret_cast<const float2*>(psi), nbits, d_terms, nterms,
-                         reinterpret_cast<float2*>(out));
-  if (rc) return rc;
-  // terms live in the shared scratch buffer: finish before it can be reused
+  // the term tables live in the shared scratch buffers: finish before they can be reused
   return sync(c, "gbq_sv_apply_paulisum");
+}
+
+int gbq_paulisum_cover(const gbq_pauli* terms, int nterms, int nbits, int* npasses, int* nwide, int* pass_terms,
+                       int max_passes) {
+  if (!npasses || !nwide || nbits < 0 || nbits > 40 || max_passes < 0 || (max_passes && !pass_terms))
+    return arg_fail("gbq_paulisum_cover: bad arguments");
+  const int rc = validate_terms(terms, nterms, nbits);
+  if (rc) return rc;
+  return paulisum_cover_stats(terms, nterms, nbits, npasses, nwide, pass_terms, max_passes);
 }
 
 int gbq_points_set_zero(gbq_ctx* c, gbq_c64* states, int nbits, int npoints) {

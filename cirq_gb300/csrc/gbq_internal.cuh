@@ -187,6 +187,14 @@ struct Ctx {
 int ensure_scratch(Ctx* c, size_t bytes);
 int ensure_host_scratch(Ctx* c, size_t bytes);
 
+// out (+)= H psi by the per-amplitude kernel (d_terms on the device, sorted by X mask)
+int do_apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* d_terms, int nterms,
+                      float2* out, int accumulate);
+// out = H psi: tiled passes over a cover of the X masks (host terms; uses both scratch buffers)
+int apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* terms, int nterms, float2* out);
+int paulisum_cover_stats(const gbq_pauli* terms, int nterms, int nbits, int* npasses, int* nwide,
+                         int* pass_terms, int max_passes);
+
 // Launchers (one translation unit per tile width; the 11- and 12-bit
 // two-state passes, and for 12 bits those with shared-memory dense ops, have
 // units of their own so the widest units compile in parallel).

@@ -136,10 +136,25 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// Per-thread probe accumulator over the CTA's tiles: a float-float pair
+// (hi, lo) updated by Knuth's TwoSum, with the rounding errors summed in lo
+// (Neumaier's compensated summation).  About 48 significant bits, like the
+// double it replaces, in FP32 instructions: FP64 issues at a small fraction
+// of the FP32 rate on this part, and a double add per probe per tile kept
+// the FP64 pipe half busy.
+struct ffacc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float b) {
+    const float s = hi + b;
+    const float bb = s - hi;
+    lo += (hi - (s - bb)) + (b - bb);
+    hi = s;
+  }
+};
 // A probe's per-thread total over the CTA's tiles into its accumulator
-// (once per CTA: the per-tile parts are added in double per thread).
-__device__ __forceinline__ void probe_flush(double v, int pidx, double* red) {
-  v = warp_sum(v);
+// (once per CTA, in double).
+__device__ __forceinline__ void probe_flush(const ffacc& f, int pidx, double* red) {
+  double v = warp_sum((double)f.hi + (double)f.lo);
   if ((threadIdx.x & 31) == 0) atomicAdd(red + pidx, v);
 }
 __host__ __device__ constexpr int popc_c(int x) { return x ? (x & 1) + popc_c(x >> 1) : 0; }
@@ -544,6 +559,18 @@ std::string jit_source(const PassArgs& a, bool dual) {
           << " + (e & " << dd - 1 << ")] = a.mats[" << (long long)op.mat << "ll + e];\n";
     staged += stride << op.nsel;
   }
+  // then the diagonal tables (2^k entries), read per tile with plain shared
+  // loads instead of read-only-cache loads that each gate the ops after them
+  for (int o = 0; o < ti.nops; ++o) {
+    const OpDev& op = a.ops[o];
+    if (op.kind != GBQ_OP_RDIAG && op.kind != GBQ_OP_RPROBE_DIAG) continue;
+    const int64_t cnt = (int64_t)1 << op.k;
+    if (staged + cnt > budget) continue;
+    soff[o] = staged;
+    stage << "  for (int e = t; e < " << cnt << "; e += 320) mtab[" << staged << " + e] = a.mats["
+          << (long long)op.mat << "ll + e];\n";
+    staged += cnt;
+  }
   int q = -1;  // current layout index
   const OpDev* lay = nullptr;
   int tbit[13];  // thread bit carrying tile bit c in the current layout, or -1
@@ -605,7 +632,7 @@ std::string jit_source(const PassArgs& a, bool dual) {
       continue;
     }
     if (op.kind == GBQ_OP_RPROBE) {
-      body << "      pacc" << op.pidx << " += (double)rprobe<" << (int)op.rmask << ", " << matrix_ptr(o, op) << ";\n";
+      body << "      pacc" << op.pidx << ".add(rprobe<" << (int)op.rmask << ", " << matrix_ptr(o, op) << ");\n";
       continue;
     }
     // RDIAG / RPROBE_DIAG: table index = thread part ^ global part ^ register-slot part
@@ -616,7 +643,14 @@ std::string jit_source(const PassArgs& a, bool dual) {
         body << "        if ((t >> " << tbit[c] << ") & 1) base ^= " << hex(op.dcol[c]) << ";\n";
     for (int j = 0; j < op.k && j < 8; ++j)
       if (op.dext[j] >= 0) body << "        base |= ((u32)(gb >> " << (int)op.dext[j] << ") & 1u) << " << j << ";\n";
-    body << "        const float2* __restrict__ tab = M + " << (long long)op.mat << "ll;\n";
+    const bool sh = soff[o] >= 0;
+    if (sh)
+      body << "        const float2* tab = mtab + " << soff[o] << ";\n";
+    else
+      body << "        const float2* __restrict__ tab = M + " << (long long)op.mat << "ll;\n";
+    auto tload = [&](uint32_t x) {
+      return sh ? "tab[base ^ " + hex(x) + "]" : "__ldg(tab + (base ^ " + hex(x) + "))";
+    };
     if (probe) body << "        float part = 0.f;\n";
     uint32_t rc[5];
     for (int p = 0; p < R; ++p) rc[p] = op.dcol[lay->rbits[p]];
@@ -625,22 +659,22 @@ std::string jit_source(const PassArgs& a, bool dual) {
       for (int p = 0; p < R; ++p)
         if ((s >> p) & 1) x ^= rc[p];
       if (probe) {
-        body << "        {\n          const float2 y = cmul(__ldg(tab + (base ^ " << hex(x) << ")), v[" << s
+        body << "        {\n          const float2 y = cmul(" << tload(x) << ", v[" << s
              << "]);\n          part = fmaf(w[" << s << "].x, y.x, fmaf(w[" << s << "].y, y.y, part));\n        }\n";
       } else {
-        body << "        {\n          const float2 d = __ldg(tab + (base ^ " << hex(x) << "));\n          v[" << s
+        body << "        {\n          const float2 d = " << tload(x) << ";\n          v[" << s
              << "] = cmul(d, v[" << s << "]);\n";
         if (dual) body << "          w[" << s << "] = cmul(d, w[" << s << "]);\n";
         body << "        }\n";
       }
     }
-    if (probe) body << "        pacc" << op.pidx << " += (double)part;\n";
+    if (probe) body << "        pacc" << op.pidx << ".add(part);\n";
     body << "      }\n";
   }
   if (lay) exit_layout();
   std::ostringstream flush;
   for (int i = 0; i < np; ++i) {
-    setup << "    double pacc" << i << " = 0.0;\n";
+    setup << "    ffacc pacc" << i << ";\n";
     flush << "    probe_flush(pacc" << i << ", " << i << ", red);\n";
   }
   if (np) {

@@ -338,10 +338,10 @@ __global__ void k_dm_expect_partial(const float2* rho, int nq, const gbq_pauli* 
   }
 }
 
-// out_i = sum_t c_t * sign_t(i ^ x_t) * psi_{i ^ x_t},  c_t = coef_t * i^ny_t
-// (terms sorted by x_t by the caller)
+// out_i (+)= sum_t c_t * sign_t(i ^ x_t) * psi_{i ^ x_t},  c_t = coef_t * i^ny_t
+// (terms sorted by x_t by the caller; accumulate: add to out)
 __global__ void k_apply_paulisum(const float2* psi, int nbits, const gbq_pauli* terms, int nterms,
-                                 float2* out) {
+                                 float2* out, int accumulate) {
   extern __shared__ float4 sterm[];  // per term: (x lo/hi bits packed), zy, c.re, c.im
   for (int t = threadIdx.x; t < nterms; t += blockDim.x) {
     const gbq_pauli tp = terms[t];
@@ -383,6 +383,10 @@ __global__ void k_apply_paulisum(const float2* psi, int nbits, const gbq_pauli* 
       const float2 v = __ldg(psi + (i ^ xcur));
       acc.x = fmaf(cf.x, v.x, fmaf(-cf.y, v.y, acc.x));
       acc.y = fmaf(cf.x, v.y, fmaf(cf.y, v.x, acc.y));
+    }
+    if (accumulate) {
+      const float2 o = out[i];
+      acc = make_float2(o.x + acc.x, o.y + acc.y);
     }
     out[i] = acc;
   }
@@ -534,7 +538,7 @@ int do_dm_expect(Ctx* c, const float2* rho, int nq, const gbq_pauli* d_terms, in
 }
 
 int do_apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* d_terms, int nterms,
-                      float2* out) {
+                      float2* out, int accumulate) {
   const uint64_t n = 1ull << nbits;
   const size_t smem = (size_t)nterms * 2 * sizeof(float4);
   if (smem > 200 * 1024) {
@@ -548,7 +552,7 @@ int do_apply_paulisum(Ctx* c, const float2* psi, int nbits, const gbq_pauli* d_t
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_apply_paulisum)");
     attr = smem;
   }
-  k_apply_paulisum<<<grid_for(c, n, 256), 256, smem, c->stream>>>(psi, nbits, d_terms, nterms, out);
+  k_apply_paulisum<<<grid_for(c, n, 256), 256, smem, c->stream>>>(psi, nbits, d_terms, nterms, out, accumulate);
   return check_launch(c, "k_apply_paulisum");
 }
 

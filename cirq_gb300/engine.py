@@ -402,6 +402,22 @@ class Engine:
             "gbq_sv_apply_paulisum",
         )
 
+    def paulisum_cover(self, nbits, terms, per_pass: bool = False) -> tuple:
+        """(tiled passes, terms left to the per-amplitude kernel) that
+        apply_paulisum uses for these terms; with per_pass, also the number
+        of terms of each pass."""
+        rec = self.pauli_records(terms)
+        npasses, nwide = ctypes.c_int(0), ctypes.c_int(0)
+        counts = np.zeros(max(1, len(rec)), dtype=np.int32)
+        check(
+            self.lib.gbq_paulisum_cover(rec.ctypes.data, len(rec), nbits, ctypes.byref(npasses), ctypes.byref(nwide),
+                                        counts.ctypes.data, len(counts)),
+            "gbq_paulisum_cover",
+        )
+        if per_pass:
+            return npasses.value, nwide.value, counts[: npasses.value].tolist()
+        return npasses.value, nwide.value
+
     def inner(self, a, b, nbits) -> complex:
         out = np.zeros(2, dtype=np.float64)
         check(self.lib.gbq_sv_inner(self.ctx, a.ptr, b.ptr, nbits, out.ctypes.data), "gbq_sv_inner")

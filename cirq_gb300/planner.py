@@ -913,6 +913,12 @@ class Planner:
                     return False
             return True
 
+        if R and ops and all(not targets(op) and reg_ok(op) for op in ops):
+            # diagonals only: one register phase on the top tile bits (every
+            # op of the pass then has a register form)
+            items.append(("layout", sorted(tile, reverse=True)[:R]))
+            items.extend(("op", op, True) for op in ops)
+            return items
         while remaining:
             first = remaining[0]
             if not R or not reg_ok(ops[first]) or (not targets(ops[first]) and not any(

@@ -86,8 +86,20 @@ def _expr_form(expr):
         form = ("const", float(expr))
     else:
         coeff, rest = expr.as_coeff_Mul()
+        num, den = sympy.fraction(expr)
+        ncoeff, nrest = num.as_coeff_Mul()
         if isinstance(rest, sympy.Symbol) and coeff.is_number:
             form = ("lin", float(coeff), rest)
+        elif den.is_number and den != 1 and isinstance(nrest, sympy.Symbol) and ncoeff.is_number:
+            # c * s / d (rx(t) gives t / pi): evaluated as (c * s) / d, kept
+            # only where that gives the lambdified expression's bits
+            form = ("div", float(ncoeff), float(den), nrest)
+            fn = sympy.lambdify((nrest,), expr, "numpy")
+            probe = np.random.RandomState(77).normal(size=16) * 4.0
+            want = np.array([float(fn(float(v))) for v in probe])
+            got = (form[1] * probe if form[1] != 1.0 else probe) / form[2]
+            if not np.array_equal(got.view(np.int64), want.view(np.int64)):
+                form = ("fn", fn, (nrest,))
         else:
             syms = tuple(sorted(expr.free_symbols, key=str))
             form = ("fn", sympy.lambdify(syms, expr, "numpy"), syms)
@@ -117,12 +129,63 @@ def _expr_values(expr, resolvers, values: dict | None) -> np.ndarray:
         v = np.full(len(resolvers), form[1])
     elif form[0] == "lin":
         v = form[1] * _expr_values(form[2], resolvers, values)
+    elif form[0] == "div":
+        v = _expr_values(form[3], resolvers, values)
+        v = (v if form[1] == 1.0 else form[1] * v) / form[2]
     else:
         args = [_expr_values(x, resolvers, values) for x in form[2]]
         v = np.broadcast_to(np.asarray(form[1](*args), dtype=np.float64), (len(resolvers),)).copy()
     if values is not None:
         values[expr] = v
     return v
+
+
+def _linear_exponents(exprs):
+    """(symbols, index, coef, div, const) when every expression is a
+    constant, a symbol, or a constant times a symbol over a constant (index
+    -1 for constants), else None."""
+    forms = [_expr_form(e) for e in exprs]
+    if not all(f[0] in ("sym", "lin", "div", "const") for f in forms):
+        return None
+    syms: list = []
+    pos: dict = {}
+    index = np.full(len(forms), -1, dtype=np.int64)
+    coef = np.ones(len(forms))
+    div = np.ones(len(forms))
+    const = np.zeros(len(forms))
+    for j, f in enumerate(forms):
+        if f[0] == "const":
+            const[j] = f[1]
+            continue
+        sym = f[1] if f[0] == "sym" else f[2] if f[0] == "lin" else f[3]
+        if f[0] in ("lin", "div"):
+            coef[j] = f[1]
+        if f[0] == "div":
+            div[j] = f[2]
+        if sym not in pos:
+            pos[sym] = len(syms)
+            syms.append(sym)
+        index[j] = pos[sym]
+    return syms, index, coef, div, const
+
+
+def _symbol_values(syms, resolvers) -> np.ndarray:
+    """(len(syms), P) values of plain symbols.  A symbol whose name maps to a
+    float or int in the resolver's dictionary takes that number (what
+    ParamResolver.value_of returns for it); anything else goes through
+    value_of."""
+    import sympy
+
+    out = np.empty((len(syms), len(resolvers)))
+    for p, r in enumerate(resolvers):
+        byname = {(k.name if isinstance(k, sympy.Symbol) else k): v for k, v in r.param_dict.items()}
+        for j, sym in enumerate(syms):
+            v = byname.get(sym.name)
+            if type(v) is float or type(v) is int:
+                out[j, p] = v
+            else:
+                out[j, p] = float(r.value_of(sym))
+    return out
 
 
 @dataclasses.dataclass
@@ -409,8 +472,25 @@ class CompiledCircuit:
         values: dict = {}
         out: dict = {}
         plain = [r.base if hasattr(r, "base") else r for r in resolvers]
-        for idx, exprs, H, Pm, conj in self._eigen_groups():
-            T = np.stack([_expr_values(e, plain, values) for e in exprs])  # (S, P)
+        lin_cache = self.__dict__.setdefault("_linear_exponent_cache", {})
+        for g, (idx, exprs, H, Pm, conj) in enumerate(self._eigen_groups()):
+            if g not in lin_cache:
+                lin_cache[g] = _linear_exponents(exprs)
+            lin = lin_cache[g]
+            if lin is None:
+                T = np.stack([_expr_values(e, plain, values) for e in exprs])  # (S, P)
+            else:
+                # constants, symbols and constant multiples of symbols: each
+                # symbol resolved once, the exponents by one gather
+                syms, index, coef, div, const = lin
+                sv = _symbol_values(syms, plain)
+                T = np.empty((len(exprs), len(plain)))
+                has = index >= 0
+                # (c * s) / d as _expr_values computes it (c = 1 and d = 1 exact)
+                T[has] = (coef[has, None] * sv[index[has]]) / div[has, None]
+                T[~has] = const[~has, None]
+                for sym, row in zip(syms, sv):
+                    values[sym] = row
             phase = np.exp(1j * np.pi * T[:, :, None] * H[:, None, :])  # (S, P, K)
             M = np.einsum("spk,skij->spij", phase, Pm)
             if conj.any():

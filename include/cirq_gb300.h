@@ -402,9 +402,19 @@ int gbq_sv64_compare(gbq_ctx* ctx, const void* state64, const gbq_c64* state32, 
  * (cirq-core/cirq/ops/pauli_string.py:734-760). */
 int gbq_dm_expect_paulis(gbq_ctx* ctx, const gbq_c64* rho, int nbits, const gbq_pauli* terms,
                          int nterms, double* out);
-/* out = sum_t coef_t P_t psi (a new state; used for lam = H psi). */
+/* out = sum_t coef_t P_t psi (a new state; used for lam = H psi).  The X
+ * masks are covered by tile bit-sets of 13 bits (bits 0..3 and nine more);
+ * one pass per bit-set applies every term whose X mask lies in it to tiles
+ * of the state held in shared memory.  Terms with more than nine X/Y factors
+ * on qubits 4 and up go through a per-amplitude kernel. */
 int gbq_sv_apply_paulisum(gbq_ctx* ctx, const gbq_c64* psi, int nbits, const gbq_pauli* terms,
                           int nterms, gbq_c64* out);
+/* The cover gbq_sv_apply_paulisum uses for these terms: number of tiled
+ * passes, of terms left to the per-amplitude kernel, and (pass_terms, up to
+ * max_passes entries; may be NULL when max_passes is 0) the terms of each
+ * pass.  Host only. */
+int gbq_paulisum_cover(const gbq_pauli* terms, int nterms, int nbits, int* npasses, int* nwide, int* pass_terms,
+                       int max_passes);
 /* out[j] = <a|b> as (re, im) in double. */
 int gbq_sv_inner(gbq_ctx* ctx, const gbq_c64* a, const gbq_c64* b, int nbits, double* out);
 
