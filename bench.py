@@ -11,10 +11,14 @@ Printed JSON line (rank 0):
   e2e        the same metric through cirq_gb300.Simulator.simulate() -- circuit
              in, final state vector out in host memory (H2D of the matrix pool
              and D2H of the 8 GiB state inside the timed region)
-  roofline   dominant kernel k_tile_ws: algorithmic bytes per launch
-             (16 B x 2^30: one read + one write of the state) / mean launch time
+  roofline   dominant kernel (k_jit, the pass-specialised tile kernels; k_tile_ws
+             where none is built): algorithmic bytes per launch (16 B x 2^30:
+             one read + one write of the state) / mean launch time
   cpu_baseline  the reference's numpy cirq.Simulator on a bounded gate sample
   fusion_sweep  gate-updates/s for fusion width k = 1..5
+
+`--extra-only NAME` runs one secondary workload (adjoint, density_matrix,
+clifford_sampling, ...) and prints its JSON.
 
 `--impl reference` times the reference (cirq.Simulator, complex64) on the
 host cores instead and prints the reference line.  Under torchrun with N > 1
@@ -798,6 +802,13 @@ def mma_bench(n: int = 30, reps: int = 3):
 
 
 # ---------------------------------------------------------------------------
+def extra_benches() -> dict:
+    """The secondary workloads reported under "extra" (name -> function)."""
+    return {"c1_20q": c1_bench, "adjoint": adjoint_bench, "density_matrix": density_bench,
+            "batch_sweep": batch_bench, "clifford_sampling": clifford_bench, "width_33": width33_bench,
+            "tensor_core_pipelined": tc_bench, "tensor_core_pass_11bit": mma_bench}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -816,12 +827,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the adjoint / density / batch lines")
+    ap.add_argument("--extra-only", default=None, help="run only this secondary workload and print its JSON")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
 
     if args.impl == "reference":
         return run_reference(args)
+    if args.extra_only:
+        _cirq()
+        benches = extra_benches()
+        if args.extra_only not in benches:
+            ap.error(f"--extra-only: one of {', '.join(benches)}")
+        print(json.dumps({args.extra_only: benches[args.extra_only]()}))
+        return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -915,10 +934,7 @@ def main():
 
     extra = {}
     if not args.no_extra and rank == 0:
-        for name, fn in (("c1_20q", c1_bench), ("adjoint", adjoint_bench), ("density_matrix", density_bench),
-                         ("batch_sweep", batch_bench), ("clifford_sampling", clifford_bench),
-                         ("width_33", width33_bench), ("tensor_core_pipelined", tc_bench),
-                         ("tensor_core_pass_11bit", mma_bench)):
+        for name, fn in extra_benches().items():
             try:
                 extra[name] = fn()
             except Exception as e:  # reported, not hidden
