@@ -39,7 +39,11 @@ cirq = ensure_cirq()
 
 
 class AdjointProgram:
-    """Forward and reverse programs of a parameterised circuit (compiled once)."""
+    """Forward and reverse programs of a parameterised circuit (compiled once).
+
+    `pass_budget` bounds the work the planner puts in one pass of the forward
+    program; `reverse_pass_budget` (default: the same) does so for the
+    two-state reverse sweep, whose passes read and write two states."""
 
     def __init__(
         self,
@@ -52,7 +56,8 @@ class AdjointProgram:
         tile_bits: int = 12,
         reverse_tile_bits: int = 11,
         fusion_max_qubits: int = 4,
-        pass_budget: float = 40.0,
+        pass_budget: float = 60.0,
+        reverse_pass_budget: float | None = None,
     ):
         self._engine = engine
         qubit_order = cirq.QubitOrder.DEFAULT if qubit_order is None else qubit_order
@@ -102,7 +107,8 @@ class AdjointProgram:
             rev.append(BitGate(bits=g.bits, matrix=g.matrix.conj().T, diagonal=g.diagonal))
             self._rev_src.append(("dagger", i, -1))
         rtb = max(MIN_TILE_BITS, min(reverse_tile_bits, self.nbits))
-        self.reverse_planner = Planner(tile_bits=rtb, kmax=2, budget=pass_budget)
+        rbudget = pass_budget if reverse_pass_budget is None else reverse_pass_budget
+        self.reverse_planner = Planner(tile_bits=rtb, kmax=2, budget=rbudget)
         for g in rev:
             if g.probe >= 0 and not g.diagonal and len(g.bits) > 3:
                 raise NotImplementedError("gradient of a gate on more than 3 qubits")
@@ -154,20 +160,25 @@ class AdjointProgram:
                 out[j] = (du[0] @ u.conj().T)[None]
         return out
 
-    def forward_state(self, values, overlap=None):
+    def forward_state(self, values, overlap=None, reuse: bool = False):
         """Runs the forward program; returns (psi, lam, E, resolver).
 
         `overlap(resolver, gates)` (optional) runs on the host while the
         forward passes execute on the GPU; its result is stored in
-        self._overlap_result."""
+        self._overlap_result.  With `reuse`, psi, lam and the pool live in
+        the program's own buffers (valid until the next reuse call);
+        otherwise they are new buffers that the caller frees."""
         eng = self.engine
         r = cirq.ParamResolver(dict(zip(self.symbols, [float(v) for v in values])))
         fwd = self.forward
         gates = fwd.gate_batch([r])
-        psi = eng.new_state(self.n, basis=0, nbits_dev=self.nbits)
+        sbytes = 8 << self.nbits
+        psi = eng.new_state(self.n, basis=0, nbits_dev=self.nbits,
+                            into=self._buffer("psi", sbytes) if reuse else None)
         pool = None
         if fwd.plan.npasses:
-            pool = eng.upload(np.ascontiguousarray(fwd.pool_from_batch(gates, 1)[0]))
+            host_pool = np.ascontiguousarray(fwd.pool_from_batch(gates, 1)[0])
+            pool = self._upload("forward_pool", host_pool) if reuse else eng.upload(host_pool)
             eng.run(psi, self.nbits, fwd.plan, pool, sync=False)
         # host work on a helper thread: the calls below wait for the GPU inside
         # the C library (ctypes releases the GIL), so it runs alongside them
@@ -181,12 +192,12 @@ class AdjointProgram:
             worker.start()
         if self.nbits > self.n:
             # padding amplitudes of lam stay zero; apply_paulisum writes the first 2^n
-            lam = eng.new_state(self.nbits, basis=0)
+            lam = eng.new_state(self.nbits, basis=0, into=self._buffer("lam", sbytes) if reuse else None)
         else:
-            lam = eng.alloc(8 << self.nbits)
+            lam = self._buffer("lam", sbytes) if reuse else eng.alloc(sbytes)
         try:
             eng.apply_paulisum(psi, self.n, self.terms, lam)  # synchronises: the forward pool is free
-            if pool is not None:
+            if pool is not None and not reuse:
                 pool.free()
             E = eng.inner(psi, lam, self.n).real
         finally:
@@ -197,16 +208,22 @@ class AdjointProgram:
     def _reverse_pool(self, resolver, gates=None) -> np.ndarray:
         return self.reverse.pool_for(self._reverse_batch(resolver, gates), 1)[0]
 
-    def gradient_from(self, psi, lam, resolver, reverse_pool=None) -> np.ndarray:
-        """Reverse sweep from (psi, lam) after the forward pass (consumes both)."""
+    def gradient_from(self, psi, lam, resolver, reverse_pool=None, reuse: bool = False) -> np.ndarray:
+        """Reverse sweep from (psi, lam) after the forward pass (consumes
+        both; with `reuse`, the pool and partials use the program's buffers)."""
         eng = self.engine
         grad = np.zeros(len(self.symbols))
         if self.nslots == 0:
             return grad
         pool = reverse_pool if reverse_pool is not None else self._reverse_pool(resolver)
-        pool_dev = eng.upload(np.ascontiguousarray(pool))
-        partial = eng.alloc(8 * self.nslots * self.reverse_tiles)
-        slots = eng.alloc(8 * self.nslots)
+        if reuse:
+            pool_dev = self._upload("reverse_pool", pool)
+            partial = self._buffer("partial", 8 * self.nslots * self.reverse_tiles)
+            slots = self._buffer("slots", 8 * self.nslots)
+        else:
+            pool_dev = eng.upload(np.ascontiguousarray(pool))
+            partial = eng.alloc(8 * self.nslots * self.reverse_tiles)
+            slots = eng.alloc(8 * self.nslots)
         eng.run_dual(psi, lam, self.nbits, self.reverse, pool_dev, partial)
         eng.reduce_slots(partial, self.nslots, self.reverse_tiles, slots)
         vals = np.empty(self.nslots, dtype=np.float64)
@@ -214,14 +231,36 @@ class AdjointProgram:
         np.add.at(grad, np.array(self.slot_symbol), 2.0 * vals)
         return grad
 
+    def _buffer(self, name: str, nbytes: int):
+        """A device buffer kept by the program for value_and_grad (reused
+        across calls: no cudaMalloc / cudaFree, which synchronises, per
+        gradient)."""
+        bufs = self.__dict__.setdefault("_buffers", {})
+        buf = bufs.get(name)
+        if buf is None or buf.nbytes < nbytes:
+            if buf is not None:
+                buf.free()
+            buf = bufs[name] = self.engine.alloc(max(nbytes, 16))
+        return buf
+
+    def release(self) -> None:
+        """Frees the device buffers value_and_grad keeps between calls."""
+        for buf in self.__dict__.pop("_buffers", {}).values():
+            buf.free()
+
+    def _upload(self, name: str, host: np.ndarray):
+        host = np.ascontiguousarray(host)
+        buf = self._buffer(name, host.nbytes)
+        buf.upload(host)
+        return buf
+
     def value_and_grad(self, values) -> tuple[float, np.ndarray]:
         # the reverse program's matrices are built on the host while the
-        # forward passes run on the GPU
+        # forward passes run on the GPU; states, pools and partials live in
+        # buffers the program keeps between calls
         overlap = self._reverse_pool if self.nslots else None
-        psi, lam, E, r = self.forward_state(values, overlap=overlap)
-        g = self.gradient_from(psi, lam, r, reverse_pool=self._overlap_result)
-        psi.free()
-        lam.free()
+        psi, lam, E, r = self.forward_state(values, overlap=overlap, reuse=True)
+        g = self.gradient_from(psi, lam, r, reverse_pool=self._overlap_result, reuse=True)
         return E, g
 
     def value_and_grad_native(self, values) -> tuple[float, np.ndarray]:

@@ -70,26 +70,44 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 // Pauli noise of one op on the 32 shots of word w: X with probability
 // p[0], Y p[1], Z p[2], each shot independently (thresholds on 32-bit
 // draws, single-precision probabilities).
+// Pauli noise on the 32 shots of one word: each shot independently gets X,
+// Y or Z with probabilities p[0], p[1], p[2].  The lanes with an error are
+// found by geometric skipping: the gap to the next error is
+// floor(ln U / ln(1 - p)) with p = p[0] + p[1] + p[2] and U uniform in
+// (0, 1] (ln U taken as log1p(-V), V = 1 - U, so that small p keeps its
+// resolution), and each error draws its type.  A word without an error
+// costs one hash instead of one per shot.
 __device__ __forceinline__ void noise_masks(const gbq_cliff_op& op, int o, int64_t w, uint64_t seed, uint32_t& mx,
                                             uint32_t& mz) {
-  const float scale = 4294967296.0f;
   const float c1 = op.p[0], c2 = c1 + op.p[1], c3 = c2 + op.p[2];
-  const uint32_t t1 = c1 >= 1.f ? 0xffffffffu : (uint32_t)(c1 * scale);
-  const uint32_t t2 = c2 >= 1.f ? 0xffffffffu : (uint32_t)(c2 * scale);
-  const uint32_t t3 = c3 >= 1.f ? 0xffffffffu : (uint32_t)(c3 * scale);
-  const uint32_t base = (uint32_t)rnd(seed, (uint64_t)o, (uint64_t)w);
   mx = 0u;
   mz = 0u;
-#pragma unroll 8
-  for (int lane = 0; lane < 32; ++lane) {
-    const uint32_t u = mix32(base ^ (0x9E3779B9u * (uint32_t)(lane + 1)));
+  if (!(c3 > 0.f)) return;
+  const float scale = 4294967296.0f;
+  // error type given an error: X below s1, Y below s2, Z above
+  const uint32_t s1 = c1 >= c3 ? 0xffffffffu : (uint32_t)((c1 / c3) * scale);
+  const uint32_t s2 = c2 >= c3 ? 0xffffffffu : (uint32_t)((c2 / c3) * scale);
+  const bool every = c3 >= 1.f;
+  const float inv_lq = every ? 0.f : 1.f / log1pf(-c3);  // 1 / ln(1 - p) < 0
+  const uint32_t base = (uint32_t)rnd(seed, (uint64_t)o, (uint64_t)w);
+  int lane = -1;
+  for (int it = 0; it < 32; ++it) {
+    int gap = 0;
+    if (!every) {
+      const uint32_t u = mix32(base ^ (0x9E3779B9u * (uint32_t)(2 * it + 1)));
+      const float g = log1pf(-(float)u * 2.3283064365386963e-10f) * inv_lq;  // >= 0, +inf for V = 1
+      gap = g < 32.f ? (int)g : 32;
+    }
+    lane += 1 + gap;
+    if (lane >= 32) break;
+    const uint32_t v = mix32(base ^ (0x85EBCA6Bu * (uint32_t)(2 * it + 2)));
     const uint32_t bit = 1u << lane;
-    if (u < t1) {
+    if (v < s1) {
       mx |= bit;
-    } else if (u < t2) {
+    } else if (v < s2) {
       mx |= bit;
       mz |= bit;
-    } else if (u < t3) {
+    } else {
       mz |= bit;
     }
   }

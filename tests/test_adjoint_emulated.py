@@ -70,3 +70,25 @@ def test_random_parameterized_circuits_vs_oracle_fd(seed, n, tile, rtile):
     assert abs(E - expectation_of_circuit(circuit, ham, r).real) < TOL
     fd = finite_difference_gradient(circuit, ham, symbols, values, h=1e-4)
     np.testing.assert_allclose(g, fd, atol=1e-5)
+
+
+def test_repeated_calls_reuse_buffers_and_match_fresh_ones():
+    circuit, symbols, _ = workloads.hea_circuit(5, 2, seed=3)
+    ham = workloads.random_pauli_hamiltonian(5, 9, seed=4)
+    eng = EmuEngine()
+    prog = adjoint.AdjointProgram(circuit, ham, symbols, engine=eng)
+    rng = np.random.default_rng(0)
+    points = [rng.uniform(-2, 2, len(symbols)) for _ in range(3)]
+    first = [prog.value_and_grad(v) for v in points]
+    kept = {k: b.ptr for k, b in prog._buffers.items()}
+    again = [prog.value_and_grad(v) for v in points]
+    assert {k: b.ptr for k, b in prog._buffers.items()} == kept  # no new buffers
+    for (e1, g1), (e2, g2) in zip(first, again):
+        assert e1 == e2 and np.array_equal(g1, g2)
+    for v, (e1, g1) in zip(points, first):
+        # the allocating path (as the torch autograd function uses it)
+        psi, lam, e, r = prog.forward_state(v)
+        g = prog.gradient_from(psi, lam, r)
+        assert e == e1 and np.array_equal(g, g1)
+    prog.release()
+    assert not getattr(prog, "_buffers", {})

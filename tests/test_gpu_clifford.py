@@ -194,3 +194,23 @@ def test_word_and_byte_outputs_agree():
     words = prog.sample_words(_eng(), reps, 77)
     bits = np.unpackbits(words.view(np.uint8), axis=1, bitorder="little")[:, :reps].T
     assert np.array_equal(bits, prog.sample_records(_eng(), reps, 77))
+
+
+def test_small_noise_rate_and_lane_uniformity():
+    # rare errors are placed by geometric skipping: the rate and the spread
+    # over the 32 shot positions of a word must match independent draws
+    q = cirq.LineQubit.range(2)
+    p = 2e-3
+    c = cirq.Circuit(cirq.bit_flip(p).on(q[0]), cirq.H(q[1]), cirq.phase_flip(0.05).on(q[1]), cirq.H(q[1]),
+                     cirq.measure(*q, key="m"))
+    reps = 1 << 22
+    m = _gpu_records(c, reps, 31, ["m"])["m"]
+    for col, pr in ((0, p), (1, 0.05)):
+        k = int(m[:, col].sum())
+        assert abs(k - pr * reps) < 5 * np.sqrt(reps * pr * (1 - pr)), (col, k)
+    lanes = np.bincount(np.nonzero(m[:, 0])[0] % 32, minlength=32)
+    expect = lanes.sum() / 32
+    chi2 = float(((lanes - expect) ** 2 / expect).sum())
+    from scipy.stats import chi2 as chi2_dist
+
+    assert chi2_dist.sf(chi2, 31) > 1e-4
