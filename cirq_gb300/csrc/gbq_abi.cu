@@ -8,8 +8,13 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <stdlib.h>
+#include <sys/mman.h>
+
 #include <algorithm>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "gbq_internal.cuh"
@@ -738,9 +743,41 @@ int gbq_free(gbq_ctx* c, void* dptr) {
   return GBQ_OK;
 }
 
+// Large pinned buffers are 2 MiB-aligned host memory advised for
+// transparent huge pages, each huge page touched once, then registered with
+// cudaHostRegister.  Measured on a GB300 host whose memory earlier processes
+// had used: 8 GiB device-to-host copies into cudaMallocHost memory took
+// 0.27-0.34 s in three of four tries, into this memory 0.0445 s every time
+// (the same as either on a fresh host).  Anything that fails falls back to
+// cudaMallocHost.
+static std::mutex g_host_mu;
+static std::unordered_map<void*, size_t> g_host_registered;
+static constexpr size_t kHugePage = 2u << 20;
+static constexpr size_t kHugeMin = 4u << 20;
+
+static void* host_alloc_huge(size_t n) {
+  const size_t len = (n + kHugePage - 1) & ~(kHugePage - 1);
+  void* p = nullptr;
+  if (posix_memalign(&p, kHugePage, len) != 0) return nullptr;
+  madvise(p, len, MADV_HUGEPAGE);  // advisory; small pages where none is free
+  for (size_t off = 0; off < len; off += kHugePage) static_cast<volatile char*>(p)[off] = 0;
+  if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+    cudaGetLastError();
+    free(p);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_registered[p] = len;
+  return p;
+}
+
 int gbq_host_alloc(size_t bytes, void** hptr) {
   if (!hptr) return arg_fail("null output pointer");
   const size_t n = bytes ? bytes : 16;
+  if (n >= kHugeMin) {
+    *hptr = host_alloc_huge(n);
+    if (*hptr) return GBQ_OK;
+  }
   cudaError_t e = cudaMallocHost(hptr, n);
   if (e != cudaSuccess) {
     *hptr = nullptr;
@@ -751,6 +788,17 @@ int gbq_host_alloc(size_t bytes, void** hptr) {
 
 int gbq_host_free(void* hptr) {
   if (!hptr) return GBQ_OK;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_registered.find(hptr);
+    if (it != g_host_registered.end()) {
+      g_host_registered.erase(it);
+      cudaError_t e = cudaHostUnregister(hptr);
+      free(hptr);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaHostUnregister");
+      return GBQ_OK;
+    }
+  }
   cudaError_t e = cudaFreeHost(hptr);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFreeHost");
   return GBQ_OK;

@@ -255,7 +255,11 @@ int gbq_pass_timing(gbq_ctx* ctx, double* total_ms, int64_t* launches);
 
 int gbq_alloc(gbq_ctx* ctx, size_t bytes, void** dptr);
 int gbq_free(gbq_ctx* ctx, void* dptr);
-int gbq_host_alloc(size_t bytes, void** hptr); /* pinned host memory */
+/* Pinned host memory.  From 4 MiB up: 2 MiB-aligned memory advised for
+ * transparent huge pages and registered with cudaHostRegister (copies keep
+ * full speed on a host whose memory is fragmented); cudaMallocHost below
+ * that or when registration fails.  Free with gbq_host_free. */
+int gbq_host_alloc(size_t bytes, void** hptr);
 int gbq_host_free(void* hptr);
 int gbq_h2d(gbq_ctx* ctx, void* dst, const void* src, size_t bytes);
 int gbq_d2h(gbq_ctx* ctx, void* dst, const void* src, size_t bytes);
@@ -370,8 +374,8 @@ int gbq_sv_expect_paulis(gbq_ctx* ctx, const gbq_c64* state, int nbits, const gb
  * implicit device synchronisation.  This entry point allocates nothing: its scratch
  * is a fixed GBQ_NOALLOC_SCRATCH_BYTES array in the library's device image,
  * present on every GPU that loads the library until the process exits, and
- * found with cudaGetSymbolAddress the first time it is called on a device --
- * make that first call before any stream capture.  `state` is a device
+ * found with cudaGetSymbolAddress the first time it is called on a device.
+ * `state` is a device
  * array, `terms` and `out` are host arrays (2 doubles per term, as for
  * gbq_sv_expect_paulis); work is ordered on `stream` (a cudaStream_t, NULL
  * for the default stream) and the call returns after it finished.  Term lists
