@@ -115,3 +115,22 @@ def test_hamiltonian_of_the_gradient_bench():
     npasses, nwide = _cover(prog.n, prog.terms)
     assert nwide == 0 and npasses < 60
     _check(prog.n, prog.terms, seed=5)
+
+
+def test_energy_at_bench_size_matches_per_term_expectations():
+    # 24 qubits, the gradient bench's 300-term H: <psi|H psi> through the
+    # tiled passes against the sum of the per-term expectation kernel's values
+    from cirq_gb300 import workloads
+    from cirq_gb300.adjoint import AdjointProgram
+
+    circuit, symbols, values = workloads.hea_circuit(24, 2, seed=0)
+    ham = workloads.random_pauli_hamiltonian(24, 300, seed=1)
+    prog = AdjointProgram(circuit, ham, symbols)
+    eng = prog.engine
+    psi, lam, e_tiled, _ = prog.forward_state(values)
+    per_term = eng.expect_paulis(psi, prog.n, prog.terms)
+    e_terms = float(np.sum(per_term).real)
+    scale = sum(abs(t[3]) for t in prog.terms)
+    assert abs(e_tiled - e_terms) <= 2e-6 * scale
+    psi.free()
+    lam.free()
