@@ -124,40 +124,73 @@ class AdjointProgram:
         return self._engine
 
     # ------------------------------------------------------------------
-    def _reverse_batch(self, resolver, gates: dict | None = None) -> dict:
-        """Reverse-program matrices at one point; `gates` are the forward
-        program's evaluated gate matrices at that point, when available."""
+    def _reverse_layout(self) -> dict:
+        """How each reverse-program entry is produced (computed once):
+        eigen-gate probes as a fixed generator times the exponent's
+        derivative, daggers of forward gates, and the rest one by one."""
+        lay = self.__dict__.get("_rev_layout")
+        if lay is not None:
+            return lay
+        import sympy
+
         fwd = self.forward
-        cache_u: dict = {}
-        values: dict = {}  # expression -> value at this point, shared by all gates
-        out = {}
-        gens = self.__dict__.setdefault("_generators", {})
+        gen_groups: dict = {}  # d -> (js, gens list, derivative exprs)
+        dag_groups: dict = {}  # d -> (js, forward source indices)
+        other: list = []
         for j, (kind, i, si) in enumerate(self._rev_src):
             src = fwd.sources[i]
             if kind != "dagger" and src.eigen is not None and src.transform == "u":
                 # U = sum_k exp(i pi t (h_k + s)) P_k with orthogonal projectors, so
                 # dU/dtheta U^dagger = i pi (dt/dtheta) sum_k (h_k + s) P_k: a fixed
                 # generator times the exponent's derivative at this point
-                key = (i, si)
-                g = gens.get(key)
-                if g is None:
-                    import sympy
-
-                    comps, shift, expr = src.eigen
-                    gen = 1j * np.pi * sum((h + shift) * np.asarray(p, dtype=np.complex128) for h, p in comps)
-                    g = gens[key] = (gen, sympy.diff(expr, self.symbols[si]))
-                gen, dexpr = g
-                dt = _expr_values(dexpr, [resolver], values)[0]
-                out[j] = (dt * gen)[None]
-                continue
-            if i not in cache_u:
-                cache_u[i] = gates[i][0] if gates is not None else src.matrices([resolver], values)[0]
-            u = cache_u[i]
-            if kind == "dagger":
-                out[j] = u.conj().T[None]
+                comps, shift, expr = src.eigen
+                gen = 1j * np.pi * sum((h + shift) * np.asarray(p, dtype=np.complex128) for h, p in comps)
+                g = gen_groups.setdefault(gen.shape[-1], ([], [], []))
+                g[0].append(j)
+                g[1].append(gen)
+                g[2].append(sympy.diff(expr, self.symbols[si]))
+            elif kind == "dagger":
+                d = fwd.gates[i].matrix.shape[-1]
+                g = dag_groups.setdefault(d, ([], []))
+                g[0].append(j)
+                g[1].append(i)
             else:
-                du = src.derivatives([resolver], self.symbols[si], values)
-                out[j] = (du[0] @ u.conj().T)[None]
+                other.append((j, kind, i, si))
+        lay = {
+            "gen": [(js, np.stack(gens), exprs) for js, gens, exprs in gen_groups.values()],
+            "dag": list(dag_groups.values()),
+            "other": other,
+        }
+        self.__dict__["_rev_layout"] = lay
+        return lay
+
+    def _reverse_batch(self, resolver, gates: dict | None = None) -> dict:
+        """Reverse-program matrices at one point; `gates` are the forward
+        program's evaluated gate matrices at that point, when available."""
+        fwd = self.forward
+        lay = self._reverse_layout()
+        values: dict = {}  # expression -> value at this point, shared by all gates
+        out: dict = {}
+        for js, gens, exprs in lay["gen"]:
+            dt = np.array([_expr_values(e, [resolver], values)[0] for e in exprs])
+            mats = dt[:, None, None] * gens
+            for k, j in enumerate(js):
+                out[j] = mats[k : k + 1]
+        cache_u: dict = {}
+
+        def forward_u(i):
+            if i not in cache_u:
+                cache_u[i] = gates[i][:1] if gates is not None else fwd.sources[i].matrices([resolver], values)[:1]
+            return cache_u[i]
+
+        for js, srcs in lay["dag"]:
+            daggers = np.concatenate([forward_u(i) for i in srcs]).conj().transpose(0, 2, 1)
+            for k, j in enumerate(js):
+                out[j] = daggers[k : k + 1]
+        for j, kind, i, si in lay["other"]:
+            u = forward_u(i)[0]
+            du = fwd.sources[i].derivatives([resolver], self.symbols[si], values)
+            out[j] = (du[0] @ u.conj().T)[None]
         return out
 
     def forward_state(self, values, overlap=None, reuse: bool = False):

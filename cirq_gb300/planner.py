@@ -354,21 +354,31 @@ class Plan:
         except Exception:  # noqa: BLE001  (no engine: the numpy replay runs)
             return None
         prog = self._native_program()
-        ng = (max(gates) + 1) if gates else 0
-        dims = np.zeros(max(ng, 1), dtype=np.int32)
-        offs = np.zeros(max(ng, 1), dtype=np.int64)
-        # one stacked block per matrix size
-        by_dim: dict = {}
-        for gi, g in gates.items():
-            by_dim.setdefault(g.shape[-1], []).append(gi)
-        blocks = []
-        at = 0
-        for d, gis in by_dim.items():
-            blocks.append(np.stack([gates[gi][0] for gi in gis]).astype(np.complex128, copy=False).reshape(-1))
-            idx = np.asarray(gis)
-            dims[idx] = d
-            offs[idx] = at + np.arange(len(gis), dtype=np.int64) * (d * d)
-            at += len(gis) * d * d
+        # one block per matrix size; the grouping depends only on the gate
+        # indices and sizes, which a program's batches share
+        key = tuple(gates)
+        groups_cache = self.__dict__.setdefault("_native_groups", {})
+        grp = groups_cache.get(key)
+        if grp is None:
+            ng = (max(gates) + 1) if gates else 0
+            dims = np.zeros(max(ng, 1), dtype=np.int32)
+            offs = np.zeros(max(ng, 1), dtype=np.int64)
+            by_dim: dict = {}
+            for gi, g in gates.items():
+                by_dim.setdefault(g.shape[-1], []).append(gi)
+            at = 0
+            for d, gis in by_dim.items():
+                idx = np.asarray(gis)
+                dims[idx] = d
+                offs[idx] = at + np.arange(len(gis), dtype=np.int64) * (d * d)
+                at += len(gis) * d * d
+            grp = (list(by_dim.values()), dims, offs, ng)
+            if len(groups_cache) >= 8:
+                groups_cache.clear()
+            groups_cache[key] = grp
+        order, dims, offs, ng = grp
+        blocks = [np.concatenate([gates[gi][:1] for gi in gis]).astype(np.complex128, copy=False).reshape(-1)
+                  for gis in order]
         flat = np.ascontiguousarray(np.concatenate(blocks)) if blocks else np.zeros(1, np.complex128)
         out = np.zeros((1, self.pool_len), dtype=np.complex64)
         rc = lib.gbq_pool_build(prog.ctypes.data, len(prog), flat.ctypes.data, offs.ctypes.data, dims.ctypes.data,
