@@ -84,3 +84,45 @@ def test_generated_two_state_pass_compiles():
     if rc == _lib.ERR_UNSUPPORTED and b"not found" in lib.gbq_last_error():
         pytest.skip("NVRTC is not installed")
     assert rc == 0, lib.gbq_last_error().decode()[:2000]
+
+
+def test_all_diagonal_passes_get_a_register_phase_and_a_specialised_form():
+    # rz layers and CZ ladders only: every pass is diagonal, and each must be
+    # one register phase (LAYOUT then register diagonals) with a generated source
+    q = cirq.LineQubit.range(16)
+    import sympy
+
+    syms = sympy.symbols("z0:16")
+    c = cirq.Circuit([cirq.rz(s).on(qq) for s, qq in zip(syms, q)],
+                     [cirq.CZ(q[i], q[i + 1]) for i in range(15)],
+                     [cirq.ZZ(q[i], q[(i + 5) % 16]) ** 0.3 for i in range(16)])
+    r = cirq.ParamResolver({s: 0.1 * (i + 1) for i, s in enumerate(syms)})
+    cc = CompiledCircuit(list(c.all_operations()), q, dm=False, planner=Planner(budget=25.0), resolvers=[r])
+    plan = cc.plan
+    lib = _lib.load()
+    for p in range(len(plan.passes)):
+        rec = plan.passes[p]
+        kinds = plan.ops["kind"][rec["op_begin"]: rec["op_begin"] + rec["op_count"]]
+        assert kinds[0] == _lib.OP_LAYOUT
+        assert set(kinds[1:].tolist()) <= {_lib.OP_RDIAG}
+        rc, src = _source(lib, cc.nbits_dev, plan, p)
+        assert rc == 0 and b"tab[base" in src  # tables staged in shared memory
+
+
+def test_two_state_diagonal_passes_have_specialised_forms():
+    from cirq_gb300 import adjoint
+
+    circuit, symbols, _ = workloads.hea_circuit(14, 2, seed=0)
+    ham = workloads.random_pauli_hamiltonian(14, 10, seed=1)
+    prog = adjoint.AdjointProgram(circuit, ham, symbols)
+    plan = prog.reverse
+    lib = _lib.load()
+    diag_only = 0
+    for p in range(len(plan.passes)):
+        rec = plan.passes[p]
+        kinds = set(plan.ops["kind"][rec["op_begin"] + 1: rec["op_begin"] + rec["op_count"]].tolist())
+        if kinds <= {_lib.OP_RDIAG, _lib.OP_RPROBE_DIAG}:
+            diag_only += 1
+        rc, _ = _source(lib, prog.nbits, plan, p, dual=1)
+        assert rc == 0, p
+    assert diag_only > 0
