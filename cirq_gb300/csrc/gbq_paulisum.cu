@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(kPsThreads, 2) k_paulisum_tile(PsArgs a) {
     unsigned long long g = 0;
     for (int j = 0; j < a.ng; ++j) g |= (unsigned long long)((tile >> j) & 1) << a.gpos[j];
     __syncthreads();  // the previous tile's readers of s and sc are done; dep tables written
+#pragma unroll 8
     for (int l = t; l < nl; l += kPsThreads) s[l] = __ldg(a.psi + (g | dep_lo[l & 127] | dep_hi[l >> 7]));
     for (int k = t; k < a.nt; k += kPsThreads) {
       const PsTerm tm = a.terms[k];
@@ -93,9 +94,15 @@ __global__ void __launch_bounds__(kPsThreads, 2) k_paulisum_tile(PsArgs a) {
     }
     __syncthreads();
     for (int l0 = t; l0 < nl; l0 += kPsThreads * kPsChunk) {
+      // passes after the first add to out: its 8 old values are loaded
+      // here, all in flight together, and land while the terms are summed
+      // (loaded next to their stores, each would wait a full HBM round trip)
       float2 acc[kPsChunk];
 #pragma unroll
-      for (int k = 0; k < kPsChunk; ++k) acc[k] = make_float2(0.f, 0.f);
+      for (int k = 0; k < kPsChunk; ++k) {
+        const int l = l0 + k * kPsThreads;
+        acc[k] = (!a.first && l < nl) ? a.out[g | dep_lo[l & 127] | dep_hi[l >> 7]] : make_float2(0.f, 0.f);
+      }
       if (FULL) {
         const uint32_t lb = (uint32_t)l0;
         for (int q = 0; q < a.nt; ++q) {
@@ -135,15 +142,7 @@ __global__ void __launch_bounds__(kPsThreads, 2) k_paulisum_tile(PsArgs a) {
 #pragma unroll
       for (int k = 0; k < kPsChunk; ++k) {
         const int l = l0 + k * kPsThreads;
-        if (l < nl) {
-          float2* p = a.out + (g | dep_lo[l & 127] | dep_hi[l >> 7]);
-          if (a.first) {
-            *p = acc[k];
-          } else {
-            const float2 o = *p;
-            *p = make_float2(o.x + acc[k].x, o.y + acc[k].y);
-          }
-        }
+        if (l < nl) a.out[g | dep_lo[l & 127] | dep_hi[l >> 7]] = acc[k];
       }
     }
   }
