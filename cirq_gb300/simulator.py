@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import collections
 import math
+import threading
 import warnings
 from typing import Any, Iterator, Sequence
 
@@ -56,6 +57,39 @@ def _check_dtype(dtype):
             f"cirq_gb300 simulates in complex64 only (got {np.dtype(dtype)}); "
             "use dtype=np.complex64"
         )
+
+
+_MEMO_LOCK = threading.Lock()
+_SPLIT_MEMO: collections.OrderedDict = collections.OrderedDict()
+
+
+def _memo(store: collections.OrderedDict, program, name, fn):
+    """fn(program), remembered per circuit object for as long as it holds
+    the same moment objects.  Moments are immutable, so the same moments are
+    the same operations.  The entry keeps the moments alive, so a reused
+    id() cannot match another circuit."""
+    moments = getattr(program, "moments", None)
+    if moments is None:
+        return fn(program)
+    moments = tuple(moments)
+    key = (id(program), name)
+    with _MEMO_LOCK:
+        hit = store.get(key)
+        if hit is not None and len(hit[0]) == len(moments) and all(a is b for a, b in zip(hit[0], moments)):
+            store.move_to_end(key)
+            return hit[1]
+    val = fn(program)
+    with _MEMO_LOCK:
+        store[key] = (moments, val)
+        while len(store) > 128:
+            store.popitem(last=False)
+    return val
+
+
+def _split_terminal(program):
+    """split_measurements(program) as tuples, remembered per circuit."""
+    return _memo(_SPLIT_MEMO, program, "split",
+                 lambda p: tuple(tuple(part) for part in split_measurements(p)))
 
 
 def _check_all_resolved(program, resolver) -> None:
@@ -217,7 +251,18 @@ class _GpuSimulatorBase:
         return noisy(prefix) + cirq.Circuit(kept) + cirq.Circuit(suffix_ops)
 
     def _compile(self, body_ops, qubits, resolvers) -> CompiledCircuit:
-        key = structure_key(body_ops, qubits, self._dm, self.planner)
+        # the key of a remembered (identical) body tuple is computed once
+        keys = self.__dict__.setdefault("_key_memo", {})
+        mk = (id(body_ops), tuple(qubits))
+        hit = keys.get(mk)
+        if hit is not None and hit[0] is body_ops:
+            key = hit[1]
+        else:
+            key = structure_key(body_ops, qubits, self._dm, self.planner)
+            if isinstance(body_ops, tuple):
+                if len(keys) > 128:
+                    keys.clear()
+                keys[mk] = (body_ops, key)
         c = self._cache.get(key)
         if c is not None:
             self._cache.move_to_end(key)
@@ -246,7 +291,7 @@ class _GpuSimulatorBase:
         # reference), checked before anything is compiled
         for r in resolvers or [cirq.ParamResolver({})]:
             _check_all_resolved(program, r)
-        body, meas = split_measurements(program)
+        body, meas = _split_terminal(program)
         self._noisy_ops(None, qubits)  # noise is placed by the entry points
         compiled = self._compile(body, qubits, resolvers or [cirq.ParamResolver({})])
         return qubits, resolvers, compiled, meas
@@ -349,14 +394,17 @@ class _GpuSimulatorBase:
         return [int(b) for b in _recorded_in_place(bits, op, self._prng)[0]]
 
     def _traj_needed(self, program) -> bool:
-        """Does this circuit need per-repetition trajectories?"""
+        """Does this circuit need per-repetition trajectories?  (Remembered
+        per circuit: the answer depends only on its operations and on this
+        simulator's kind and noise.)"""
         from cirq_gb300.ir import flatten_ops
 
         if not program.all_qubits():
             return False
         if not self._dm and self.noise is not cirq.NO_NOISE:
             return True
-        return _traj.needs_trajectories(flatten_ops(program), self._dm)
+        store = self.__dict__.setdefault("_traj_memo", collections.OrderedDict())
+        return _memo(store, program, "traj", lambda p: _traj.needs_trajectories(flatten_ops(p), self._dm))
 
     def _traj_states(self, program, qubits, resolver, initial_state, reps, records_only=False):
         """Yields (runner, device state, records) for `reps` trajectories; the
