@@ -26,10 +26,13 @@ class DeviceBuffer:
     def __init__(self, engine: "Engine", nbytes: int):
         self.engine = engine
         self.nbytes = int(nbytes)
-        p = ctypes.c_void_p()
-        check(engine.lib.gbq_alloc(engine.ctx, self.nbytes, ctypes.byref(p)), "gbq_alloc")
-        self.ptr = p.value
-        self._fin = weakref.finalize(self, Engine._free, engine.lib, engine.ctx, self.ptr)
+        ptr = engine._take_spare(self.nbytes)
+        if ptr is None:
+            p = ctypes.c_void_p()
+            check(engine.lib.gbq_alloc(engine.ctx, self.nbytes, ctypes.byref(p)), "gbq_alloc")
+            ptr = p.value
+        self.ptr = ptr
+        self._fin = weakref.finalize(self, engine._release, self.nbytes, self.ptr)
 
     def free(self) -> None:
         self._fin()
@@ -138,6 +141,9 @@ class Engine:
         self.total_bytes = total.value
         self.pinned = PinnedArrayPool(self.lib)
         self._pool_cache: dict = {}
+        self._spare: dict[int, list[int]] = {}
+        self._spare_bytes = 0
+        self._spare_lock = threading.Lock()
 
     @classmethod
     def get(cls, device: int = 0) -> "Engine":
@@ -154,6 +160,37 @@ class Engine:
             lib.gbq_free(ctx, ptr)
         except Exception:
             pass
+
+    # Freed buffers of up to SPARE_MAX bytes are kept (SPARE_TOTAL in all)
+    # and handed out again for the same size: a small simulate() then needs
+    # no cudaMalloc and no synchronising cudaFree.  Reuse is safe because all
+    # of the engine's work is ordered on its one stream.
+    SPARE_MAX = 64 << 20
+    SPARE_TOTAL = 256 << 20
+
+    def _take_spare(self, nbytes: int):
+        with self._spare_lock:
+            lst = self._spare.get(nbytes)
+            if not lst:
+                return None
+            self._spare_bytes -= nbytes
+            return lst.pop()
+
+    def _release(self, nbytes: int, ptr: int) -> None:
+        with self._spare_lock:
+            if nbytes <= self.SPARE_MAX and self._spare_bytes + nbytes <= self.SPARE_TOTAL:
+                self._spare.setdefault(nbytes, []).append(ptr)
+                self._spare_bytes += nbytes
+                return
+        Engine._free(self.lib, self.ctx, ptr)
+
+    def release_spare(self) -> None:
+        """Frees the kept buffers."""
+        with self._spare_lock:
+            spare, self._spare, self._spare_bytes = self._spare, {}, 0
+        for ptrs in spare.values():
+            for ptr in ptrs:
+                Engine._free(self.lib, self.ctx, ptr)
 
     # ---- buffers -------------------------------------------------------
     def alloc(self, nbytes: int) -> DeviceBuffer:

@@ -538,7 +538,12 @@ class CompiledCircuit:
 
     @property
     def parameterized(self) -> bool:
-        return any(self.sources[i].const is None for i in self.kept)
+        # fixed once the plan's gates are chosen (kept); remembered for them
+        hit = self.__dict__.get("_parameterized")
+        if hit is None or hit[0] is not self.kept:
+            hit = (self.kept, any(self.sources[i].const is None for i in self.kept))
+            self.__dict__["_parameterized"] = hit
+        return hit[1]
 
     def pool(self, resolvers) -> np.ndarray:
         """complex64 (P, pool_len) matrix pools for the resolvers."""

@@ -112,7 +112,12 @@ def _check_all_resolved(program, resolver) -> None:
 
 def _symbolic_repetitions(program) -> bool:
     """Does a CircuitOperation of `program` repeat a symbolic number of
-    times?  Its structure is then known only per sweep point."""
+    times?  Its structure is then known only per sweep point.  (Remembered
+    per circuit.)"""
+    return _memo(_SPLIT_MEMO, program, "symbolic_repetitions", _symbolic_repetitions_of)
+
+
+def _symbolic_repetitions_of(program) -> bool:
     gate_op = cirq.GateOperation
     for op in program.all_operations():
         if type(op) is gate_op:
@@ -121,7 +126,7 @@ def _symbolic_repetitions(program) -> bool:
         if isinstance(u, cirq.ClassicallyControlledOperation):
             u = u.without_classical_controls().untagged
         if isinstance(u, cirq.CircuitOperation):
-            if cirq.is_parameterized(u.repetitions) or _symbolic_repetitions(u.circuit):
+            if cirq.is_parameterized(u.repetitions) or _symbolic_repetitions_of(u.circuit):
                 return True
     return False
 
