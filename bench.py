@@ -18,7 +18,8 @@ Printed JSON line (rank 0):
   fusion_sweep  gate-updates/s for fusion width k = 1..5
 
 `--extra-only NAME` runs one secondary workload (adjoint, density_matrix,
-clifford_sampling, ...) and prints its JSON.
+clifford_sampling, ...) and prints its JSON (with --no-cpu, the Clifford
+line skips timing the reference's sampler).
 
 `--impl reference` times the reference (cirq.Simulator, complex64) on the
 host cores instead and prints the reference line.  Under torchrun with N > 1
@@ -842,7 +843,12 @@ def main():
         benches = extra_benches()
         if args.extra_only not in benches:
             ap.error(f"--extra-only: one of {', '.join(benches)}")
-        print(json.dumps({args.extra_only: benches[args.extra_only]()}))
+        fn = benches[args.extra_only]
+        if args.no_cpu and args.extra_only == "clifford_sampling":
+            result = fn(ref_shots=0)  # the reference sampler takes about a minute per shot
+        else:
+            result = fn()
+        print(json.dumps({args.extra_only: result}))
         return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
