@@ -180,6 +180,7 @@ SIGNATURES = {
     "gbq_set_graphs": [_P, _I],
     "gbq_set_jit": [_P, _I],
     "gbq_pool_build": [_P, _I64, _P, _P, _P, _I, _P, _I64],
+    "gbq_pool_build_points": [_P, _I64, _P, _I64, _P, _P, _I, _I, _P, _I64, _I],
     "gbq_cliff_validate": [_I, _P, _I, _I, _I, _I],
     "gbq_cliff_reference": [_P, _I, _P, _I, _P, _I, _P, _I, _I, _P],
     "gbq_cliff_sample": [_P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _I64, _U64, _P, _P, _I, _I],

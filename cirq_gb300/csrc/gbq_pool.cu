@@ -30,6 +30,9 @@
 
 #include <complex>
 #include <string>
+#include <algorithm>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include "gbq_internal.cuh"
@@ -266,14 +269,30 @@ static void run_dense_steps(Reader& r, int nsteps, const Gates& g, Dense& M) {
   }
 }
 
+// Pool entries as complex64, with real and imaginary parts whose magnitude
+// is below 1e-12 (compared on the float32 bit pattern) stored as +0: the
+// planner's snap of the numpy replay, so that both give the same bits.
+static float snapped(double x) {
+  static const uint32_t kSnap = [] {
+    const float f = 1e-12f;
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return b;
+  }();
+  const float f = (float)x;
+  uint32_t b;
+  memcpy(&b, &f, 4);
+  return (b & 0x7fffffffu) < kSnap ? 0.0f : f;
+}
+
 static void put(gbq_c64* out, int64_t len, int64_t off, const std::vector<cd>& v, bool& ok) {
   if (off < 0 || off + (int64_t)v.size() > len) {
     ok = false;
     return;
   }
   for (size_t i = 0; i < v.size(); ++i) {
-    out[off + i].re = (float)v[i].real();
-    out[off + i].im = (float)v[i].imag();
+    out[off + i].re = snapped(v[i].real());
+    out[off + i].im = snapped(v[i].imag());
   }
 }
 
@@ -350,3 +369,29 @@ extern "C" int gbq_pool_build(const int32_t* prog, int64_t prog_len, const doubl
   }
   return (r.ok && ok) ? GBQ_OK : GBQ_ERR_ARG;
 }
+
+extern "C" int gbq_pool_build_points(const int32_t* prog, int64_t prog_len, const double* gates, int64_t gate_stride,
+                                     const int64_t* gate_off, const int32_t* gate_dim, int ngates, int npoints,
+                                     gbq_c64* out, int64_t pool_len, int nthreads) {
+  if (npoints < 0 || gate_stride < 0 || (npoints && !out) || (npoints && ngates && !gates)) return GBQ_ERR_ARG;
+  if (npoints == 0) return GBQ_OK;
+  int nt = nthreads > 0 ? nthreads : (int)std::thread::hardware_concurrency();
+  nt = std::max(1, std::min({nt, npoints, 64}));
+  std::atomic<int> next{0};
+  std::atomic<int> rc{GBQ_OK};
+  auto work = [&]() {
+    for (;;) {
+      const int p = next.fetch_add(1);
+      if (p >= npoints || rc.load() != GBQ_OK) break;
+      const int r = gbq_pool_build(prog, prog_len, gates + 2 * gate_stride * (int64_t)p, gate_off, gate_dim, ngates,
+                                   out + pool_len * (int64_t)p, pool_len);
+      if (r != GBQ_OK) rc.store(r);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  return rc.load();
+}
+

@@ -346,9 +346,10 @@ class Plan:
         self.__dict__["_native_prog"] = prog
         return prog
 
-    def _native_pool(self, gates: dict) -> np.ndarray | None:
-        """The pool of one point through gbq_pool_build (None if the library
-        cannot be loaded)."""
+    def _native_pool(self, gates: dict, npoints: int = 1) -> np.ndarray | None:
+        """The pools of `npoints` points through gbq_pool_build (one point)
+        or gbq_pool_build_points (host threads over the points); None if the
+        library cannot be loaded."""
         try:
             lib = _lib.load()
         except Exception:  # noqa: BLE001  (no engine: the numpy replay runs)
@@ -372,20 +373,34 @@ class Plan:
                 dims[idx] = d
                 offs[idx] = at + np.arange(len(gis), dtype=np.int64) * (d * d)
                 at += len(gis) * d * d
-            grp = (list(by_dim.values()), dims, offs, ng)
+            grp = (list(by_dim.items()), dims, offs, ng)
             if len(groups_cache) >= 8:
                 groups_cache.clear()
             groups_cache[key] = grp
         order, dims, offs, ng = grp
-        blocks = [np.concatenate([gates[gi][:1] for gi in gis]).astype(np.complex128, copy=False).reshape(-1)
-                  for gis in order]
-        flat = np.ascontiguousarray(np.concatenate(blocks)) if blocks else np.zeros(1, np.complex128)
-        out = np.zeros((1, self.pool_len), dtype=np.complex64)
-        rc = lib.gbq_pool_build(prog.ctypes.data, len(prog), flat.ctypes.data, offs.ctypes.data, dims.ctypes.data,
-                                ng, out.ctypes.data, self.pool_len)
+        if npoints == 1:
+            blocks = [np.concatenate([gates[gi][:1] for gi in gis]).astype(np.complex128, copy=False).reshape(-1)
+                      for _, gis in order]
+            flat = np.ascontiguousarray(np.concatenate(blocks)) if blocks else np.zeros(1, np.complex128)
+            out = np.zeros((1, self.pool_len), dtype=np.complex64)
+            rc = lib.gbq_pool_build(prog.ctypes.data, len(prog), flat.ctypes.data, offs.ctypes.data, dims.ctypes.data,
+                                    ng, out.ctypes.data, self.pool_len)
+        else:
+            # (points, gate elements): each size group's (P, d, d) matrices side
+            # by side, in the order of the one-point layout
+            blocks = [np.stack([np.broadcast_to(gates[gi], (npoints, d, d)) for gi in gis], axis=1)
+                      .reshape(npoints, -1) for d, gis in order]
+            if blocks:
+                flat = np.ascontiguousarray(np.concatenate(blocks, axis=1), dtype=np.complex128)
+            else:
+                flat = np.zeros((npoints, 1), np.complex128)
+            out = np.zeros((npoints, self.pool_len), dtype=np.complex64)
+            rc = lib.gbq_pool_build_points(prog.ctypes.data, len(prog), flat.ctypes.data, flat.shape[1],
+                                           offs.ctypes.data, dims.ctypes.data, ng, npoints, out.ctypes.data,
+                                           self.pool_len, 0)
         if rc != 0:
             raise ValueError("gbq_pool_build rejected the plan's recipes")
-        return _snap(out)
+        return out  # snapped by the builder
 
     def pool_for(self, gates: dict, npoints: int, codes: dict | None = None) -> np.ndarray:
         """Recomputes the matrix pool for a batch: gates[gi] is (P, d, d).
@@ -396,11 +411,14 @@ class Plan:
         count as equal everywhere.  Each op is then built once per distinct
         combination of its gates and gathered to the points.
 
-        Returns complex64 (P, pool_len).  One point runs natively
-        (gbq_pool_build): the same steps as plain loops.
+        Returns complex64 (P, pool_len).  Without `codes` the points run
+        natively (gbq_pool_build / gbq_pool_build_points, the same steps as
+        plain loops, host threads over the points).
         """
-        if npoints == 1 and NATIVE_POOLS:
-            pool = self._native_pool(gates)
+        if NATIVE_POOLS and (npoints == 1 or codes is None):
+            # trajectory batches (codes) keep the replay below, which builds
+            # each op once per distinct combination of drawn unitaries
+            pool = self._native_pool(gates, npoints)
             if pool is not None:
                 return pool
         out = np.zeros((npoints, self.pool_len), dtype=np.complex64)

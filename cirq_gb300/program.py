@@ -169,11 +169,15 @@ def _linear_exponents(exprs):
     return syms, index, coef, div, const
 
 
+# values that ParamResolver.value_of returns as the same number
+_PLAIN_NUMBERS = frozenset({float, int, np.float64, np.float32, np.int64, np.int32})
+
+
 def _symbol_values(syms, resolvers) -> np.ndarray:
     """(len(syms), P) values of plain symbols.  A symbol whose name maps to a
-    float or int in the resolver's dictionary takes that number (what
-    ParamResolver.value_of returns for it); anything else goes through
-    value_of."""
+    float or int (Python or numpy) in the resolver's dictionary takes that
+    number (what ParamResolver.value_of returns for it); anything else goes
+    through value_of."""
     import sympy
 
     out = np.empty((len(syms), len(resolvers)))
@@ -181,7 +185,7 @@ def _symbol_values(syms, resolvers) -> np.ndarray:
         byname = {(k.name if isinstance(k, sympy.Symbol) else k): v for k, v in r.param_dict.items()}
         for j, sym in enumerate(syms):
             v = byname.get(sym.name)
-            if type(v) is float or type(v) is int:
+            if type(v) in _PLAIN_NUMBERS:
                 out[j, p] = v
             else:
                 out[j, p] = float(r.value_of(sym))
@@ -492,7 +496,9 @@ class CompiledCircuit:
                 for sym, row in zip(syms, sv):
                     values[sym] = row
             phase = np.exp(1j * np.pi * T[:, :, None] * H[:, None, :])  # (S, P, K)
-            M = np.einsum("spk,skij->spij", phase, Pm)
+            S_, K_, d_ = Pm.shape[0], Pm.shape[1], Pm.shape[-1]
+            # sum_k phase_k P_k as one batched product (S, P, K) @ (S, K, d*d)
+            M = np.matmul(phase, Pm.reshape(S_, K_, d_ * d_)).reshape(S_, phase.shape[1], d_, d_)
             if conj.any():
                 M[conj] = np.conjugate(M[conj])
             for j, i in enumerate(idx):

@@ -145,11 +145,18 @@ int gbq_launch_count(gbq_ctx* ctx, int64_t* out);
  * cirq_gb300/csrc/gbq_pool.cu), `gates` the point's gate matrices as
  * complex128 (gate g at element gate_off[g], gate_dim[g] x gate_dim[g],
  * row-major).  out receives pool_len complex64 entries (zero where no op
- * writes).  Replaces the per-point replay of the planner's fusion recipes;
+ * writes; real and imaginary parts below 1e-12 in magnitude stored as 0).  Replaces the per-point replay of the planner's fusion recipes;
  * the fused ops themselves replace the reference's per-gate
  * apply_unitary calls (cirq-core/cirq/protocols/apply_unitary_protocol.py:306-418). */
 int gbq_pool_build(const int32_t* prog, int64_t prog_len, const double* gates, const int64_t* gate_off,
                    const int32_t* gate_dim, int ngates, gbq_c64* out, int64_t pool_len);
+/* gbq_pool_build for npoints points: point p's gates start gate_stride
+ * complex128 elements after point p-1's (same gate_off / gate_dim), its pool
+ * at out + p * pool_len.  Points run on nthreads host threads (0: one per
+ * hardware thread); the first error code is returned. */
+int gbq_pool_build_points(const int32_t* prog, int64_t prog_len, const double* gates, int64_t gate_stride,
+                          const int64_t* gate_off, const int32_t* gate_dim, int ngates, int npoints,
+                          gbq_c64* out, int64_t pool_len, int nthreads);
 
 /* ---- Clifford circuits: reference tableau run + Pauli-frame shots ---------
  * Replaces the reference's per-repetition stabilizer simulation
