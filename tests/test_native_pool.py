@@ -68,3 +68,28 @@ def test_adjoint_reverse_program_with_probes():
     gates = prog.forward.gate_batch([r])
     batch = prog._reverse_batch(r, gates)
     _check(prog.reverse, batch)
+
+
+def test_points_match_one_point_builds_and_the_numpy_batch_replay():
+    # gbq_pool_build_points on host threads: every point's pool equals the
+    # one-point build bit for bit, and the numpy replay of the whole batch
+    # to float32 rounding
+    c, gammas, betas, _, _ = workloads.qaoa_circuit(14, 3, seed=5)
+    rng = np.random.default_rng(3)
+    res = [cirq.ParamResolver({**{g: float(rng.uniform(-1, 1)) for g in gammas},
+                               **{b: np.float64(rng.uniform(-1, 1)) for b in betas}}) for _ in range(37)]
+    cc = _compiled(c, Planner(budget=25.0), resolvers=res[:1])
+    gates = cc.gate_batch(res)
+    g = {i: gates[j] for i, j in enumerate(cc.kept)}
+    plan = cc.plan
+    many = plan._native_pool(g, len(res))
+    for p in range(len(res)):
+        one = plan._native_pool({k: v[p : p + 1] for k, v in g.items()}, 1)
+        assert np.array_equal(many[p : p + 1].view(np.uint32), one.view(np.uint32)), p
+    P.NATIVE_POOLS = False
+    try:
+        ref = plan.pool_for(g, len(res))
+    finally:
+        P.NATIVE_POOLS = True
+    assert np.allclose(many, ref, rtol=2e-7, atol=1e-7)
+    assert np.array_equal(plan.pool_for(g, len(res)), many)  # pool_for takes the native route
