@@ -42,6 +42,13 @@ namespace {
 
 using cd = std::complex<double>;
 
+// (a.re b.re - a.im b.im, a.re b.im + a.im b.re): the value std::complex's
+// operator* returns for finite operands, without its library call for the
+// infinite / NaN cases (every pool entry is finite)
+static inline cd cmul(const cd& a, const cd& b) {
+  return cd(a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real());
+}
+
 struct Gates {
   const cd* base;
   const int64_t* off;
@@ -100,7 +107,7 @@ static void run_diag_steps(Reader& r, int nsteps, const Gates& g, std::vector<cd
         int sub = 0;
         for (int i = 0; i < np; ++i) sub |= (int)((x >> pos[i]) & 1) << i;
         if (sub >= dg) return void(r.ok = false);
-        D[x] *= G[(int64_t)sub * dg + sub];
+        D[x] = cmul(D[x], G[(int64_t)sub * dg + sub]);
       }
     } else {
       r.ok = false;
@@ -192,12 +199,21 @@ static void run_dense_steps(Reader& r, int nsteps, const Gates& g, Dense& M) {
         for (int sx = 0; sx < M.ns; ++sx) {
           const cd* m = &M.m[(size_t)sx * d * d];
           cd* o = &out[(size_t)sx * d * d];
-          for (int a = 0; a < d; ++a)
+          // F[a][b] is zero unless a and b agree outside the gate's bits:
+          // sum only those b (ascending, as a dense product would), which
+          // leaves out exact-zero terms alone
+          for (int a = 0; a < d; ++a) {
+            const int base = a & ~mask;
             for (int c = 0; c < d; ++c) {
               cd acc(0.0, 0.0);
-              for (int b = 0; b < d; ++b) acc += F[(size_t)a * d + b] * m[(size_t)b * d + c];
+              for (int t = 0;; t = (t - mask) & mask) {
+                const int b = base | t;
+                acc += cmul(F[(size_t)a * d + b], m[(size_t)b * d + c]);
+                if (t == mask) break;
+              }
               o[(size_t)a * d + c] = acc;
             }
+          }
         }
         M.m.swap(out);
         break;
@@ -220,7 +236,7 @@ static void run_dense_steps(Reader& r, int nsteps, const Gates& g, Dense& M) {
             if (v >= dg) return void(r.ok = false);
             const cd f = G[(int64_t)v * dg + v];
             cd* row = &M.m[((size_t)sx * d + a) * d];
-            for (int c = 0; c < d; ++c) row[c] *= f;
+            for (int c = 0; c < d; ++c) row[c] = cmul(row[c], f);
           }
         break;
       }
