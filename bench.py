@@ -577,7 +577,7 @@ def batch_bench(points: int = 4096, widths=(16, 18, 20, 22), p: int = 4):
     }
 
 
-def clifford_bench(n: int = 500, depth: int = 100, shots: int = 1_000_000, ref_shots: int = 3):
+def clifford_bench(n: int = 500, depth: int = 100, shots: int = 1_000_000, ref_shots: int = 1):
     """Clifford sampling: a random Clifford circuit of n qubits and depth
     layers with a mid-circuit measurement and reset every layer, depolarizing
     noise and a final measurement of every qubit, sampled `shots` times by
